@@ -1,0 +1,162 @@
+/*
+ * qgb.h -- C ABI of the GB300 (sm_103a) gate-application engine.
+ *
+ * Plain C: pointers, sizes and a CUDA stream passed as `void*` (a
+ * cudaStream_t; NULL = legacy default stream). No allocation of state happens
+ * behind these calls: every state, matrix and scratch buffer is owned by the
+ * caller (in the Python host layer: torch's caching allocator). Every entry
+ * point is asynchronous on `stream`, returns 0 on success or a negative
+ * QGB_E* code, and leaves a message for qgb_last_error() (thread-local).
+ * Argument errors are detected on the host before any launch.
+ *
+ * State layout (the reference's convention): a state of n qubits is 2^n
+ * interleaved complex numbers (float2 for QGB_C64, double2 for QGB_C128);
+ * site q is bit (n-1-q) of the flat index (site 0 is the most significant
+ * axis of the reference's reshape([2]*n), tensorQ/statevector_sim.py:36,47).
+ * A gate on sites `indices[0..k)` carries a row-major 2^k x 2^k matrix whose
+ * row/column bit (k-1-j) belongs to indices[j] (tensorQ/statevector_sim.py:124-140).
+ * A density matrix of n qubits is vec(rho) of 4^n entries, row (ket) index
+ * in the high n bits, column (bra) index in the low n bits
+ * (tensorQ/density_matrix_sim.py:12-42).
+ */
+#ifndef QGB_H
+#define QGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QGB_ABI_VERSION 1
+
+enum { QGB_C64 = 0, QGB_C128 = 1 };
+
+enum {
+    QGB_OK = 0,
+    QGB_EINVAL = -1,   /* bad argument, detected on the host before launch */
+    QGB_ECUDA = -2,    /* CUDA runtime error (launch or attribute call)      */
+    QGB_ETIMEOUT = -3, /* a bounded device-side wait ran out                 */
+    QGB_ESCRATCH = -4  /* scratch buffer too small (size query: qgb_*_scratch_bytes) */
+};
+
+#define QGB_MAX_QUBITS 34       /* 2^34 c64 amplitudes = 128 GiB */
+#define QGB_MAX_K 6             /* largest dense gate (64 x 64)  */
+#define QGB_SWEEP_MAX_OPS 64
+#define QGB_SWEEP_MAX_HIGH 10
+#define QGB_SWEEP_MAX_TILE_BITS 14
+
+/* One fused pass over the state: a tile of 2^(low_bits + n_high) amplitudes
+ * (flat bits [0, low_bits) plus the listed high bits) is staged in shared
+ * memory, every op is applied to it in order, and it is written back.
+ * op_pos[i][j] is the tile-local bit (0 .. low_bits+n_high-1) of matrix bit
+ * (k-1-j); tile bit low_bits+h is flat bit high_bits[h]. op_mat[i] is the
+ * element offset of op i's 2^k x 2^k matrix in the `mats` buffer. */
+typedef struct {
+    int32_t low_bits;
+    int32_t n_high;
+    int32_t high_bits[QGB_SWEEP_MAX_HIGH];
+    int32_t n_ops;
+    int32_t op_k[QGB_SWEEP_MAX_OPS];
+    int32_t op_pos[QGB_SWEEP_MAX_OPS][QGB_MAX_K];
+    int64_t op_mat[QGB_SWEEP_MAX_OPS];
+} qgb_sweep;
+
+int qgb_abi_version(void);
+const char* qgb_last_error(void);
+/* Reads and clears the device status word set by bounded waits; returns
+ * QGB_OK or QGB_ETIMEOUT. Synchronises `stream`. */
+int qgb_check_status(void* stream);
+
+/* ---- statevector ------------------------------------------------------ */
+
+/* Replaces op_action (tensorQ/statevector_sim.py:124-140) as called by
+ * StatevectorSim.apply_gate (:50-52): sv <- op on sites indices[0..k).
+ * `op` is a device pointer to the 2^k x 2^k matrix in the state's dtype.
+ * batch > 1 applies to `batch` states spaced sv_stride elements apart, each
+ * with its own matrix spaced op_stride elements apart (0 = shared matrix). */
+int qgb_op_action(void* sv, int dtype, int n, const int* indices, int k, const void* op,
+                  int64_t op_stride, int64_t batch, int64_t sv_stride, void* stream);
+
+/* A fused pass (several gates per read+write of the state), planned by the
+ * host compiler from a Circuit's gate list (core/base_sim.py:30-53 loop). */
+int qgb_apply_sweep(void* sv, int dtype, int n, const qgb_sweep* sweep, const void* mats,
+                    int64_t mat_stride, int64_t batch, int64_t sv_stride, void* stream);
+
+/* Writes |bits> (StatevectorSim.initialize_state, :31-48) to `batch` states. */
+int qgb_init_basis(void* sv, int dtype, int n, uint64_t index, int64_t batch, int64_t sv_stride,
+                   void* stream);
+
+/* sv *= scale[b] for every state b (scale: device, float64, one per state). */
+int qgb_scale(void* sv, int dtype, int n, const double* scale, int64_t batch, int64_t sv_stride,
+              void* stream);
+
+/* Scratch bytes needed by the reductions below for a given problem. */
+size_t qgb_reduce_scratch_bytes(int n, int nterms, int64_t batch);
+
+/* out[b] = ||sv_b||^2 in float64 (normalize_state, :107-109). */
+int qgb_norm2(const void* sv, int dtype, int n, int64_t batch, int64_t sv_stride, double* out,
+              void* scratch, size_t scratch_bytes, void* stream);
+
+/* Replaces pauli_expectation_sv (tensorQ/statevector_sim.py:217-234):
+ * out[b * nterms + t] = coeff[t] * <sv_b| P_t |sv_b> accumulated in float64.
+ * `paulis` holds nterms strings of n characters 'i','x','y','z' and `coeff`
+ * nterms weights (both host memory; coeff may be NULL for weights of 1). */
+int qgb_pauli_expectation(const void* sv, int dtype, int n, const char* paulis, const double* coeff,
+                          int nterms, int64_t batch, int64_t sv_stride, double* out, void* scratch,
+                          size_t scratch_bytes, void* stream);
+
+/* <a_b|b_b> = sum conj(a) b for every state b: out[2b], out[2b+1] = real,
+ * imaginary part (float64). With b = (x)_q O_q a it gives
+ * StatevectorSim.local_expectation / one_local_expectation (:63-73, :81-94). */
+int qgb_inner_product(const void* a, const void* b, int dtype, int n, int64_t batch, int64_t stride, double* out,
+                      void* scratch, size_t scratch_bytes, void* stream);
+
+/* out = sum_t coeff[t] P_t sv  (H|psi> for the adjoint start); out and sv
+ * distinct buffers of the same shape; paulis and coeff in host memory, at most
+ * 128 terms. */
+int qgb_pauli_apply(const void* sv, void* out, int dtype, int n, const char* paulis,
+                    const double* coeff, int nterms, int64_t batch, int64_t sv_stride, void* stream);
+
+/* Replaces partial_overlap (tensorQ/statevector_sim.py:155-180) on sites
+ * indices[0..k): out[b, r, c] = sum_rest a_b[r, rest] conj(b_b[c, rest]),
+ * rows/cols ordered by `indices` as a gate matrix; float64 complex out
+ * (device, batch * 4^k double2). */
+int qgb_partial_overlap(const void* a, const void* b, int dtype, int n, const int* indices, int k,
+                        int64_t batch, int64_t sv_stride, double* out, void* scratch,
+                        size_t scratch_bytes, void* stream);
+
+/* ---- density matrix ---------------------------------------------------- */
+
+/* Replaces DensityMatrixSim.apply_gate (tensorQ/density_matrix_sim.py:38-42)
+ * for a superoperator given in the reference's to_superop() layout
+ * (core/gates.py:43-44, core/noise.py:10-13): a row-major 4^k x 4^k matrix
+ * whose row/col bits are (bra sites.., ket sites..) in `indices` order.
+ * Applied to vec(rho) of n qubits (4^n entries). Input legs follow
+ * `indices`; output legs follow ascending site order, exactly as the
+ * reference's generate_gate_indices (:91-99) assigns them. */
+int qgb_dm_apply_superop(void* rho, int dtype, int n, const int* indices, int k,
+                         const void* superop, int64_t batch, int64_t rho_stride, void* stream);
+
+/* out[b * nterms + t] = coeff[t] * Tr(rho_b P_t) for Pauli strings (float64;
+ * paulis and coeff in host memory). */
+int qgb_dm_pauli_expectation(const void* rho, int dtype, int n, const char* paulis,
+                             const double* coeff, int nterms, int64_t batch, int64_t rho_stride,
+                             double* out, void* scratch, size_t scratch_bytes, void* stream);
+
+/* out[b] = Re Tr((x)_q O_q rho_b) for single-site operators (host, n 2x2
+ * complex128 row-major) -- DensityMatrixSim.local_expectation /
+ * one_local_expectation (:49-70). */
+int qgb_dm_product_expectation(const void* rho, int dtype, int n, const double* ops, int64_t batch,
+                               int64_t rho_stride, double* out, void* scratch, size_t scratch_bytes,
+                               void* stream);
+
+/* out[b] = Re Tr(rho_b) (float64) -- normalize_state (:85-89). */
+int qgb_dm_trace(const void* rho, int dtype, int n, int64_t batch, int64_t rho_stride, double* out,
+                 void* scratch, size_t scratch_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QGB_H */

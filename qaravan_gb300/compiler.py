@@ -1,0 +1,252 @@
+"""Circuit compiler: gate fusion and tile-sweep planning.
+
+The reference applies gates one at a time, layer by layer (``BaseSim.run``,
+``core/base_sim.py:30-53``), each as a full contraction over the state
+(``op_action``, ``tensorQ/statevector_sim.py:124-140``). This compiler turns
+the same op sequence into fewer passes over HBM:
+
+1. **Fusion** (``fuse``): ops are merged into dense blocks of at most ``width``
+   bits. An op joins the latest block it depends on when the union of their
+   bits stays within ``width`` (it commutes past every later block, which by
+   construction shares no bit with it); earlier blocks whose bits are covered
+   and that nothing in between touches are then absorbed too, which folds
+   single-qubit layers into the neighbouring two-qubit gates. Matrices are
+   composed on the host in complex128.
+2. **Sweep planning** (``plan_sweeps``): consecutive blocks are grouped into
+   sweeps whose bits fit one shared-memory tile (the low ``L`` flat bits plus up
+   to ``H`` chosen high bits). A block is skipped -- and every later block
+   touching its bits with it -- when the tile cannot take its bits, so blocks
+   only move past blocks they commute with.
+
+Ops are ``(bits, matrix)`` with flat bit positions in matrix order (bit
+``bits[j]`` is matrix-index bit ``k-1-j``); for a statevector of ``n`` qubits,
+site ``q`` is bit ``n-1-q``.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from ._lib import QGB_SWEEP_MAX_HIGH, QGB_SWEEP_MAX_OPS, QGB_SWEEP_MAX_TILE_BITS
+
+
+@dataclass
+class Op:
+    bits: list
+    matrix: np.ndarray  # complex128, 2^k x 2^k
+    kind: str = "unitary"  # "unitary" | "nonunitary"
+
+
+@dataclass
+class DenseStep:
+    bits: list
+    mat: int  # index into the plan's matrix list
+
+
+@dataclass
+class SweepStep:
+    low_bits: int
+    high_bits: list
+    ops: list  # (tile-local positions in matrix order, matrix index)
+
+
+@dataclass
+class NormalizeStep:
+    pass
+
+
+@dataclass
+class Plan:
+    nbits: int
+    steps: list = field(default_factory=list)
+    matrices: list = field(default_factory=list)  # complex128 arrays
+    n_gates: int = 0  # original op count
+
+    def add_matrix(self, m):
+        self.matrices.append(np.ascontiguousarray(m, dtype=np.complex128))
+        return len(self.matrices) - 1
+
+    @property
+    def n_sweeps(self):
+        return sum(1 for s in self.steps if isinstance(s, (DenseStep, SweepStep)))
+
+
+# ----------------------------------------------------------------- algebra
+
+def embed(mat, bits, target):
+    """Matrix of ``mat`` (acting on ``bits``) on the larger bit list ``target``."""
+    bits, target = list(bits), list(target)
+    K, k = len(target), len(bits)
+    if bits == target:
+        return np.asarray(mat, dtype=np.complex128)
+    pos = [target.index(b) for b in bits]  # position j in target order (0 = MSB)
+    idx = np.arange(2 ** K)
+    sub = np.zeros(2 ** K, dtype=np.int64)
+    for j, p in enumerate(pos):
+        sub |= ((idx >> (K - 1 - p)) & 1) << (k - 1 - j)
+    other_mask = 0
+    for p in range(K):
+        if p not in pos:
+            other_mask |= 1 << (K - 1 - p)
+    rest = idx & other_mask
+    same = rest[:, None] == rest[None, :]
+    full = np.where(same, np.asarray(mat, dtype=np.complex128)[sub[:, None], sub[None, :]], 0)
+    return full
+
+
+def _union(a, b):
+    out = list(a)
+    for x in b:
+        if x not in out:
+            out.append(x)
+    return out
+
+
+# ------------------------------------------------------------------ fusion
+
+@dataclass
+class Block:
+    bits: list
+    matrix: np.ndarray
+    n_ops: int = 1
+
+
+def fuse(ops, width):
+    """Greedy order-preserving fusion into blocks of at most ``width`` bits."""
+    blocks: list = []
+    last: dict = {}  # bit -> index of the latest block touching it
+    for op in ops:
+        bits = list(op.bits)
+        if len(bits) > width:
+            raise ValueError(f"op on {len(bits)} bits exceeds fusion width {width}")
+        deps = [last[b] for b in bits if b in last]
+        cand = max(deps) if deps else None
+        if cand is not None and blocks[cand] is not None and len(_union(blocks[cand].bits, bits)) <= width:
+            blk = blocks[cand]
+            u = sorted(_union(blk.bits, bits), reverse=True)
+            blk.matrix = embed(op.matrix, bits, u) @ embed(blk.matrix, blk.bits, u)
+            blk.bits = u
+            blk.n_ops += 1
+            for b in bits:
+                last[b] = cand
+            # absorb earlier blocks covered by the union with nothing in between touching them
+            for j in sorted({d for d in deps if d != cand}, reverse=True):
+                bj = blocks[j]
+                if bj is None or not set(bj.bits) <= set(u):
+                    continue
+                if any(blocks[i] is not None and set(blocks[i].bits) & set(bj.bits) for i in range(j + 1, cand)):
+                    continue
+                blk.matrix = blk.matrix @ embed(bj.matrix, bj.bits, u)
+                blk.n_ops += bj.n_ops
+                blocks[j] = None
+                for b in bj.bits:
+                    if last.get(b) == j:
+                        last[b] = cand
+            continue
+        blocks.append(Block(sorted(bits, reverse=True) if len(bits) > 1 else list(bits),
+                            embed(op.matrix, bits, sorted(bits, reverse=True)), 1))
+        for b in bits:
+            last[b] = len(blocks) - 1
+    return [b for b in blocks if b is not None]
+
+
+# --------------------------------------------------------- sweep planning
+
+def plan_sweeps(blocks, nbits, tile_bits, low_bits=None, max_high=QGB_SWEEP_MAX_HIGH):
+    """Group blocks into tile sweeps; returns a list of (low_bits, high_bits, [blocks])."""
+    m = min(tile_bits, nbits, QGB_SWEEP_MAX_TILE_BITS)
+    L = min(5 if low_bits is None else low_bits, m)
+    if m == nbits:
+        L = nbits
+    H = m - L
+    if H > max_high:
+        H = max_high
+        L = m - H
+    widest = max((len(b.bits) for b in blocks), default=1)
+    if m < nbits and H < widest:  # the tile must take any single block's bits
+        H = min(widest, max_high, m - 1)
+        L = m - H
+    remaining = list(blocks)
+    sweeps = []
+    while remaining:
+        high: list = []
+        taken, rest = [], []
+        blocked: set = set()
+        for blk in remaining:
+            bset = set(blk.bits)
+            if bset & blocked or len(taken) >= QGB_SWEEP_MAX_OPS:
+                blocked |= bset
+                rest.append(blk)
+                continue
+            need = [b for b in blk.bits if b >= L and b not in high]
+            if len(high) + len(need) <= H:
+                high.extend(need)
+                taken.append(blk)
+            else:
+                blocked |= bset
+                rest.append(blk)
+        if not taken:
+            raise RuntimeError("sweep planner made no progress (block wider than the tile)")
+        sweeps.append((L, sorted(high), taken))
+        remaining = rest
+    return sweeps
+
+
+# ------------------------------------------------------------------- plans
+
+def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, max_sweep_k=5):
+    """Compile an op sequence (with ``None`` marking a renormalisation point)
+    into a :class:`Plan`.
+
+    ``mode``: ``"gate"`` one pass per op; ``"fused"`` one pass per fused block of
+    ``width`` bits; ``"sweep"`` fused blocks grouped into shared-memory tile sweeps.
+    """
+    plan = Plan(nbits=nbits, n_gates=sum(1 for o in ops if o is not None))
+    segments, cur = [], []
+    for o in ops:
+        if o is None:
+            segments.append(cur)
+            segments.append(None)
+            cur = []
+        else:
+            cur.append(o)
+    segments.append(cur)
+    for seg in segments:
+        if seg is None:
+            plan.steps.append(NormalizeStep())
+            continue
+        if not seg:
+            continue
+        if mode == "gate":
+            for o in seg:
+                plan.steps.append(DenseStep(list(o.bits), plan.add_matrix(o.matrix)))
+            continue
+        w = max(width, max(len(o.bits) for o in seg))
+        blocks = fuse(seg, w)
+        if mode == "fused" or w > max_sweep_k or tile_bits <= 0:
+            for b in blocks:
+                plan.steps.append(DenseStep(list(b.bits), plan.add_matrix(b.matrix)))
+            continue
+        for L, high, taken in plan_sweeps(blocks, nbits, tile_bits, low_bits):
+            tpos = {b: b for b in range(L)}
+            for h, b in enumerate(high):
+                tpos[b] = L + h
+            sops = [([tpos[b] for b in blk.bits], plan.add_matrix(blk.matrix)) for blk in taken]
+            plan.steps.append(SweepStep(L, list(high), sops))
+    return plan
+
+
+def plan_flops(plan):
+    """(algorithmic bytes, flops) per vector element summed over passes: bytes
+    are two vector passes (read + write) per dense/sweep step; flops are
+    8 * 2^k per element per dense op of width k."""
+    passes, flops = 0, 0
+    for s in plan.steps:
+        if isinstance(s, DenseStep):
+            passes += 1
+            flops += 8 * 2 ** len(s.bits)
+        elif isinstance(s, SweepStep):
+            passes += 1
+            flops += sum(8 * 2 ** len(p) for p, _ in s.ops)
+    return passes, flops

@@ -1,0 +1,65 @@
+// C ABI plumbing: version, thread-local last error, launch checks, the device
+// status word of bounded waits.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+
+#include "qgb_common.cuh"
+
+namespace qgb {
+__device__ int g_status = 0;
+}
+
+namespace {
+thread_local char g_last_error[512] = "";
+}
+
+namespace qgb_host {
+
+int set_error(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int check_launch(const char* what) {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(QGB_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+    return QGB_OK;
+}
+
+int sm_count() {
+    static int cached = 0;
+    if (cached == 0) {
+        int dev = 0, v = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0)
+            cached = v;
+        else
+            cached = 148;
+    }
+    return cached;
+}
+
+}  // namespace qgb_host
+
+extern "C" int qgb_abi_version(void) { return QGB_ABI_VERSION; }
+
+extern "C" const char* qgb_last_error(void) { return g_last_error; }
+
+extern "C" int qgb_check_status(void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return qgb_host::set_error(QGB_ECUDA, "stream sync: %s", cudaGetErrorString(e));
+    int status = 0;
+    e = cudaMemcpyFromSymbol(&status, qgb::g_status, sizeof(int));
+    if (e != cudaSuccess) return qgb_host::set_error(QGB_ECUDA, "status read: %s", cudaGetErrorString(e));
+    if (status != 0) {
+        const int zero = 0;
+        cudaMemcpyToSymbol(qgb::g_status, &zero, sizeof(int));
+        return qgb_host::set_error(QGB_ETIMEOUT, "a bounded device wait gave up (code %d)", status);
+    }
+    return QGB_OK;
+}

@@ -1,0 +1,70 @@
+// Shared device/host helpers of the gate-application engine (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/qgb.h"
+
+namespace qgb {
+
+template <typename T> struct CplxOf;
+template <> struct CplxOf<float> { using type = float2; };
+template <> struct CplxOf<double> { using type = double2; };
+template <typename T> using cplx = typename CplxOf<T>::type;
+
+template <typename T> __host__ __device__ __forceinline__ cplx<T> mk(T re, T im) {
+    cplx<T> r;
+    r.x = re;
+    r.y = im;
+    return r;
+}
+
+// acc += a * b (complex), four fused multiply-adds.
+template <typename C> __device__ __forceinline__ void cfma(C& acc, const C& a, const C& b) {
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(-a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(a.y, b.x, acc.y);
+}
+
+// Insert a zero at each (ascending) bit position of `sorted_bits`.
+__device__ __forceinline__ uint64_t insert_zeros(uint64_t g, const int* sorted_bits, int k) {
+#pragma unroll 6
+    for (int j = 0; j < k; ++j) {
+        const int b = sorted_bits[j];
+        const uint64_t lo = g & ((uint64_t(1) << b) - 1);
+        g = ((g >> b) << (b + 1)) | lo;
+    }
+    return g;
+}
+
+// Scatter the low bits of `v` to the listed bit positions (ascending list).
+__device__ __forceinline__ uint64_t scatter_bits(uint64_t v, const int* bits, int nb) {
+    uint64_t out = 0;
+    for (int j = 0; j < nb; ++j) out |= ((v >> j) & 1ull) << bits[j];
+    return out;
+}
+
+// Offset of matrix row/column r in the state: bit (k-1-j) of r goes to bit pos[j].
+__host__ __device__ __forceinline__ uint64_t matrix_offset(int r, const int* pos, int k) {
+    uint64_t off = 0;
+    for (int j = 0; j < k; ++j) off |= uint64_t((r >> (k - 1 - j)) & 1) << pos[j];
+    return off;
+}
+
+// Shared-memory swizzle for a staged tile, on 16-byte granules: the 16-byte
+// chunk index has bits 3..5 XORed into bits 0..2, which spreads the amplitudes
+// a warp touches over the 32 banks when the gate acts on the tile's low bits.
+template <typename T> __device__ __forceinline__ uint32_t swz(uint32_t e);
+template <> __device__ __forceinline__ uint32_t swz<float>(uint32_t e) { return e ^ (((e >> 4) & 7u) << 1); }
+template <> __device__ __forceinline__ uint32_t swz<double>(uint32_t e) { return e ^ ((e >> 3) & 7u); }
+
+}  // namespace qgb
+
+// ---- host-side helpers shared by the translation units -------------------
+namespace qgb_host {
+int set_error(int code, const char* fmt, ...);
+int check_launch(const char* what);
+int sm_count();
+}  // namespace qgb_host

@@ -1,0 +1,567 @@
+// Expectation values and other reductions, accumulated in float64.
+//
+// Replaces the reference's ncon-based reductions (pauli_expectation_sv,
+// tensorQ/statevector_sim.py:217-234; local/one_local_expectation :63-94;
+// partial_overlap :155-180; DensityMatrixSim expectations and trace,
+// tensorQ/density_matrix_sim.py:49-89). Each reduction reads the state once
+// per group of terms, keeps per-thread float64 sums, reduces a block in a
+// fixed shuffle order, writes one partial per block into caller-provided
+// scratch, and a second kernel sums the partials in a fixed order, so the
+// result is bitwise reproducible run to run.
+#include <cstring>
+#include <vector>
+
+#include "qgb_common.cuh"
+
+namespace qgb {
+
+constexpr int kRedThreads = 256;
+
+// Blocks per vector for a reduction over 2^nbits entries (independent of the
+// device, so the scratch size is a pure function of the problem).
+__host__ __device__ inline int red_blocks(int nbits) {
+    const int64_t len = int64_t(1) << nbits;
+    int64_t b = len / 4096;
+    if (b < 1) b = 1;
+    if (b > 1216) b = 1216;
+    return int(b);
+}
+
+template <int NV>
+__device__ __forceinline__ void block_reduce_store(double (&v)[NV], double* __restrict__ dst, int64_t dst_stride,
+                                                   int nvalid = NV) {
+    __shared__ double red[kRedThreads / 32][NV];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+        double x = v[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) red[warp][j] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < nvalid) {
+        double s = 0;
+        for (int w = 0; w < kRedThreads / 32; ++w) s += red[w][threadIdx.x];
+        dst[int64_t(threadIdx.x) * dst_stride] = s;
+    }
+    __syncthreads();
+}
+
+struct PauliGroup {
+    uint64_t xmask;
+    int nterms;
+    int slot0;  // first output slot of this group
+    uint64_t zmask[32];
+    int ny[32];
+    double coeff[32];
+};
+
+// Re( i^ny * z )
+__device__ __forceinline__ double re_iny(double re, double im, int ny) {
+    switch (ny & 3) {
+        case 0: return re;
+        case 1: return -im;
+        case 2: return -re;
+        default: return im;
+    }
+}
+
+// One pass over the vector for all terms sharing one X mask.
+// partials[(b * nslots + slot) * nblk + blk]
+template <typename T, int NT>
+__global__ void __launch_bounds__(kRedThreads) pauli_group_kernel(const cplx<T>* __restrict__ sv, int n, int64_t sv_stride,
+                                                                  const __grid_constant__ PauliGroup g, int nslots,
+                                                                  double* __restrict__ partials) {
+    const int64_t b = blockIdx.y;
+    const cplx<T>* s = sv + b * sv_stride;
+    const int nblk = gridDim.x;
+    double acc[NT];
+#pragma unroll
+    for (int j = 0; j < NT; ++j) acc[j] = 0.0;
+    const uint64_t stride = uint64_t(nblk) * blockDim.x;
+    if (g.xmask == 0) {
+        const uint64_t len = uint64_t(1) << n;
+        for (uint64_t x = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; x < len; x += stride) {
+            const cplx<T> a = s[x];
+            const double p = double(a.x) * double(a.x) + double(a.y) * double(a.y);
+#pragma unroll
+            for (int j = 0; j < NT; ++j)
+                if (j < g.nterms) acc[j] += (__popcll(x & g.zmask[j]) & 1) ? -p : p;
+        }
+    } else {
+        // visit each pair {x, x ^ xmask} once: x has a zero at the top bit of xmask
+        const int top = 63 - __clzll(g.xmask);
+        const uint64_t half = uint64_t(1) << (n - 1);
+        for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < half; i += stride) {
+            const uint64_t x = ((i >> top) << (top + 1)) | (i & ((uint64_t(1) << top) - 1));
+            const uint64_t y = x ^ g.xmask;
+            const cplx<T> a = s[x], c = s[y];
+            // v = conj(psi[y]) psi[x] contributes at x; conj(v) contributes at y
+            const double vr = double(c.x) * a.x + double(c.y) * a.y;
+            const double vi = double(c.x) * a.y - double(c.y) * a.x;
+#pragma unroll
+            for (int j = 0; j < NT; ++j)
+                if (j < g.nterms) {
+                    const double tx = re_iny(vr, vi, g.ny[j]);
+                    const double ty = re_iny(vr, -vi, g.ny[j]);
+                    acc[j] += ((__popcll(x & g.zmask[j]) & 1) ? -tx : tx) + ((__popcll(y & g.zmask[j]) & 1) ? -ty : ty);
+                }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < NT; ++j) acc[j] *= g.coeff[j < g.nterms ? j : 0];
+    double* dst = partials + (int64_t(b) * nslots + g.slot0) * nblk + blockIdx.x;
+    block_reduce_store<NT>(acc, dst, nblk, g.nterms);
+}
+
+// out[b * nslots + t] = coeff[t] * sum_blk partials[(b * nslots + t) * nblk + blk]
+__global__ void finish_kernel(const double* __restrict__ partials, int nblk, int nslots, int64_t batch,
+                              const double* __restrict__ coeff, double* __restrict__ out) {
+    const int64_t item = int64_t(blockIdx.x) * (blockDim.x / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (item >= batch * nslots) return;
+    const double* p = partials + item * nblk;
+    double s = 0;
+    for (int i = lane; i < nblk; i += 32) s += p[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) out[item] = s * (coeff ? coeff[item % nslots] : 1.0);
+}
+
+// Sum of |v|^2 (slot 0) -- normalize_state.
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) norm2_kernel(const cplx<T>* __restrict__ sv, int n, int64_t sv_stride,
+                                                            double* __restrict__ partials) {
+    const cplx<T>* s = sv + int64_t(blockIdx.y) * sv_stride;
+    const uint64_t len = uint64_t(1) << n, stride = uint64_t(gridDim.x) * blockDim.x;
+    double acc[1] = {0.0};
+    for (uint64_t x = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; x < len; x += stride) {
+        const cplx<T> a = s[x];
+        acc[0] += double(a.x) * a.x + double(a.y) * a.y;
+    }
+    block_reduce_store<1>(acc, partials + int64_t(blockIdx.y) * gridDim.x + blockIdx.x, gridDim.x);
+}
+
+// <a|b> = sum conj(a) b (slots 0, 1 = real, imaginary).
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) inner_kernel(const cplx<T>* __restrict__ a, const cplx<T>* __restrict__ bv,
+                                                            int n, int64_t stride_ab, double* __restrict__ partials) {
+    const int64_t b = blockIdx.y;
+    const cplx<T>* x = a + b * stride_ab;
+    const cplx<T>* y = bv + b * stride_ab;
+    const uint64_t len = uint64_t(1) << n, stride = uint64_t(gridDim.x) * blockDim.x;
+    double acc[2] = {0.0, 0.0};
+    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < len; i += stride) {
+        const cplx<T> u = x[i], v = y[i];
+        acc[0] += double(u.x) * v.x + double(u.y) * v.y;
+        acc[1] += double(u.x) * v.y - double(u.y) * v.x;
+    }
+    block_reduce_store<2>(acc, partials + (b * 2) * gridDim.x + blockIdx.x, gridDim.x);
+}
+
+// Partial overlap on k <= 2 sites: slots 2*(r*D+c) (+1) = re/im of sum a[r,rest] conj(b[c,rest]).
+struct OverlapArgs {
+    int n, k;
+    int sorted[2];
+    uint32_t off[4];
+};
+
+template <typename T, int K>
+__global__ void __launch_bounds__(kRedThreads) overlap_kernel(const cplx<T>* __restrict__ a, const cplx<T>* __restrict__ bv,
+                                                              int64_t stride_ab, const __grid_constant__ OverlapArgs o,
+                                                              double* __restrict__ partials) {
+    constexpr int D = 1 << K;
+    const int64_t b = blockIdx.y;
+    const cplx<T>* x = a + b * stride_ab;
+    const cplx<T>* y = bv + b * stride_ab;
+    const uint64_t groups = uint64_t(1) << (o.n - K), stride = uint64_t(gridDim.x) * blockDim.x;
+    double acc[2 * D * D];
+#pragma unroll
+    for (int j = 0; j < 2 * D * D; ++j) acc[j] = 0.0;
+    for (uint64_t g = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; g < groups; g += stride) {
+        uint64_t base = g;
+#pragma unroll
+        for (int j = 0; j < K; ++j) base = ((base >> o.sorted[j]) << (o.sorted[j] + 1)) | (base & ((uint64_t(1) << o.sorted[j]) - 1));
+        cplx<T> u[D], v[D];
+#pragma unroll
+        for (int r = 0; r < D; ++r) {
+            u[r] = x[base + o.off[r]];
+            v[r] = y[base + o.off[r]];
+        }
+#pragma unroll
+        for (int r = 0; r < D; ++r)
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                // u[r] * conj(v[c])
+                acc[2 * (r * D + c)] += double(u[r].x) * v[c].x + double(u[r].y) * v[c].y;
+                acc[2 * (r * D + c) + 1] += double(u[r].y) * v[c].x - double(u[r].x) * v[c].y;
+            }
+    }
+    block_reduce_store<2 * D * D>(acc, partials + (b * 2 * D * D) * gridDim.x + blockIdx.x, gridDim.x);
+}
+
+// DM: Tr(rho P) for one Pauli group: sum_x rho[x, x ^ xmask] i^ny (-1)^{pop(x & zmask)}.
+template <typename T, int NT>
+__global__ void __launch_bounds__(kRedThreads) dm_pauli_kernel(const cplx<T>* __restrict__ rho, int n, int64_t stride,
+                                                               const __grid_constant__ PauliGroup g, int nslots,
+                                                               double* __restrict__ partials) {
+    const int64_t b = blockIdx.y;
+    const cplx<T>* r = rho + b * stride;
+    const uint64_t dim = uint64_t(1) << n, step = uint64_t(gridDim.x) * blockDim.x;
+    double acc[NT];
+#pragma unroll
+    for (int j = 0; j < NT; ++j) acc[j] = 0.0;
+    for (uint64_t x = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; x < dim; x += step) {
+        const cplx<T> v = r[(x << n) | (x ^ g.xmask)];
+#pragma unroll
+        for (int j = 0; j < NT; ++j)
+            if (j < g.nterms) {
+                const double t = re_iny(double(v.x), double(v.y), g.ny[j]);
+                acc[j] += (__popcll(x & g.zmask[j]) & 1) ? -t : t;
+            }
+    }
+#pragma unroll
+    for (int j = 0; j < NT; ++j) acc[j] *= g.coeff[j < g.nterms ? j : 0];
+    block_reduce_store<NT>(acc, partials + (int64_t(b) * nslots + g.slot0) * gridDim.x + blockIdx.x, gridDim.x,
+                           g.nterms);
+}
+
+// DM: Re Tr((x)_q O_q rho) = Re sum_{x,y} prod_q O_q[x_q, y_q] rho[y, x].
+struct ProductOps {
+    int n;
+    double2 o[QGB_MAX_QUBITS][4];  // o[q][2*a + b] = O_q[a][b]
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) dm_product_kernel(const cplx<T>* __restrict__ rho, int64_t stride,
+                                                                 const __grid_constant__ ProductOps p,
+                                                                 double* __restrict__ partials) {
+    const int n = p.n;
+    const cplx<T>* r = rho + int64_t(blockIdx.y) * stride;
+    const uint64_t len = uint64_t(1) << (2 * n), step = uint64_t(gridDim.x) * blockDim.x;
+    const uint64_t lo = (uint64_t(1) << n) - 1;
+    double acc[1] = {0.0};
+    for (uint64_t v = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; v < len; v += step) {
+        const uint64_t y = v >> n, x = v & lo;  // entry rho[y, x]
+        double wr = 1.0, wi = 0.0;
+        for (int q = 0; q < n; ++q) {
+            const int xa = int((x >> (n - 1 - q)) & 1), yb = int((y >> (n - 1 - q)) & 1);
+            const double2 c = p.o[q][2 * xa + yb];
+            const double tr = wr * c.x - wi * c.y;
+            wi = wr * c.y + wi * c.x;
+            wr = tr;
+        }
+        const cplx<T> e = r[v];
+        acc[0] += wr * double(e.x) - wi * double(e.y);
+    }
+    block_reduce_store<1>(acc, partials + int64_t(blockIdx.y) * gridDim.x + blockIdx.x, gridDim.x);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) dm_trace_kernel(const cplx<T>* __restrict__ rho, int n, int64_t stride,
+                                                               double* __restrict__ partials) {
+    const cplx<T>* r = rho + int64_t(blockIdx.y) * stride;
+    const uint64_t dim = uint64_t(1) << n, step = uint64_t(gridDim.x) * blockDim.x;
+    double acc[1] = {0.0};
+    for (uint64_t x = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; x < dim; x += step)
+        acc[0] += double(r[(x << n) | x].x);
+    block_reduce_store<1>(acc, partials + int64_t(blockIdx.y) * gridDim.x + blockIdx.x, gridDim.x);
+}
+
+// out = sum_t coeff[t] P_t sv
+struct PauliApplyArgs {
+    int n, nterms;
+    uint64_t xmask[128], zmask[128];
+    int ny[128];
+    double coeff[128];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) pauli_apply_kernel(const cplx<T>* __restrict__ sv, cplx<T>* __restrict__ out,
+                                                          int64_t stride, const __grid_constant__ PauliApplyArgs a) {
+    const int64_t b = blockIdx.y;
+    const cplx<T>* s = sv + b * stride;
+    cplx<T>* o = out + b * stride;
+    const uint64_t len = uint64_t(1) << a.n, step = uint64_t(gridDim.x) * blockDim.x;
+    for (uint64_t y = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; y < len; y += step) {
+        double ar = 0, ai = 0;
+        for (int t = 0; t < a.nterms; ++t) {
+            const uint64_t x = y ^ a.xmask[t];
+            const cplx<T> v = s[x];
+            // P|x> = i^ny (-1)^{pop(x & z)} |x ^ xmask> ; contribution to out[y]
+            double cr = double(v.x), ci = double(v.y);
+            switch (a.ny[t] & 3) {
+                case 1: { double t2 = cr; cr = -ci; ci = t2; } break;
+                case 2: cr = -cr; ci = -ci; break;
+                case 3: { double t2 = cr; cr = ci; ci = -t2; } break;
+                default: break;
+            }
+            const double f = ((__popcll(x & a.zmask[t]) & 1) ? -a.coeff[t] : a.coeff[t]);
+            ar += f * cr;
+            ai += f * ci;
+        }
+        o[y] = mk<T>(T(ar), T(ai));
+    }
+}
+
+}  // namespace qgb
+
+using namespace qgb;
+using namespace qgb_host;
+
+namespace {
+
+struct ParsedPauli {
+    uint64_t x, z;
+    int ny;
+};
+
+int parse_paulis(const char* paulis, int n, int nterms, std::vector<ParsedPauli>& out) {
+    if (!paulis) return set_error(QGB_EINVAL, "null Pauli strings");
+    if (n > 64) return set_error(QGB_EINVAL, "Pauli strings limited to 64 sites");
+    out.resize(nterms);
+    for (int t = 0; t < nterms; ++t) {
+        ParsedPauli p{0, 0, 0};
+        for (int q = 0; q < n; ++q) {
+            const uint64_t bit = 1ull << (n - 1 - q);
+            switch (paulis[size_t(t) * n + q]) {
+                case 'i': case 'I': break;
+                case 'x': case 'X': p.x |= bit; break;
+                case 'y': case 'Y': p.x |= bit; p.z |= bit; p.ny++; break;
+                case 'z': case 'Z': p.z |= bit; break;
+                default: return set_error(QGB_EINVAL, "invalid Pauli character in term %d", t);
+            }
+        }
+        out[t] = p;
+    }
+    return QGB_OK;
+}
+
+size_t red_scratch(int nbits, int nslots, int64_t batch) {
+    return sizeof(double) * size_t(red_blocks(nbits)) * size_t(nslots) * size_t(batch);
+}
+
+int check_common(const void* p, int dtype, int nbits, int64_t batch, int64_t stride) {
+    if (!p) return set_error(QGB_EINVAL, "null state");
+    if (dtype != QGB_C64 && dtype != QGB_C128) return set_error(QGB_EINVAL, "dtype %d unknown", dtype);
+    if (nbits < 1 || nbits > 2 * QGB_MAX_QUBITS) return set_error(QGB_EINVAL, "n=%d invalid", nbits);
+    if (batch < 1 || batch > 65535) return set_error(QGB_EINVAL, "batch out of range");
+    if (batch > 1 && stride < (int64_t(1) << nbits)) return set_error(QGB_EINVAL, "stride smaller than the state");
+    return QGB_OK;
+}
+
+int finish(const double* partials, int nblk, int nslots, int64_t batch, const double* coeff, double* out, cudaStream_t st) {
+    const int64_t items = batch * nslots;
+    const unsigned blocks = unsigned((items + 7) / 8);
+    finish_kernel<<<blocks, 256, 0, st>>>(partials, nblk, nslots, batch, coeff, out);
+    return check_launch("reduction finish");
+}
+
+template <typename T, int NT>
+void launch_group(const void* sv, int n, int64_t stride, const PauliGroup& g, int nslots, double* partials,
+                  int64_t batch, bool dm, cudaStream_t st) {
+    const int nbits = dm ? 2 * n : n;
+    dim3 grid(red_blocks(nbits), unsigned(batch));
+    if (dm)
+        dm_pauli_kernel<T, NT><<<grid, kRedThreads, 0, st>>>((const cplx<T>*)sv, n, stride, g, nslots, partials);
+    else
+        pauli_group_kernel<T, NT><<<grid, kRedThreads, 0, st>>>((const cplx<T>*)sv, n, stride, g, nslots, partials);
+}
+
+template <typename T>
+void launch_group_nt(const void* sv, int n, int64_t stride, const PauliGroup& g, int nslots, double* partials,
+                     int64_t batch, bool dm, cudaStream_t st) {
+    if (g.nterms <= 1) launch_group<T, 1>(sv, n, stride, g, nslots, partials, batch, dm, st);
+    else if (g.nterms <= 4) launch_group<T, 4>(sv, n, stride, g, nslots, partials, batch, dm, st);
+    else if (g.nterms <= 8) launch_group<T, 8>(sv, n, stride, g, nslots, partials, batch, dm, st);
+    else launch_group<T, 32>(sv, n, stride, g, nslots, partials, batch, dm, st);
+}
+
+int pauli_expect_impl(const void* sv, int dtype, int n, const char* paulis, const double* coeff, int nterms,
+                      int64_t batch, int64_t stride, double* out, void* scratch, size_t scratch_bytes, bool dm,
+                      cudaStream_t st) {
+    const int nbits = dm ? 2 * n : n;
+    int rc = check_common(sv, dtype, nbits, batch, stride);
+    if (rc) return rc;
+    if (!out) return set_error(QGB_EINVAL, "null output");
+    if (nterms < 1) return set_error(QGB_EINVAL, "no terms");
+    if (!scratch || scratch_bytes < red_scratch(nbits, nterms, batch))
+        return set_error(QGB_ESCRATCH, "scratch of %zu bytes needed", red_scratch(nbits, nterms, batch));
+    std::vector<ParsedPauli> ps;
+    if ((rc = parse_paulis(paulis, n, nterms, ps))) return rc;
+    // Output slot t belongs to term t; terms are grouped by X mask (<= 32 per launch)
+    // and each group's slots must be contiguous: process terms in an order where
+    // each launch covers a contiguous run of slots with a common X mask.
+    double* partials = (double*)scratch;
+    int t = 0;
+    while (t < nterms) {
+        PauliGroup g{};
+        g.xmask = ps[t].x;
+        g.slot0 = t;
+        g.nterms = 0;
+        while (t < nterms && ps[t].x == g.xmask && g.nterms < 32) {
+            g.zmask[g.nterms] = ps[t].z;
+            g.ny[g.nterms] = ps[t].ny;
+            g.coeff[g.nterms] = coeff ? coeff[t] : 1.0;
+            ++g.nterms;
+            ++t;
+        }
+        if (dtype == QGB_C64) launch_group_nt<float>(sv, n, stride, g, nterms, partials, batch, dm, st);
+        else launch_group_nt<double>(sv, n, stride, g, nterms, partials, batch, dm, st);
+        if ((rc = check_launch("pauli expectation"))) return rc;
+    }
+    return finish(partials, red_blocks(nbits), nterms, batch, nullptr, out, st);
+}
+
+}  // namespace
+
+extern "C" size_t qgb_reduce_scratch_bytes(int n, int nterms, int64_t batch) {
+    if (n < 1 || n > 2 * QGB_MAX_QUBITS || nterms < 1 || batch < 1) return 0;
+    // the largest reduction over 2^n entries (n already doubled by DM callers)
+    int slots = nterms < 32 ? 32 : nterms;  // partial overlap on 2 sites needs 32 slots
+    return red_scratch(n, slots, batch);
+}
+
+extern "C" int qgb_norm2(const void* sv, int dtype, int n, int64_t batch, int64_t sv_stride, double* out, void* scratch,
+                         size_t scratch_bytes, void* stream) {
+    int rc = check_common(sv, dtype, n, batch, sv_stride);
+    if (rc) return rc;
+    if (!out) return set_error(QGB_EINVAL, "null output");
+    if (!scratch || scratch_bytes < red_scratch(n, 1, batch)) return set_error(QGB_ESCRATCH, "scratch too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    dim3 grid(red_blocks(n), unsigned(batch));
+    if (dtype == QGB_C64) norm2_kernel<float><<<grid, kRedThreads, 0, st>>>((const float2*)sv, n, sv_stride, (double*)scratch);
+    else norm2_kernel<double><<<grid, kRedThreads, 0, st>>>((const double2*)sv, n, sv_stride, (double*)scratch);
+    if ((rc = check_launch("norm2"))) return rc;
+    return finish((const double*)scratch, red_blocks(n), 1, batch, nullptr, out, st);
+}
+
+extern "C" int qgb_inner_product(const void* a, const void* b, int dtype, int n, int64_t batch, int64_t stride,
+                                 double* out, void* scratch, size_t scratch_bytes, void* stream) {
+    int rc = check_common(a, dtype, n, batch, stride);
+    if (rc) return rc;
+    if (!b || !out) return set_error(QGB_EINVAL, "null pointer");
+    if (!scratch || scratch_bytes < red_scratch(n, 2, batch)) return set_error(QGB_ESCRATCH, "scratch too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    dim3 grid(red_blocks(n), unsigned(batch));
+    if (dtype == QGB_C64)
+        inner_kernel<float><<<grid, kRedThreads, 0, st>>>((const float2*)a, (const float2*)b, n, stride, (double*)scratch);
+    else
+        inner_kernel<double><<<grid, kRedThreads, 0, st>>>((const double2*)a, (const double2*)b, n, stride, (double*)scratch);
+    if ((rc = check_launch("inner product"))) return rc;
+    return finish((const double*)scratch, red_blocks(n), 2, batch, nullptr, out, st);
+}
+
+extern "C" int qgb_pauli_expectation(const void* sv, int dtype, int n, const char* paulis, const double* coeff,
+                                     int nterms, int64_t batch, int64_t sv_stride, double* out, void* scratch,
+                                     size_t scratch_bytes, void* stream) {
+    return pauli_expect_impl(sv, dtype, n, paulis, coeff, nterms, batch, sv_stride, out, scratch, scratch_bytes, false,
+                             (cudaStream_t)stream);
+}
+
+extern "C" int qgb_dm_pauli_expectation(const void* rho, int dtype, int n, const char* paulis, const double* coeff,
+                                        int nterms, int64_t batch, int64_t rho_stride, double* out, void* scratch,
+                                        size_t scratch_bytes, void* stream) {
+    return pauli_expect_impl(rho, dtype, n, paulis, coeff, nterms, batch, rho_stride, out, scratch, scratch_bytes, true,
+                             (cudaStream_t)stream);
+}
+
+extern "C" int qgb_partial_overlap(const void* a, const void* b, int dtype, int n, const int* indices, int k,
+                                   int64_t batch, int64_t sv_stride, double* out, void* scratch, size_t scratch_bytes,
+                                   void* stream) {
+    int rc = check_common(a, dtype, n, batch, sv_stride);
+    if (rc) return rc;
+    if (!b || !out || !indices) return set_error(QGB_EINVAL, "null pointer");
+    if (k < 1 || k > 2 || k > n) return set_error(QGB_EINVAL, "partial overlap supports 1 or 2 sites (k=%d)", k);
+    const int slots = 2 << (2 * k);
+    if (!scratch || scratch_bytes < red_scratch(n, slots, batch)) return set_error(QGB_ESCRATCH, "scratch too small");
+    OverlapArgs o{};
+    o.n = n;
+    o.k = k;
+    int pos[2];
+    for (int j = 0; j < k; ++j) {
+        if (indices[j] < 0 || indices[j] >= n) return set_error(QGB_EINVAL, "site out of range");
+        pos[j] = n - 1 - indices[j];
+        o.sorted[j] = pos[j];
+    }
+    if (k == 2) {
+        if (pos[0] == pos[1]) return set_error(QGB_EINVAL, "repeated site");
+        if (o.sorted[0] > o.sorted[1]) { int t = o.sorted[0]; o.sorted[0] = o.sorted[1]; o.sorted[1] = t; }
+    }
+    for (int r = 0; r < (1 << k); ++r) o.off[r] = uint32_t(matrix_offset(r, pos, k));
+    cudaStream_t st = (cudaStream_t)stream;
+    dim3 grid(red_blocks(n), unsigned(batch));
+    if (dtype == QGB_C64) {
+        if (k == 1) overlap_kernel<float, 1><<<grid, kRedThreads, 0, st>>>((const float2*)a, (const float2*)b, sv_stride, o, (double*)scratch);
+        else overlap_kernel<float, 2><<<grid, kRedThreads, 0, st>>>((const float2*)a, (const float2*)b, sv_stride, o, (double*)scratch);
+    } else {
+        if (k == 1) overlap_kernel<double, 1><<<grid, kRedThreads, 0, st>>>((const double2*)a, (const double2*)b, sv_stride, o, (double*)scratch);
+        else overlap_kernel<double, 2><<<grid, kRedThreads, 0, st>>>((const double2*)a, (const double2*)b, sv_stride, o, (double*)scratch);
+    }
+    if ((rc = check_launch("partial overlap"))) return rc;
+    return finish((const double*)scratch, red_blocks(n), slots, batch, nullptr, out, st);
+}
+
+extern "C" int qgb_dm_product_expectation(const void* rho, int dtype, int n, const double* ops, int64_t batch,
+                                          int64_t rho_stride, double* out, void* scratch, size_t scratch_bytes,
+                                          void* stream) {
+    int rc = check_common(rho, dtype, 2 * n, batch, rho_stride);
+    if (rc) return rc;
+    if (!ops || !out) return set_error(QGB_EINVAL, "null pointer");
+    if (n > QGB_MAX_QUBITS) return set_error(QGB_EINVAL, "n too large");
+    if (!scratch || scratch_bytes < red_scratch(2 * n, 1, batch)) return set_error(QGB_ESCRATCH, "scratch too small");
+    ProductOps p{};
+    p.n = n;
+    for (int q = 0; q < n; ++q)
+        for (int e = 0; e < 4; ++e) p.o[q][e] = make_double2(ops[(q * 4 + e) * 2], ops[(q * 4 + e) * 2 + 1]);
+    cudaStream_t st = (cudaStream_t)stream;
+    dim3 grid(red_blocks(2 * n), unsigned(batch));
+    if (dtype == QGB_C64) dm_product_kernel<float><<<grid, kRedThreads, 0, st>>>((const float2*)rho, rho_stride, p, (double*)scratch);
+    else dm_product_kernel<double><<<grid, kRedThreads, 0, st>>>((const double2*)rho, rho_stride, p, (double*)scratch);
+    if ((rc = check_launch("dm product expectation"))) return rc;
+    return finish((const double*)scratch, red_blocks(2 * n), 1, batch, nullptr, out, st);
+}
+
+extern "C" int qgb_dm_trace(const void* rho, int dtype, int n, int64_t batch, int64_t rho_stride, double* out,
+                            void* scratch, size_t scratch_bytes, void* stream) {
+    int rc = check_common(rho, dtype, 2 * n, batch, rho_stride);
+    if (rc) return rc;
+    if (!out) return set_error(QGB_EINVAL, "null output");
+    if (!scratch || scratch_bytes < red_scratch(2 * n, 1, batch)) return set_error(QGB_ESCRATCH, "scratch too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    dim3 grid(red_blocks(2 * n), unsigned(batch));
+    if (dtype == QGB_C64) dm_trace_kernel<float><<<grid, kRedThreads, 0, st>>>((const float2*)rho, n, rho_stride, (double*)scratch);
+    else dm_trace_kernel<double><<<grid, kRedThreads, 0, st>>>((const double2*)rho, n, rho_stride, (double*)scratch);
+    if ((rc = check_launch("dm trace"))) return rc;
+    return finish((const double*)scratch, red_blocks(2 * n), 1, batch, nullptr, out, st);
+}
+
+extern "C" int qgb_pauli_apply(const void* sv, void* out, int dtype, int n, const char* paulis, const double* coeff,
+                               int nterms, int64_t batch, int64_t sv_stride, void* stream) {
+    int rc = check_common(sv, dtype, n, batch, sv_stride);
+    if (rc) return rc;
+    if (!out || !coeff) return set_error(QGB_EINVAL, "null pointer");
+    if (out == sv) return set_error(QGB_EINVAL, "output must not alias the input");
+    if (nterms < 1 || nterms > 128) return set_error(QGB_EINVAL, "1..128 terms supported (got %d)", nterms);
+    std::vector<ParsedPauli> ps;
+    if ((rc = parse_paulis(paulis, n, nterms, ps))) return rc;
+    PauliApplyArgs a{};
+    a.n = n;
+    a.nterms = nterms;
+    for (int t = 0; t < nterms; ++t) {
+        a.xmask[t] = ps[t].x;
+        a.zmask[t] = ps[t].z;
+        a.ny[t] = ps[t].ny;
+        a.coeff[t] = coeff[t];
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    const uint64_t len = uint64_t(1) << n;
+    uint64_t bx = (len + 255) / 256;
+    const uint64_t cap = uint64_t(sm_count()) * 8;
+    if (bx > cap) bx = cap;
+    dim3 grid((unsigned)bx, (unsigned)batch);
+    if (dtype == QGB_C64) pauli_apply_kernel<float><<<grid, 256, 0, st>>>((const float2*)sv, (float2*)out, sv_stride, a);
+    else pauli_apply_kernel<double><<<grid, 256, 0, st>>>((const double2*)sv, (double2*)out, sv_stride, a);
+    return check_launch("pauli apply");
+}

@@ -1,0 +1,370 @@
+"""Gate objects with the reference's index and matrix conventions.
+
+Host-side mirror of ``core/gates.py`` and ``core/param_gates.py`` of the
+reference, so circuits can be built where the reference package is not
+installed. Reference gate objects work too: every simulator here reads only
+``.name``, ``.indices``, ``.matrix`` (NumPy or torch), ``.span`` and, for
+noise carriers, ``.nm`` / ``.time`` / ``.dd``, and ``Reset.normalize``.
+
+Conventions kept (they decide the numbers):
+
+* a gate's matrix is indexed by its ``indices`` list in order, ``indices[0]``
+  being the most-significant bit of the row/column index
+  (``tensorQ/statevector_sim.py:124-140``);
+* ``CNOT(indices)`` takes ``(target, control)`` and stores ascending sites,
+  transposing the matrix when the target is the larger site
+  (``core/gates.py:135-170,217-220``);
+* rotations carry no factor 1/2: ``RX(t) = expm(-i t X)``
+  (``core/param_gates.py:51-103``);
+* ``Reset`` is a projector followed by renormalisation
+  (``core/gates.py:172-187``, ``core/base_sim.py:25-28``).
+
+Only qubits (local dimension 2) are supported by the CUDA path.
+"""
+from __future__ import annotations
+
+import copy
+from functools import reduce
+
+import numpy as np
+import scipy.linalg
+import torch
+
+from .paulis import pauli_X, pauli_Y, pauli_Z, pauli_mapping
+
+
+def _is_torch(x) -> bool:
+    return torch.is_tensor(x)
+
+
+class Gate:
+    """Dense gate on ``indices`` (``core/gates.py:32-55``)."""
+
+    def __init__(self, name, indices, matrix, time=None):
+        self.name = name
+        self.indices = [indices] if isinstance(indices, (int, np.integer)) else list(indices)
+        self.indices = [int(i) for i in self.indices]
+        self.span = len(self.indices)
+        self.matrix = matrix
+        self.time = time
+
+    def __str__(self):
+        return f"{self.name} gate on site(s) {self.indices}"
+
+    def to_superop(self):
+        m = self.matrix
+        if _is_torch(m):
+            m = m.detach().cpu().numpy()
+        return np.kron(np.conj(m), m).reshape([self.get_local_dim()] * 4 * self.span)
+
+    def get_local_dim(self):
+        return int(round(self.matrix.shape[0] ** (1 / self.span)))
+
+    def dag(self):
+        g = copy.deepcopy(self)
+        g.matrix = g.matrix.conj().T
+        return g
+
+    def shallow_copy(self):
+        return Gate(self.name, self.indices, self.matrix, time=self.time)
+
+
+class ID(Gate):
+    """Idling / noise carrier (``core/gates.py:81-95``)."""
+
+    def __init__(self, local_dim, time, indices, nm, dd=False):
+        super().__init__("ID", indices, matrix=None, time=time)
+        self.matrix = np.eye(local_dim ** self.span)
+        self.dd = dd
+        self.nm = nm
+
+    def to_superop(self):
+        return self.nm.get_superop(self.time, self.dd).reshape([self.get_local_dim()] * 4 * self.span)
+
+    def shallow_copy(self):
+        # The reference's ID inherits Gate.shallow_copy and silently drops its
+        # noise model on Circuit.copy(); here the carrier keeps it.
+        return ID(self.get_local_dim(), self.time, self.indices, self.nm, self.dd)
+
+
+class CNOTGate(Gate):
+    """``indices = (target, control)`` (``core/gates.py:137-170``)."""
+
+    def __init__(self, indices, matrix, n):
+        d = int(np.sqrt(matrix.shape[0]))
+        indices = [int(i) for i in indices]
+        if abs(indices[0] - indices[1]) > 1:
+            temp = np.array(indices) + 1
+            if temp[0] % n < temp[1] % n:
+                mat, bottom = matrix, False
+            else:
+                indices = indices[::-1]
+                mat = matrix.reshape(d, d, d, d).transpose(1, 0, 3, 2).reshape(d * d, d * d)
+                bottom = True
+        else:
+            if indices[0] < indices[1]:
+                mat, bottom = matrix, False
+            else:
+                indices = indices[::-1]
+                mat = matrix.reshape(d, d, d, d).transpose(1, 0, 3, 2).reshape(d * d, d * d)
+                bottom = True
+        super().__init__(f"CNOT{d}", indices, mat)
+        self.bottom_heavy = bottom
+
+
+class Reset(Gate):
+    """Projector onto ``reset_to`` then renormalise (``core/gates.py:172-187``)."""
+
+    def __init__(self, indices, reset_to: str, normalize=True, time=None):
+        up = np.array([[1, 0], [0, 0]])
+        down = np.array([[0, 0], [0, 1]])
+        matrix = reduce(np.kron, [up if b == '0' else down for b in reset_to])
+        super().__init__("Reset", indices, matrix, time=time)
+        self.reset_to = reset_to
+        self.normalize = normalize
+
+    def shallow_copy(self):
+        return Reset(self.indices, self.reset_to, self.normalize, self.time)
+
+
+def SX(indices):
+    return Gate("SX", indices, (1 / np.sqrt(2)) * np.array([[1, -1j], [-1j, 1]]))
+
+
+def X(indices):
+    return Gate("X", indices, np.array([[0, 1], [1, 0]]))
+
+
+def Y(indices):
+    return Gate("Y", indices, pauli_Y)
+
+
+def Z(indices):
+    return Gate("Z", indices, pauli_Z)
+
+
+def H(indices):
+    return Gate("H", indices, np.array([[1, 1], [1, -1]]) / np.sqrt(2))
+
+
+def SDG(indices):
+    return Gate("SDG", indices, np.array([[1, 0], [0, -1j]]))
+
+
+def CNOT(indices, n=1000):
+    """``indices = (target, control)`` (``core/gates.py:217-220``)."""
+    return CNOTGate(indices, np.array([[1, 0, 0, 0], [0, 0, 0, 1], [0, 0, 1, 0], [0, 1, 0, 0]]), n=n)
+
+
+def CZ(indices):
+    return Gate("CZ", indices, np.diag([1, 1, 1, -1]).astype(complex))
+
+
+def SWAP(indices):
+    return Gate("SWAP", indices, np.array([[1, 0, 0, 0], [0, 0, 1, 0], [0, 1, 0, 0], [0, 0, 0, 1]]))
+
+
+def iSWAP(indices):
+    return Gate("iSWAP", indices, np.array([[1, 0, 0, 0], [0, 0, 1j, 0], [0, 1j, 0, 0], [0, 0, 0, 1]]))
+
+
+def proj_up(indices):
+    return Gate("P0", indices, np.array([[1, 0], [0, 0]]))
+
+
+def proj_down(indices):
+    return Gate("P1", indices, np.array([[0, 0], [0, 1]]))
+
+
+def random_unitary(size):
+    """The reference's (non-Haar) generator, ``core/gates.py:289-293``."""
+    a = np.random.rand(size, size) + 1.j * np.random.rand(size, size)
+    _, u = np.linalg.eigh(a @ a.conj().T)
+    return u
+
+
+def is_unitary(u):
+    eye = np.eye(u.shape[0])
+    return np.allclose(u @ u.conj().T, eye, atol=1e-10) and np.allclose(u.conj().T @ u, eye, atol=1e-10)
+
+
+pauli_gate_map = {'x': X, 'y': Y, 'z': Z}
+
+
+def pauli_string_to_gates(string):
+    return [pauli_gate_map[op](i) for i, op in enumerate(string) if op != 'i']
+
+
+# ---------------------------------------------------------------- parametrised
+
+_XT = torch.tensor([[0, 1], [1, 0]], dtype=torch.complex128)
+_YT = torch.tensor([[0, -1.j], [1.j, 0]], dtype=torch.complex128)
+_ZT = torch.tensor([[1, 0], [0, -1]], dtype=torch.complex128)
+_xxN, _yyN, _zzN = np.kron(pauli_X, pauli_X), np.kron(pauli_Y, pauli_Y), np.kron(pauli_Z, pauli_Z)
+_xxT, _yyT, _zzT = torch.kron(_XT, _XT), torch.kron(_YT, _YT), torch.kron(_ZT, _ZT)
+
+
+def _arr(x, backend):
+    if backend == "torch":
+        return torch.stack([torch.stack([torch.as_tensor(e, dtype=torch.complex128) for e in row])
+                            for row in x]).to(torch.complex128)
+    return np.array(x, dtype=np.complex128)
+
+
+class ParamGate(Gate):
+    """Angle-parametrised gate (``core/param_gates.py:21-49``). Torch angles keep
+    the autograd graph through ``torch.linalg.matrix_exp``."""
+
+    def __init__(self, name, indices, *args):
+        super().__init__(name, indices, None)
+        self.backend = "torch" if _is_torch(args[0]) else "numpy"
+        if isinstance(args[0], np.ndarray) and args[0].ndim == 2:
+            self.matrix = args[0]
+            self.angles = self.solve_angles()
+        else:
+            self.angles = args
+            self.matrix = self.construct_matrix()
+
+    def __str__(self):
+        return f"{self.name} gate on site(s) {self.indices} with angle(s) {self.angles}"
+
+    def update_matrix(self, mat):
+        self.matrix = mat
+
+    def construct_matrix(self):
+        raise NotImplementedError
+
+    def solve_angles(self):
+        return "unsolved"
+
+    def shallow_copy(self):
+        return type(self)(self.indices, *self.angles)
+
+    def _expm(self, gen_np, gen_t):
+        t = self.angles[0]
+        if self.backend == "torch":
+            return torch.linalg.matrix_exp(-1.j * t * gen_t)
+        return scipy.linalg.expm(-1.j * t * gen_np)
+
+
+class RX(ParamGate):
+    def __init__(self, indices, *args):
+        super().__init__("RX", indices, *args)
+
+    def construct_matrix(self):
+        return self._expm(pauli_X, _XT)
+
+
+class RY(ParamGate):
+    def __init__(self, indices, *args):
+        super().__init__("RY", indices, *args)
+
+    def construct_matrix(self):
+        return self._expm(pauli_Y, _YT)
+
+
+class RZ(ParamGate):
+    def __init__(self, indices, *args):
+        super().__init__("RZ", indices, *args)
+
+    def construct_matrix(self):
+        return self._expm(pauli_Z, _ZT)
+
+
+class RXX(ParamGate):
+    def __init__(self, indices, *args):
+        super().__init__("RXX", indices, *args)
+
+    def construct_matrix(self):
+        return self._expm(_xxN, _xxT)
+
+
+class RYY(ParamGate):
+    def __init__(self, indices, *args):
+        super().__init__("RYY", indices, *args)
+
+    def construct_matrix(self):
+        return self._expm(_yyN, _yyT)
+
+
+class RZZ(ParamGate):
+    def __init__(self, indices, *args):
+        super().__init__("RZZ", indices, *args)
+
+    def construct_matrix(self):
+        return self._expm(_zzN, _zzT)
+
+
+class XYCoupling(ParamGate):
+    def __init__(self, indices, *args):
+        super().__init__("XYCoupling", indices, *args)
+
+    def construct_matrix(self):
+        return self._expm(_xxN + _yyN, _xxT + _yyT)
+
+
+class HeisenbergCoupling(ParamGate):
+    def __init__(self, indices, *args):
+        super().__init__("HeisenbergCoupling", indices, *args)
+
+    def construct_matrix(self):
+        return self._expm(_xxN + _yyN + _zzN, _xxT + _yyT + _zzT)
+
+
+class CPhase(ParamGate):
+    def __init__(self, indices, *args):
+        super().__init__("CPhase", indices, *args)
+
+    def construct_matrix(self):
+        xp = torch if self.backend == "torch" else np
+        ph = xp.exp(1.j * self.angles[0])
+        return _arr([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 1, 0], [0, 0, 0, ph]], self.backend)
+
+    def solve_angles(self):
+        return (np.angle(self.matrix[3, 3]),)
+
+
+class U(ParamGate):
+    """``U(indices, theta, phi, lambda)`` (``core/param_gates.py:118-158``)."""
+
+    def __init__(self, indices, *args):
+        super().__init__("U", indices, *args)
+
+    def construct_matrix(self):
+        t, p, l = self.angles
+        xp = torch if self.backend == "torch" else np
+        return _arr([[xp.cos(t / 2), -xp.exp(1j * l) * xp.sin(t / 2)],
+                     [xp.exp(1j * p) * xp.sin(t / 2), xp.exp(1j * (p + l)) * xp.cos(t / 2)]], self.backend)
+
+    def solve_angles(self):
+        m = self.matrix / np.exp(1.j * np.angle(self.matrix[0, 0]))
+        t = np.arccos(np.clip(m[0, 0].real, -1, 1)) * 2
+        if abs(np.sin(t / 2)) > 1e-12:
+            l = np.angle(-m[0, 1] / np.sin(t / 2))
+            p = np.angle(m[1, 1] / m[0, 0]) - l
+        else:
+            l = p = np.angle(m[1, 1]) / 2
+        return t, p, l
+
+
+class Givens(ParamGate):
+    def __init__(self, indices, *args):
+        super().__init__("Givens", indices, *args)
+
+    def construct_matrix(self):
+        th = self.angles[0]
+        xp = torch if self.backend == "torch" else np
+        c, s = xp.cos(th / 2), xp.sin(th / 2)
+        return _arr([[1, 0, 0, 0], [0, c, -s, 0], [0, s, c, 0], [0, 0, 0, 1]], self.backend)
+
+
+def kak_unitary(params):
+    """15-parameter two-qubit unitary (``core/param_gates.py:247-259``)."""
+    backend = "torch" if _is_torch(params) else "numpy"
+    xp = torch if backend == "torch" else np
+    xx, yy, zz = (_xxT, _yyT, _zzT) if backend == "torch" else (_xxN, _yyN, _zzN)
+    expm = torch.linalg.matrix_exp if backend == "torch" else scipy.linalg.expm
+    left = xp.kron(U(0, *params[0:3]).matrix, U(0, *params[3:6]).matrix)
+    right = xp.kron(U(0, *params[9:12]).matrix, U(0, *params[12:15]).matrix)
+    arg = sum(p * P for p, P in zip(params[6:9], [xx, yy, zz]))
+    return left @ expm(1.j * arg) @ right

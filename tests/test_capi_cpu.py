@@ -1,0 +1,81 @@
+"""C ABI checks that need no GPU: the library builds, loads, exports every
+symbol ``include/qgb.h`` declares, the ctypes struct matches the C layout, and
+argument errors are rejected on the host before any CUDA call."""
+import ctypes as C
+import os
+import re
+import subprocess
+import tempfile
+
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "qgb.h")
+
+
+def _declared():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:int|size_t|const char\*)\s+(qgb_\w+)\s*\(", text, re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from qaravan_gb300 import build, _lib
+    build.build()
+    return _lib.lib()
+
+
+def test_header_symbols_exported(lib):
+    names = _declared()
+    assert len(names) >= 15
+    out = subprocess.run(["nm", "-D", "--defined-only", os.path.join(ROOT, "qaravan_gb300", "_lib", "libqgb.so")],
+                         capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (qgb_\w+)", out))
+    missing = [n for n in names if n not in exported]
+    assert not missing, missing
+    from qaravan_gb300 import _lib
+    bound = set(_lib.SIGNATURES)
+    assert set(names) <= bound | {"qgb_sweep_noalloc"}, set(names) - bound
+
+
+def test_sweep_struct_layout(lib):
+    from qaravan_gb300 import _lib
+    src = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "qgb.h"
+int main(void) {
+  printf("%zu %zu %zu %zu\n", sizeof(qgb_sweep), offsetof(qgb_sweep, op_k), offsetof(qgb_sweep, op_pos),
+         offsetof(qgb_sweep, op_mat));
+  return 0;
+}
+'''
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "t.c")
+        open(c, "w").write(src)
+        exe = os.path.join(d, "t")
+        subprocess.check_call(["gcc", "-I" + os.path.join(ROOT, "include"), c, "-o", exe])
+        vals = [int(x) for x in subprocess.check_output([exe]).split()]
+    S = _lib.Sweep
+    assert vals == [C.sizeof(S), S.op_k.offset, S.op_pos.offset, S.op_mat.offset]
+
+
+def test_abi_version_and_host_validation(lib):
+    from qaravan_gb300 import _lib
+    assert lib.qgb_abi_version() == 1
+    idx = _lib.int_array([0])
+    # n out of range, k out of range, bad site, bad dtype: all rejected before touching CUDA
+    assert lib.qgb_op_action(1, 0, 0, idx, 1, 1, 0, 1, 0, None) == -1
+    assert lib.qgb_op_action(1, 0, 4, idx, 7, 1, 0, 1, 0, None) == -1
+    assert lib.qgb_op_action(1, 0, 4, _lib.int_array([5]), 1, 1, 0, 1, 0, None) == -1
+    assert b"out of range" in lib.qgb_last_error()
+    assert lib.qgb_op_action(1, 7, 4, idx, 1, 1, 0, 1, 0, None) == -1
+    assert lib.qgb_op_action(1, 0, 4, _lib.int_array([1, 1]), 2, 1, 0, 1, 0, None) == -1
+    assert b"repeated" in lib.qgb_last_error()
+    sw = _lib.Sweep()
+    sw.low_bits, sw.n_high, sw.n_ops = 20, 0, 0
+    assert lib.qgb_apply_sweep(1, 0, 10, C.byref(sw), 1, 0, 1, 0, None) == -1  # tile wider than state
+    assert lib.qgb_pauli_expectation(1, 0, 3, b"ixq", None, 1, 1, 0, 1, 1, 1 << 20, None) == -1
+    assert lib.qgb_reduce_scratch_bytes(20, 3, 1) > 0
+    assert lib.qgb_dm_apply_superop(1, 0, 3, _lib.int_array([0, 1, 2, 0]), 4, 1, 1, 0, None) == -1
