@@ -188,6 +188,12 @@ def plan_sweeps(blocks, nbits, tile_bits, low_bits=None, max_high=QGB_SWEEP_MAX_
                 rest.append(blk)
         if not taken:
             raise RuntimeError("sweep planner made no progress (block wider than the tile)")
+        # pad the tile to its full size with unused bits (more work per CTA, same traffic)
+        for b in range(L, nbits):
+            if len(high) >= H:
+                break
+            if b not in high:
+                high.append(b)
         sweeps.append((L, sorted(high), taken))
         remaining = rest
     return sweeps
@@ -195,13 +201,16 @@ def plan_sweeps(blocks, nbits, tile_bits, low_bits=None, max_high=QGB_SWEEP_MAX_
 
 # ------------------------------------------------------------------- plans
 
-def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, max_sweep_k=5):
+def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, max_sweep_k=5, itemsize=8):
     """Compile an op sequence (with ``None`` marking a renormalisation point)
     into a :class:`Plan`.
 
     ``mode``: ``"gate"`` one pass per op; ``"fused"`` one pass per fused block of
     ``width`` bits; ``"sweep"`` fused blocks grouped into shared-memory tile sweeps.
+    ``itemsize`` (8 for complex64, 16 for complex128) caps the tile at 128 KiB
+    of shared memory.
     """
+    tile_bits = min(tile_bits, 14 if itemsize <= 8 else 13)
     plan = Plan(nbits=nbits, n_gates=sum(1 for o in ops if o is not None))
     segments, cur = [], []
     for o in ops:

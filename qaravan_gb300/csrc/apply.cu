@@ -99,13 +99,13 @@ __global__ void __launch_bounds__(256) dense_smem_kernel(cplx<T>* __restrict__ s
     }
     C* s = sv + b * a.sv_stride;
     const int r = threadIdx.x % D, gs = threadIdx.x / D;
-    const uint64_t nchunks = a.groups / G;  // groups is a multiple of G (n >= 10 enforced)
+    const uint64_t nchunks = (a.groups + G - 1) / G;  // the last chunk may be partial (small vectors)
     __syncthreads();
     for (uint64_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
         const uint64_t g0 = ch * G;
         for (int i = threadIdx.x; i < G * D; i += blockDim.x) {
             const int gi = i / D, c = i % D;
-            V[i] = s[insert_zeros(g0 + gi, a.sorted, K) + a.off_in[c]];
+            V[i] = (g0 + gi < a.groups) ? s[insert_zeros(g0 + gi, a.sorted, K) + a.off_in[c]] : mk<T>(0, 0);
         }
         __syncthreads();
         C acc[PER];
@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(256) dense_smem_kernel(cplx<T>* __restrict__ s
 #pragma unroll
         for (int j = 0; j < PER; ++j) {
             const int gi = gs + j * NG;
-            s[insert_zeros(g0 + gi, a.sorted, K) + a.off_out[r]] = acc[j];
+            if (g0 + gi < a.groups) s[insert_zeros(g0 + gi, a.sorted, K) + a.off_out[r]] = acc[j];
         }
         __syncthreads();
     }
@@ -178,7 +178,7 @@ int launch_dense(void* sv, const void* op, const DenseArgs& a, cudaStream_t st) 
                 return check_launch("dense_smem attribute");
             attr = true;
         }
-        const uint64_t nchunks = a.groups / Geo::G;
+        const uint64_t nchunks = (a.groups + Geo::G - 1) / Geo::G;
         dim3 grid(grid_x_for(nchunks * 256, a.batch, 256), unsigned(a.batch));
         dense_smem_kernel<T, K><<<grid, 256, Geo::bytes, st>>>((cplx<T>*)sv, (const cplx<T>*)op, a);
     }
@@ -210,11 +210,13 @@ int apply_dense_bits(void* sv, int dtype, int nbits, const int* in_bits, const i
     if (dtype != QGB_C64 && dtype != QGB_C128) return set_error(QGB_EINVAL, "dtype %d unknown", dtype);
     if (k < 1 || k > QGB_MAX_K) return set_error(QGB_EINVAL, "gate width k=%d not in [1, %d]", k, QGB_MAX_K);
     if (nbits < k || nbits > 2 * QGB_MAX_QUBITS) return set_error(QGB_EINVAL, "n=%d invalid for k=%d", nbits, k);
-    if (k >= 5 && nbits < 10) return set_error(QGB_EINVAL, "k=%d needs at least 10 qubits (n=%d)", k, nbits);
     if (batch < 1 || batch > 65535) return set_error(QGB_EINVAL, "batch %lld not in [1, 65535]", (long long)batch);
     if (batch > 1 && sv_stride < (int64_t(1) << nbits))
         return set_error(QGB_EINVAL, "state stride %lld smaller than the state", (long long)sv_stride);
     if (op_stride < 0) return set_error(QGB_EINVAL, "negative operator stride");
+    const uintptr_t esz = dtype == QGB_C64 ? 8 : 16;
+    if ((reinterpret_cast<uintptr_t>(sv) % esz) || (reinterpret_cast<uintptr_t>(op) % esz))
+        return set_error(QGB_EINVAL, "state or operator pointer not aligned to the element size");
     DenseArgs a{};
     a.n = nbits;
     a.k = k;

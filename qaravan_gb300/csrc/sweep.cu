@@ -106,9 +106,12 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_kernel(cplx<T>* __restric
     using C = cplx<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = a.sw.low_bits, H = a.sw.n_high, m = L + H;
+    // layout: tile (2^m complex) | matrix stage (4^min(KMAX,4) complex) | hoff (2^H uint64);
+    // both complex regions start on 16-byte boundaries
     C* tile = reinterpret_cast<C*>(smem_raw);
-    uint64_t* hoff = reinterpret_cast<uint64_t*>(tile + (1u << m));
-    C* msh = reinterpret_cast<C*>(hoff + (1u << H));
+    C* msh = tile + (1u << m);
+    constexpr int kStage = KMAX >= 3 ? (1 << (2 * (KMAX < kStageK ? KMAX : kStageK))) : 0;
+    uint64_t* hoff = reinterpret_cast<uint64_t*>(msh + kStage);
     for (uint32_t h = threadIdx.x; h < (1u << H); h += blockDim.x) {
         uint64_t o = 0;
         for (int j = 0; j < H; ++j) o |= uint64_t((h >> j) & 1u) << a.sw.high_bits[j];
@@ -172,6 +175,8 @@ template <typename T> constexpr int max_sweep_k() { return sizeof(T) == 4 ? 5 : 
 
 template <typename T>
 size_t sweep_smem_bytes(int m, int H, int kmax) {
+    // kmax is rounded up to the launched instantiation (1 -> 2)
+    if (kmax < 2) kmax = 2;
     size_t stage = kmax >= 3 ? (size_t(1) << (2 * (kmax < kStageK ? kmax : kStageK))) : 0;
     return sizeof(cplx<T>) * ((size_t(1) << m) + stage) + sizeof(uint64_t) * (size_t(1) << H);
 }
@@ -223,11 +228,14 @@ extern "C" int qgb_apply_sweep(void* sv, int dtype, int n, const qgb_sweep* swee
     if (batch < 1) return set_error(QGB_EINVAL, "batch %lld < 1", (long long)batch);
     if (batch > 1 && sv_stride < (int64_t(1) << n)) return set_error(QGB_EINVAL, "state stride too small");
     if (mat_stride < 0) return set_error(QGB_EINVAL, "negative matrix stride");
+    const size_t esz = dtype == QGB_C64 ? 8 : 16;
+    if ((reinterpret_cast<uintptr_t>(sv) & 15) || (batch > 1 && (sv_stride * int64_t(esz)) % 16))
+        return set_error(QGB_EINVAL, "state pointer and stride must be 16-byte aligned");
+    if (mats && (reinterpret_cast<uintptr_t>(mats) % esz)) return set_error(QGB_EINVAL, "matrix buffer misaligned");
     const qgb_sweep& sw = *sweep;
     const int L = sw.low_bits, H = sw.n_high, m = L + H;
     if (L < 1 || H < 0 || H > QGB_SWEEP_MAX_HIGH || m > n || m > QGB_SWEEP_MAX_TILE_BITS)
         return set_error(QGB_EINVAL, "tile geometry L=%d H=%d invalid for n=%d", L, H, n);
-    if (m < 8 && m != n) return set_error(QGB_EINVAL, "tile of %d bits too small (min 8 unless it is the whole state)", m);
     if (sw.n_ops < 0 || sw.n_ops > QGB_SWEEP_MAX_OPS) return set_error(QGB_EINVAL, "n_ops=%d out of range", sw.n_ops);
     SweepArgs a{};
     a.sw = sw;

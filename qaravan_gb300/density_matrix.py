@@ -116,7 +116,8 @@ class DensityMatrixSim:
         if self._exec is None:
             kcap = 5 if self.dtype == torch.complex64 else 4
             plan = compile_ops(self.op_sequence(), 2 * self.num_sites, mode=self.mode, width=self.fusion_width,
-                               tile_bits=self.tile_bits, low_bits=self.low_bits, max_sweep_k=kcap)
+                               tile_bits=self.tile_bits, low_bits=self.low_bits, max_sweep_k=kcap,
+                               itemsize=torch.empty(0, dtype=self.dtype).element_size())
             self._exec = Executor(plan, self.dtype, self.device, mode_normalize="dm")
         return self._exec
 

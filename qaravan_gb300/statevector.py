@@ -108,7 +108,8 @@ class StatevectorSim:
             ops = gates_to_ops(seq, self.num_sites)
             kcap = 5 if self.dtype == torch.complex64 else 4
             plan = compile_ops(ops, self.num_sites, mode=self.mode, width=self.fusion_width,
-                               tile_bits=self.tile_bits, low_bits=self.low_bits, max_sweep_k=kcap)
+                               tile_bits=self.tile_bits, low_bits=self.low_bits, max_sweep_k=kcap,
+                               itemsize=torch.empty(0, dtype=self.dtype).element_size())
             self._exec = Executor(plan, self.dtype, self.device)
         return self._exec
 
@@ -222,7 +223,7 @@ def product_expectation(state, n, site_ops):
     single-site operators with one fused sweep, inner product in float64."""
     ops = [Op([n - 1 - q], _to_np(o)) for q, o in sorted(site_ops.items())]
     kcap = 5 if state.dtype == torch.complex64 else 4
-    plan = compile_ops(ops, n, mode="sweep" if n >= 8 else "gate", width=1, tile_bits=13, max_sweep_k=kcap)
+    plan = compile_ops(ops, n, mode="sweep", width=1, tile_bits=13, max_sweep_k=kcap, itemsize=state.element_size())
     phi = state.reshape(-1).clone()
     Executor(plan, state.dtype, state.device).run(phi)
     ip = inner_product(state.reshape(-1), phi, n)

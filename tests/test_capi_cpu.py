@@ -66,16 +66,16 @@ def test_abi_version_and_host_validation(lib):
     assert lib.qgb_abi_version() == 1
     idx = _lib.int_array([0])
     # n out of range, k out of range, bad site, bad dtype: all rejected before touching CUDA
-    assert lib.qgb_op_action(1, 0, 0, idx, 1, 1, 0, 1, 0, None) == -1
-    assert lib.qgb_op_action(1, 0, 4, idx, 7, 1, 0, 1, 0, None) == -1
-    assert lib.qgb_op_action(1, 0, 4, _lib.int_array([5]), 1, 1, 0, 1, 0, None) == -1
+    assert lib.qgb_op_action(4096, 0, 0, idx, 1, 4096, 0, 1, 0, None) == -1
+    assert lib.qgb_op_action(4096, 0, 4, idx, 7, 4096, 0, 1, 0, None) == -1
+    assert lib.qgb_op_action(4096, 0, 4, _lib.int_array([5]), 1, 4096, 0, 1, 0, None) == -1
     assert b"out of range" in lib.qgb_last_error()
-    assert lib.qgb_op_action(1, 7, 4, idx, 1, 1, 0, 1, 0, None) == -1
-    assert lib.qgb_op_action(1, 0, 4, _lib.int_array([1, 1]), 2, 1, 0, 1, 0, None) == -1
+    assert lib.qgb_op_action(4096, 7, 4, idx, 1, 4096, 0, 1, 0, None) == -1
+    assert lib.qgb_op_action(4096, 0, 4, _lib.int_array([1, 1]), 2, 4096, 0, 1, 0, None) == -1
     assert b"repeated" in lib.qgb_last_error()
     sw = _lib.Sweep()
     sw.low_bits, sw.n_high, sw.n_ops = 20, 0, 0
-    assert lib.qgb_apply_sweep(1, 0, 10, C.byref(sw), 1, 0, 1, 0, None) == -1  # tile wider than state
-    assert lib.qgb_pauli_expectation(1, 0, 3, b"ixq", None, 1, 1, 0, 1, 1, 1 << 20, None) == -1
+    assert lib.qgb_apply_sweep(4096, 0, 10, C.byref(sw), 4096, 0, 1, 0, None) == -1  # tile wider than state
+    assert lib.qgb_pauli_expectation(4096, 0, 3, b"ixq", None, 1, 1, 0, 1, 1, 1 << 20, None) == -1
     assert lib.qgb_reduce_scratch_bytes(20, 3, 1) > 0
-    assert lib.qgb_dm_apply_superop(1, 0, 3, _lib.int_array([0, 1, 2, 0]), 4, 1, 1, 0, None) == -1
+    assert lib.qgb_dm_apply_superop(4096, 0, 3, _lib.int_array([0, 1, 2, 0]), 4, 1, 1, 0, None) == -1
