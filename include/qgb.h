@@ -84,6 +84,10 @@ int qgb_op_action(void* sv, int dtype, int n, const int* indices, int k, const v
 int qgb_apply_sweep(void* sv, int dtype, int n, const qgb_sweep* sweep, const void* mats,
                     int64_t mat_stride, int64_t batch, int64_t sv_stride, void* stream);
 
+/* Selects the sweep kernel: 0 (default) = TMA-staged double-buffered tiles
+ * when the geometry allows it, 1 = plain load/store tiles. Process-wide. */
+int qgb_set_sweep_impl(int impl);
+
 /* Writes |bits> (StatevectorSim.initialize_state, :31-48) to `batch` states. */
 int qgb_init_basis(void* sv, int dtype, int n, uint64_t index, int64_t batch, int64_t sv_stride,
                    void* stream);

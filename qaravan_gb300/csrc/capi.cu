@@ -4,7 +4,7 @@
 #include <cstdio>
 #include <cstring>
 
-#include "qgb_common.cuh"
+#include "sweep_common.cuh"
 
 namespace qgb {
 __device__ int g_status = 0;
@@ -61,5 +61,8 @@ extern "C" int qgb_check_status(void* stream) {
         cudaMemcpyToSymbol(qgb::g_status, &zero, sizeof(int));
         return qgb_host::set_error(QGB_ETIMEOUT, "a bounded device wait gave up (code %d)", status);
     }
+    const int sweep = qgb_host::sweep_status_read_clear();
+    if (sweep < 0) return qgb_host::set_error(QGB_ECUDA, "sweep status read failed");
+    if (sweep != 0) return qgb_host::set_error(QGB_ETIMEOUT, "a sweep's tile-load wait gave up (code %d)", sweep);
     return QGB_OK;
 }

@@ -4,114 +4,37 @@
 // state (core/base_sim.py:30-53 -> tensorQ/statevector_sim.py:124-140). Here
 // the host compiler groups consecutive gates whose qubits fit one tile: a CTA
 // stages a tile of 2^m amplitudes -- the low `L` flat bits (contiguous runs of
-// 2^L amplitudes, coalesced 16-byte loads) times every combination of `H`
-// chosen high bits -- in shared memory, applies the whole op list to it, and
-// writes it back. HBM traffic is one read and one write of the state per
-// sweep instead of per gate; the op math runs out of shared memory (swizzled
-// on 16-byte granules against bank conflicts) with the small matrices in
-// registers.
-#include "qgb_common.cuh"
+// 2^L amplitudes) times every combination of `H` chosen high bits -- in
+// shared memory, applies the whole op list to it, and writes it back. HBM
+// traffic is one read and one write of the state per sweep instead of per
+// gate.
+//
+// Two kernels share the in-tile math (sweep_common.cuh):
+//  * sweep_tma_kernel (sweep_tma.cu), the default: TMA tiled copies with the
+//    hardware 128-byte swizzle into a double buffer, so the load of the next
+//    tile overlaps the ops on the current one;
+//  * sweep_ldst_kernel (here): plain 16-byte loads/stores by all threads, used
+//    when the tile geometry is too small for TMA (runs under 128 bytes) or
+//    when QGB_SWEEP_IMPL=ldst.
+#include <cstdlib>
+#include <cstring>
+
+#include "sweep_common.cuh"
 
 namespace qgb {
 
-struct SweepArgs {
-    qgb_sweep sw;
-    int n;  // bits per vector
-    int n_outer;
-    int outer_bits[2 * QGB_MAX_QUBITS];
-    int64_t mat_stride, batch, sv_stride;
-    uint64_t tiles;  // tiles per vector
-};
-
-constexpr int kSweepThreads = 256;
-constexpr int kStageK = 4;  // ops with k >= 3 stage their matrix in shared memory (k <= 4)
-
-template <typename T, int K>
-__device__ __forceinline__ void tile_op(cplx<T>* __restrict__ tile, int m, const int* pos_in,
-                                        const cplx<T>* __restrict__ mat, cplx<T>* __restrict__ msh) {
-    constexpr int D = 1 << K;
-    using C = cplx<T>;
-    int pos[K], srt[K];
-#pragma unroll
-    for (int j = 0; j < K; ++j) pos[j] = srt[j] = pos_in[j];
-#pragma unroll
-    for (int i = 1; i < K; ++i)
-#pragma unroll
-        for (int j = i; j > 0; --j)
-            if (srt[j - 1] > srt[j]) {
-                int t = srt[j];
-                srt[j] = srt[j - 1];
-                srt[j - 1] = t;
-            }
-    uint32_t off[D];
-#pragma unroll
-    for (int r = 0; r < D; ++r) {
-        uint32_t o = 0;
-#pragma unroll
-        for (int j = 0; j < K; ++j) o |= uint32_t((r >> (K - 1 - j)) & 1) << pos[j];
-        off[r] = o;
-    }
-    const uint32_t groups = 1u << (m - K);
-    if constexpr (K <= 2) {
-        C mr[D * D];
-#pragma unroll
-        for (int i = 0; i < D * D; ++i) mr[i] = __ldg(&mat[i]);
-        for (uint32_t g = threadIdx.x; g < groups; g += blockDim.x) {
-            uint32_t base = g;
-#pragma unroll
-            for (int j = 0; j < K; ++j) base = ((base >> srt[j]) << (srt[j] + 1)) | (base & ((1u << srt[j]) - 1));
-            C v[D];
-#pragma unroll
-            for (int c = 0; c < D; ++c) v[c] = tile[swz<T>(base | off[c])];
-#pragma unroll
-            for (int r = 0; r < D; ++r) {
-                C acc = mk<T>(0, 0);
-#pragma unroll
-                for (int c = 0; c < D; ++c) cfma(acc, mr[r * D + c], v[c]);
-                tile[swz<T>(base | off[r])] = acc;
-            }
-        }
-    } else {
-        const C* mm = mat;
-        if constexpr (K <= kStageK) {
-            for (int i = threadIdx.x; i < D * D; i += blockDim.x) msh[i] = mat[i];
-            __syncthreads();
-            mm = msh;
-        }
-        for (uint32_t g = threadIdx.x; g < groups; g += blockDim.x) {
-            uint32_t base = g;
-#pragma unroll
-            for (int j = 0; j < K; ++j) base = ((base >> srt[j]) << (srt[j] + 1)) | (base & ((1u << srt[j]) - 1));
-            C v[D];
-#pragma unroll
-            for (int c = 0; c < D; ++c) v[c] = tile[swz<T>(base | off[c])];
-#pragma unroll 1
-            for (int r = 0; r < D; ++r) {
-                const C* mrow = mm + r * D;
-                C acc = mk<T>(0, 0);
-#pragma unroll
-                for (int c = 0; c < D; ++c) cfma(acc, mrow[c], v[c]);
-                uint32_t o = 0;
-#pragma unroll
-                for (int j = 0; j < K; ++j) o |= uint32_t((r >> (K - 1 - j)) & 1) << pos[j];
-                tile[swz<T>(base | o)] = acc;
-            }
-        }
-    }
-}
+constexpr int kLdstThreads = 256;
 
 template <typename T, int KMAX>
-__global__ void __launch_bounds__(kSweepThreads) sweep_kernel(cplx<T>* __restrict__ sv, const cplx<T>* __restrict__ mats,
-                                                              const __grid_constant__ SweepArgs a) {
+__global__ void __launch_bounds__(kLdstThreads) sweep_ldst_kernel(cplx<T>* __restrict__ sv, const cplx<T>* __restrict__ mats,
+                                                                  const __grid_constant__ SweepArgs a) {
     using C = cplx<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = a.sw.low_bits, H = a.sw.n_high, m = L + H;
-    // layout: tile (2^m complex) | matrix stage (4^min(KMAX,4) complex) | hoff (2^H uint64);
-    // both complex regions start on 16-byte boundaries
+    // layout: tile (2^m complex) | matrix stage | hoff (2^H uint64); complex regions 16-byte aligned
     C* tile = reinterpret_cast<C*>(smem_raw);
     C* msh = tile + (1u << m);
-    constexpr int kStage = KMAX >= 3 ? (1 << (2 * (KMAX < kStageK ? KMAX : kStageK))) : 0;
-    uint64_t* hoff = reinterpret_cast<uint64_t*>(msh + kStage);
+    uint64_t* hoff = reinterpret_cast<uint64_t*>(msh + stage_elems<KMAX>());
     for (uint32_t h = threadIdx.x; h < (1u << H); h += blockDim.x) {
         uint64_t o = 0;
         for (int j = 0; j < H; ++j) o |= uint64_t((h >> j) & 1u) << a.sw.high_bits[j];
@@ -129,37 +52,22 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_kernel(cplx<T>* __restric
         if constexpr (sizeof(T) == 4) {
             for (uint32_t e = 2 * threadIdx.x; e < (1u << m); e += 2 * blockDim.x) {
                 const uint64_t gi = base | hoff[e >> L] | (e & lmask);
-                const float4 v = *reinterpret_cast<const float4*>(s + gi);
-                *reinterpret_cast<float4*>(tile + swz<T>(e)) = v;
+                *reinterpret_cast<float4*>(tile + swz<T>(e)) = *reinterpret_cast<const float4*>(s + gi);
             }
         } else {
-            for (uint32_t e = threadIdx.x; e < (1u << m); e += blockDim.x) {
-                const uint64_t gi = base | hoff[e >> L] | (e & lmask);
-                tile[swz<T>(e)] = s[gi];
-            }
+            for (uint32_t e = threadIdx.x; e < (1u << m); e += blockDim.x)
+                tile[swz<T>(e)] = s[base | hoff[e >> L] | (e & lmask)];
         }
         __syncthreads();
-        for (int i = 0; i < a.sw.n_ops; ++i) {
-            const int k = a.sw.op_k[i];
-            const C* mat = mb + a.sw.op_mat[i];
-            const int* pos = a.sw.op_pos[i];
-            if (k == 1) tile_op<T, 1>(tile, m, pos, mat, msh);
-            else if (k == 2) { if constexpr (KMAX >= 2) tile_op<T, 2>(tile, m, pos, mat, msh); }
-            else if (k == 3) { if constexpr (KMAX >= 3) tile_op<T, 3>(tile, m, pos, mat, msh); }
-            else if (k == 4) { if constexpr (KMAX >= 4) tile_op<T, 4>(tile, m, pos, mat, msh); }
-            else if (k == 5) { if constexpr (KMAX >= 5) tile_op<T, 5>(tile, m, pos, mat, msh); }
-            __syncthreads();
-        }
+        apply_ops<T, KMAX>(tile, m, a, mb, msh);
         if constexpr (sizeof(T) == 4) {
             for (uint32_t e = 2 * threadIdx.x; e < (1u << m); e += 2 * blockDim.x) {
                 const uint64_t gi = base | hoff[e >> L] | (e & lmask);
                 *reinterpret_cast<float4*>(s + gi) = *reinterpret_cast<const float4*>(tile + swz<T>(e));
             }
         } else {
-            for (uint32_t e = threadIdx.x; e < (1u << m); e += blockDim.x) {
-                const uint64_t gi = base | hoff[e >> L] | (e & lmask);
-                s[gi] = tile[swz<T>(e)];
-            }
+            for (uint32_t e = threadIdx.x; e < (1u << m); e += blockDim.x)
+                s[base | hoff[e >> L] | (e & lmask)] = tile[swz<T>(e)];
         }
     }
 }
@@ -171,54 +79,66 @@ using namespace qgb_host;
 
 namespace {
 
-template <typename T> constexpr int max_sweep_k() { return sizeof(T) == 4 ? 5 : 4; }
-
 template <typename T>
-size_t sweep_smem_bytes(int m, int H, int kmax) {
-    // kmax is rounded up to the launched instantiation (1 -> 2)
-    if (kmax < 2) kmax = 2;
-    size_t stage = kmax >= 3 ? (size_t(1) << (2 * (kmax < kStageK ? kmax : kStageK))) : 0;
+size_t ldst_smem_bytes(int m, int H, int kmax_inst) {
+    size_t stage = kmax_inst >= 3 ? (size_t(1) << (2 * (kmax_inst < kStageK ? kmax_inst : kStageK))) : 0;
     return sizeof(cplx<T>) * ((size_t(1) << m) + stage) + sizeof(uint64_t) * (size_t(1) << H);
 }
 
 template <typename T, int KMAX>
-int launch_sweep(void* sv, const void* mats, const SweepArgs& a, size_t smem, cudaStream_t st) {
+int launch_ldst(void* sv, const void* mats, const SweepArgs& a, cudaStream_t st) {
+    const int m = a.sw.low_bits + a.sw.n_high;
+    const size_t smem = ldst_smem_bytes<T>(m, a.sw.n_high, KMAX);
+    if (smem > 227 * 1024) return set_error(QGB_EINVAL, "sweep needs %zu bytes of shared memory", smem);
     static bool attr = false;
     if (!attr) {
-        if (cudaFuncSetAttribute(sweep_kernel<T, KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) !=
+        if (cudaFuncSetAttribute(sweep_ldst_kernel<T, KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) !=
             cudaSuccess)
             return check_launch("sweep attribute");
         attr = true;
     }
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel<T, KMAX>, kSweepThreads, smem) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_ldst_kernel<T, KMAX>, kLdstThreads, smem) !=
         cudaSuccess)
         return check_launch("sweep occupancy");
     if (per_sm < 1) return set_error(QGB_EINVAL, "sweep tile of %zu bytes does not fit on an SM", smem);
     const uint64_t total = uint64_t(a.batch) * a.tiles;
     uint64_t grid = uint64_t(per_sm) * sm_count();
     if (grid > total) grid = total;
-    sweep_kernel<T, KMAX><<<unsigned(grid), kSweepThreads, smem, st>>>((cplx<T>*)sv, (const cplx<T>*)mats, a);
+    sweep_ldst_kernel<T, KMAX><<<unsigned(grid), kLdstThreads, smem, st>>>((cplx<T>*)sv, (const cplx<T>*)mats, a);
     return check_launch("sweep kernel");
 }
 
 template <typename T>
-int dispatch_sweep(void* sv, const void* mats, const SweepArgs& a, int kmax, cudaStream_t st) {
-    const int m = a.sw.low_bits + a.sw.n_high;
-    const size_t smem = sweep_smem_bytes<T>(m, a.sw.n_high, kmax);
-    if (smem > 227 * 1024) return set_error(QGB_EINVAL, "sweep needs %zu bytes of shared memory", smem);
+int dispatch_ldst(void* sv, const void* mats, const SweepArgs& a, int kmax, cudaStream_t st) {
     switch (kmax) {
         case 1:
-        case 2: return launch_sweep<T, 2>(sv, mats, a, smem, st);
-        case 3: return launch_sweep<T, 3>(sv, mats, a, smem, st);
-        case 4: return launch_sweep<T, 4>(sv, mats, a, smem, st);
+        case 2: return launch_ldst<T, 2>(sv, mats, a, st);
+        case 3: return launch_ldst<T, 3>(sv, mats, a, st);
+        case 4: return launch_ldst<T, 4>(sv, mats, a, st);
         case 5:
-            if constexpr (max_sweep_k<T>() >= 5) return launch_sweep<T, 5>(sv, mats, a, smem, st);
+            if constexpr (sizeof(T) == 4) return launch_ldst<T, 5>(sv, mats, a, st);
     }
     return set_error(QGB_EINVAL, "sweep op width %d unsupported for this dtype", kmax);
 }
 
+int g_sweep_impl = -1;  // 0 = TMA when eligible, 1 = load/store kernel only
+
+int sweep_impl() {
+    if (g_sweep_impl < 0) {
+        const char* e = getenv("QGB_SWEEP_IMPL");
+        g_sweep_impl = (e && strcmp(e, "ldst") == 0) ? 1 : 0;
+    }
+    return g_sweep_impl;
+}
+
 }  // namespace
+
+extern "C" int qgb_set_sweep_impl(int impl) {
+    if (impl != 0 && impl != 1) return set_error(QGB_EINVAL, "sweep implementation %d unknown (0 = TMA, 1 = load/store)", impl);
+    g_sweep_impl = impl;
+    return QGB_OK;
+}
 
 extern "C" int qgb_apply_sweep(void* sv, int dtype, int n, const qgb_sweep* sweep, const void* mats,
                                int64_t mat_stride, int64_t batch, int64_t sv_stride, void* stream) {
@@ -240,7 +160,7 @@ extern "C" int qgb_apply_sweep(void* sv, int dtype, int n, const qgb_sweep* swee
     SweepArgs a{};
     a.sw = sw;
     a.n = n;
-    uint64_t in_tile = (L >= 64) ? ~0ull : ((1ull << L) - 1);
+    uint64_t in_tile = (1ull << L) - 1;
     int prev = L - 1;
     for (int h = 0; h < H; ++h) {
         const int b = sw.high_bits[h];
@@ -271,5 +191,9 @@ extern "C" int qgb_apply_sweep(void* sv, int dtype, int n, const qgb_sweep* swee
     a.sv_stride = sv_stride;
     a.tiles = uint64_t(1) << (n - m);
     cudaStream_t st = (cudaStream_t)stream;
-    return dtype == QGB_C64 ? dispatch_sweep<float>(sv, mats, a, kmax, st) : dispatch_sweep<double>(sv, mats, a, kmax, st);
+    if (sweep_impl() == 0) {
+        const int rc = launch_sweep_tma(dtype, sv, mats, a, kmax, st);
+        if (rc != 1) return rc;
+    }
+    return dtype == QGB_C64 ? dispatch_ldst<float>(sv, mats, a, kmax, st) : dispatch_ldst<double>(sv, mats, a, kmax, st);
 }
