@@ -331,8 +331,8 @@ def main():
     p.add_argument("--depth", type=int, default=DEPTH)
     p.add_argument("--dtype", default="c64", choices=["c64", "c128"])
     p.add_argument("--mode", default="sweep", choices=["gate", "fused", "sweep"])
-    p.add_argument("--width", type=int, default=2)
-    p.add_argument("--tile", type=int, default=13)
+    p.add_argument("--width", type=int, default=4)
+    p.add_argument("--tile", type=int, default=14)
     p.add_argument("--low", type=int, default=None)
     p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--no-e2e", action="store_true")

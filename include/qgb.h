@@ -84,8 +84,9 @@ int qgb_op_action(void* sv, int dtype, int n, const int* indices, int k, const v
 int qgb_apply_sweep(void* sv, int dtype, int n, const qgb_sweep* sweep, const void* mats,
                     int64_t mat_stride, int64_t batch, int64_t sv_stride, void* stream);
 
-/* Selects the sweep kernel: 0 (default) = TMA-staged double-buffered tiles
- * when the geometry allows it, 1 = plain load/store tiles. Process-wide. */
+/* Selects the sweep kernel: 0 (default) = cp.async double-buffered tiles,
+ * 1 = TMA-staged tiles with a producer warp when the geometry allows it
+ * (runs of at least 128 bytes). Process-wide; both give identical results. */
 int qgb_set_sweep_impl(int impl);
 
 /* Writes |bits> (StatevectorSim.initialize_state, :31-48) to `batch` states. */

@@ -20,31 +20,22 @@ constexpr int kStageK = 4;  // ops with 3 <= k <= 4 stage their matrix in shared
 
 template <int KMAX> __host__ __device__ constexpr int stage_elems() { return KMAX >= 3 ? (1 << (2 * (KMAX < kStageK ? KMAX : kStageK))) : 0; }
 
-// ---- packed fp32x2 arithmetic (one instruction = two FMAs) ----------------
-__device__ __forceinline__ uint64_t pack2(float lo, float hi) {
-    uint64_t r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "r"(__float_as_uint(lo)), "r"(__float_as_uint(hi)));
-    return r;
-}
-__device__ __forceinline__ uint64_t swap2(uint64_t v) {
-    uint32_t lo, hi;
-    asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "l"(v));
-    uint64_t r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "r"(hi), "r"(lo));
-    return r;
-}
-__device__ __forceinline__ uint64_t ffma2(uint64_t a, uint64_t b, uint64_t c) {
-    uint64_t d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
+// Barrier over the threads that run the ops: the whole CTA, or (in the
+// warp-specialised kernel) only the compute warps, on named barrier 1.
+struct CtaSync {
+    __device__ static void sync(int) { __syncthreads(); }
+};
+struct ComputeSync {
+    __device__ static void sync(int nthr) { asm volatile("bar.sync 1, %0;" ::"r"(nthr) : "memory"); }
+};
 
-// Applies one dense op of width K to the whole tile. `tile` is swizzled with
-// swz<T>, which is linear over XOR, so swz(base | off) = swz(base) ^ swz(off)
-// and the per-access address costs one XOR.
-template <typename T, int K>
+// Applies one dense op of width K to the whole tile, threads tid = 0..nthr-1.
+// `tile` is swizzled with swz<T>, which is linear over XOR, so
+// swz(base | off) = swz(base) ^ swz(off) and each access costs one XOR.
+template <typename T, int K, typename Sync>
 __device__ __forceinline__ void tile_op(cplx<T>* __restrict__ tile, int m, const int* pos_in,
-                                        const cplx<T>* __restrict__ mat, cplx<T>* __restrict__ msh) {
+                                        const cplx<T>* __restrict__ mat, cplx<T>* __restrict__ msh, int tid,
+                                        int nthr) {
     constexpr int D = 1 << K;
     using C = cplx<T>;
     int pos[K], srt[K];
@@ -68,43 +59,11 @@ __device__ __forceinline__ void tile_op(cplx<T>* __restrict__ tile, int m, const
         soff[r] = swz<T>(o);
     }
     const uint32_t groups = 1u << (m - K);
-    if constexpr (K <= 2 && sizeof(T) == 4) {
-        // complex MAC as two packed FMAs: acc += (m.x, m.x) * (v.x, v.y) + (-m.y, m.y) * (v.y, v.x)
-        uint64_t A1[D * D], A2[D * D];
-#pragma unroll
-        for (int i = 0; i < D * D; ++i) {
-            const float2 mm = __ldg(reinterpret_cast<const float2*>(mat) + i);
-            A1[i] = pack2(mm.x, mm.x);
-            A2[i] = pack2(-mm.y, mm.y);
-        }
-        uint64_t* t64 = reinterpret_cast<uint64_t*>(tile);
-        for (uint32_t g = threadIdx.x; g < groups; g += blockDim.x) {
-            uint32_t base = g;
-#pragma unroll
-            for (int j = 0; j < K; ++j) base = ((base >> srt[j]) << (srt[j] + 1)) | (base & ((1u << srt[j]) - 1));
-            const uint32_t sb = swz<T>(base);
-            uint64_t v[D], vs[D];
-#pragma unroll
-            for (int c = 0; c < D; ++c) {
-                v[c] = t64[sb ^ soff[c]];
-                vs[c] = swap2(v[c]);
-            }
-#pragma unroll
-            for (int r = 0; r < D; ++r) {
-                uint64_t acc = 0;
-#pragma unroll
-                for (int c = 0; c < D; ++c) {
-                    acc = ffma2(A1[r * D + c], v[c], acc);
-                    acc = ffma2(A2[r * D + c], vs[c], acc);
-                }
-                t64[sb ^ soff[r]] = acc;
-            }
-        }
-    } else if constexpr (K <= 2) {
+    if constexpr (K <= 2) {
         C mr[D * D];
 #pragma unroll
         for (int i = 0; i < D * D; ++i) mr[i] = __ldg(&mat[i]);
-        for (uint32_t g = threadIdx.x; g < groups; g += blockDim.x) {
+        for (uint32_t g = tid; g < groups; g += nthr) {
             uint32_t base = g;
 #pragma unroll
             for (int j = 0; j < K; ++j) base = ((base >> srt[j]) << (srt[j] + 1)) | (base & ((1u << srt[j]) - 1));
@@ -121,48 +80,78 @@ __device__ __forceinline__ void tile_op(cplx<T>* __restrict__ tile, int m, const
             }
         }
     } else {
+        // Wide op: the matrix is read from shared memory (staged for K <= 4),
+        // two element pairs per 16-byte load, and every element feeds two groups.
         const C* mm = mat;
         if constexpr (K <= kStageK) {
-            for (int i = threadIdx.x; i < D * D; i += blockDim.x) msh[i] = mat[i];
-            __syncthreads();
+            for (int i = tid; i < D * D; i += nthr) msh[i] = mat[i];
+            Sync::sync(nthr);
             mm = msh;
         }
-        for (uint32_t g = threadIdx.x; g < groups; g += blockDim.x) {
-            uint32_t base = g;
+        // groups g and g + half go together (a single group is processed twice when the op spans the tile)
+        const uint32_t half = groups > 1 ? groups >> 1 : 1;
+        for (uint32_t g = tid; g < half; g += nthr) {
+            uint32_t b0 = g, b1 = groups > 1 ? g + half : g;
 #pragma unroll
-            for (int j = 0; j < K; ++j) base = ((base >> srt[j]) << (srt[j] + 1)) | (base & ((1u << srt[j]) - 1));
-            const uint32_t sb = swz<T>(base);
-            C v[D];
+            for (int j = 0; j < K; ++j) {
+                b0 = ((b0 >> srt[j]) << (srt[j] + 1)) | (b0 & ((1u << srt[j]) - 1));
+                b1 = ((b1 >> srt[j]) << (srt[j] + 1)) | (b1 & ((1u << srt[j]) - 1));
+            }
+            const uint32_t s0 = swz<T>(b0), s1 = swz<T>(b1);
+            C v0[D], v1[D];
 #pragma unroll
-            for (int c = 0; c < D; ++c) v[c] = tile[sb ^ soff[c]];
+            for (int c = 0; c < D; ++c) {
+                v0[c] = tile[s0 ^ soff[c]];
+                v1[c] = tile[s1 ^ soff[c]];
+            }
 #pragma unroll 1
             for (int r = 0; r < D; ++r) {
                 const C* mrow = mm + r * D;
-                C acc = mk<T>(0, 0);
+                C a0 = mk<T>(0, 0), a1 = mk<T>(0, 0);
+                if constexpr (sizeof(T) == 4) {
+                    const float4* m4 = reinterpret_cast<const float4*>(mrow);
 #pragma unroll
-                for (int c = 0; c < D; ++c) cfma(acc, mrow[c], v[c]);
+                    for (int c = 0; c < D; c += 2) {
+                        const float4 q = m4[c >> 1];
+                        const C e0 = mk<T>(q.x, q.y), e1 = mk<T>(q.z, q.w);
+                        cfma(a0, e0, v0[c]);
+                        cfma(a1, e0, v1[c]);
+                        cfma(a0, e1, v0[c + 1]);
+                        cfma(a1, e1, v1[c + 1]);
+                    }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < D; ++c) {
+                        const C e = mrow[c];
+                        cfma(a0, e, v0[c]);
+                        cfma(a1, e, v1[c]);
+                    }
+                }
                 uint32_t o = 0;
 #pragma unroll
                 for (int j = 0; j < K; ++j) o |= uint32_t((r >> (K - 1 - j)) & 1) << pos[j];
-                tile[sb ^ swz<T>(o)] = acc;
+                const uint32_t so = swz<T>(o);
+                tile[s0 ^ so] = a0;
+                tile[s1 ^ so] = a1;
             }
         }
     }
 }
 
-// All ops of a sweep on one staged tile, with a CTA barrier after each op.
-template <typename T, int KMAX>
-__device__ __forceinline__ void apply_ops(cplx<T>* tile, int m, const SweepArgs& a, const cplx<T>* mb, cplx<T>* msh) {
+// All ops of a sweep on one staged tile, with a barrier after each op.
+template <typename T, int KMAX, typename Sync>
+__device__ __forceinline__ void apply_ops(cplx<T>* tile, int m, const SweepArgs& a, const cplx<T>* mb, cplx<T>* msh,
+                                          int tid, int nthr) {
     for (int i = 0; i < a.sw.n_ops; ++i) {
         const int k = a.sw.op_k[i];
         const cplx<T>* mat = mb + a.sw.op_mat[i];
         const int* pos = a.sw.op_pos[i];
-        if (k == 1) tile_op<T, 1>(tile, m, pos, mat, msh);
-        else if (k == 2) { if constexpr (KMAX >= 2) tile_op<T, 2>(tile, m, pos, mat, msh); }
-        else if (k == 3) { if constexpr (KMAX >= 3) tile_op<T, 3>(tile, m, pos, mat, msh); }
-        else if (k == 4) { if constexpr (KMAX >= 4) tile_op<T, 4>(tile, m, pos, mat, msh); }
-        else if (k == 5) { if constexpr (KMAX >= 5) tile_op<T, 5>(tile, m, pos, mat, msh); }
-        __syncthreads();
+        if (k == 1) tile_op<T, 1, Sync>(tile, m, pos, mat, msh, tid, nthr);
+        else if (k == 2) { if constexpr (KMAX >= 2) tile_op<T, 2, Sync>(tile, m, pos, mat, msh, tid, nthr); }
+        else if (k == 3) { if constexpr (KMAX >= 3) tile_op<T, 3, Sync>(tile, m, pos, mat, msh, tid, nthr); }
+        else if (k == 4) { if constexpr (KMAX >= 4) tile_op<T, 4, Sync>(tile, m, pos, mat, msh, tid, nthr); }
+        else if (k == 5) { if constexpr (KMAX >= 5) tile_op<T, 5, Sync>(tile, m, pos, mat, msh, tid, nthr); }
+        Sync::sync(nthr);
     }
 }
 

@@ -67,7 +67,7 @@ def gates_to_ops(seq, n):
 
 class StatevectorSim:
     def __init__(self, circ, init_state=None, backend="torch", device="cuda", dtype=torch.complex64,
-                 mode="sweep", fusion_width=2, tile_bits=13, low_bits=None, nm=None):
+                 mode="sweep", fusion_width=4, tile_bits=14, low_bits=None, nm=None):
         self.circ = circ.copy() if hasattr(circ, "copy") else circ
         self.num_sites = circ.num_sites
         self.local_dim = getattr(circ, "local_dim", 2)
