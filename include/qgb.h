@@ -132,6 +132,34 @@ int qgb_partial_overlap(const void* a, const void* b, int dtype, int n, const in
                         int64_t batch, int64_t sv_stride, double* out, void* scratch,
                         size_t scratch_bytes, void* stream);
 
+/* ---- noisy trajectories -------------------------------------------------- */
+
+/* Blocks per trajectory used by qgb_traj_step (sizes its `partials`: at least
+ * ntraj * qgb_traj_blocks(n) * 4 doubles). */
+int qgb_traj_blocks(int n);
+
+/* One gate of a batch of `ntraj` noisy trajectories (states of n qubits,
+ * `stride` elements apart), replacing the per-sample statevector runs of
+ * MonteCarloSim (tensorQ/monte_carlo_sim.py:14-35) and extending them to
+ * amplitude damping. Applies, per trajectory: the pending normalised Kraus
+ * operators of the previous gate's sites (`prev_sites`, `kprev`; read from
+ * `kraus`), then the gate (`sites`, `k` <= 2, device matrix `gate`), then an
+ * independent depolarising Pauli (I w.p. 1-p_dep, X/Y/Z w.p. p_dep/3) on each
+ * gate site; then draws each site's amplitude-damping branch (gamma) from the
+ * exact populations and overwrites `kraus` (device, ntraj x 2 x 4 complex of
+ * the state dtype) with the chosen K0/sqrt(1-p) or K1/sqrt(p) for the next
+ * call. k = 0 only applies the pending operators. Random numbers are
+ * Philox4x32-10 of (event, trajectory, 2*site + {0: Pauli, 1: damping}) keyed
+ * by `seed`; `event` must be unique per gate of a run. pauli_log / jump_log
+ * (device, ntraj x 2 bytes, or NULL) record the branches. */
+int qgb_traj_step(void* sv, int dtype, int n, int64_t ntraj, int64_t stride, const int* sites, int k,
+                  const void* gate, const int* prev_sites, int kprev, void* kraus, double p_dep, double gamma,
+                  uint64_t seed, uint32_t event, double* partials, uint8_t* pauli_log, uint8_t* jump_log,
+                  void* stream);
+
+/* The Philox uniform the trajectory kernels draw (host-side, for replays). */
+void qgb_philox_uniform(uint32_t event, uint32_t traj, uint32_t stream, uint64_t seed, double* out);
+
 /* ---- density matrix ---------------------------------------------------- */
 
 /* Replaces DensityMatrixSim.apply_gate (tensorQ/density_matrix_sim.py:38-42)

@@ -1,0 +1,410 @@
+// Batched noisy trajectories (Monte-Carlo wavefunction unravelling).
+//
+// The reference samples noisy circuits one at a time on the CPU
+// (MonteCarloSim, tensorQ/monte_carlo_sim.py:14-35) and only for Pauli
+// channels; amplitude damping exists only as a density-matrix superoperator
+// (core/noise.py:29-49). Here all trajectories advance together, one gate at a
+// time, each keeping its own normalised 2^n state:
+//
+//  * traj_gate_kernel: per (trajectory, block) CTA, compose in shared memory
+//    the trajectory's op on the union U of the gate's sites and the previous
+//    gate's sites (at most 4 bits): the previous gate's pending Kraus
+//    operators (normalised), then the gate, then the depolarising Paulis
+//    sampled for this trajectory and gate; apply it to every group of 2^|U|
+//    amplitudes; accumulate |out_r|^2 per output row r (float64 partials).
+//  * traj_decide_kernel: one thread per trajectory sums the partials into the
+//    joint populations of the gate's sites and draws the amplitude-damping
+//    branches site by site (exact sequential probabilities gamma * P(1)),
+//    writing the normalised Kraus operators K0/sqrt(1-p) or K1/sqrt(p) that
+//    the next traj_gate launch applies, and logging the branches.
+//
+// Random numbers: Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random
+// numbers: as easy as 1, 2, 3", SC'11), counter = (event, trajectory, stream,
+// 0), key = the run's seed; 53-bit uniforms from two output words.
+#include "qgb_common.cuh"
+
+namespace qgb {
+
+struct Philox {
+    __host__ __device__ static inline void mulhilo(uint32_t a, uint32_t b, uint32_t& hi, uint32_t& lo) {
+        const uint64_t p = uint64_t(a) * uint64_t(b);
+        hi = uint32_t(p >> 32);
+        lo = uint32_t(p);
+    }
+    // ten rounds of the Philox4x32 bijection
+    __host__ __device__ static inline void gen(uint32_t c[4], uint32_t k0, uint32_t k1) {
+        for (int r = 0; r < 10; ++r) {
+            uint32_t hi0, lo0, hi1, lo1;
+            mulhilo(0xD2511F53u, c[0], hi0, lo0);
+            mulhilo(0xCD9E8D57u, c[2], hi1, lo1);
+            const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+            c[0] = n0;
+            c[1] = lo1;
+            c[2] = n2;
+            c[3] = lo0;
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+    }
+    // uniform in [0, 1) with 53 random bits
+    __host__ __device__ static inline double uniform(uint32_t event, uint32_t traj, uint32_t stream, uint32_t k0,
+                                                     uint32_t k1) {
+        uint32_t c[4] = {event, traj, stream, 0u};
+        gen(c, k0, k1);
+        const uint64_t bits = (uint64_t(c[0]) << 21) ^ uint64_t(c[1] >> 11);
+        return double(bits & ((uint64_t(1) << 53) - 1)) * (1.0 / 9007199254740992.0);
+    }
+};
+
+struct TrajGateArgs {
+    int n;
+    int64_t ntraj, stride;
+    int ku;            // |U|: union bits (0..4)
+    int ubits[4];      // flat bits of U, matrix order (bit ku-1-j of the local index <-> ubits[j])
+    int kg;            // gate width (0..2); gate site j is U position gpos[j]
+    int gpos[2];
+    int kp;            // pending Kraus sites (0..2); site j is U position ppos[j]
+    int ppos[2];
+    double p_dep;      // depolarising probability per gate site (0 = none)
+    uint32_t seed0, seed1, event;
+    int nblk;
+    int log_paulis;    // write the sampled Pauli indices to the log
+};
+
+// out = A (2x2 on U position p) applied to the rows of X (D x D), i.e. X <- (A on p) X
+template <typename C>
+__device__ void left_apply_1q(C* X, int D, int ku, int p, const C A[4], C* tmp) {
+    const int bit = 1 << (ku - 1 - p);
+    for (int idx = threadIdx.x; idx < D * D; idx += blockDim.x) {
+        const int r = idx / D, c = idx % D;
+        const int r0 = r & ~bit, a = (r & bit) ? 1 : 0;
+        C acc;
+        acc.x = 0;
+        acc.y = 0;
+        for (int bb = 0; bb < 2; ++bb) {
+            const C m = A[2 * a + bb];
+            const C x = X[(r0 | (bb ? bit : 0)) * D + c];
+            cfma(acc, m, x);
+        }
+        tmp[idx] = acc;
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < D * D; idx += blockDim.x) X[idx] = tmp[idx];
+    __syncthreads();
+}
+
+template <typename T, int K>
+__global__ void __launch_bounds__(256) traj_gate_kernel(cplx<T>* __restrict__ sv, const cplx<T>* __restrict__ gate,
+                                                        const cplx<T>* __restrict__ kraus, double* __restrict__ partials,
+                                                        uint8_t* __restrict__ pauli_log, const __grid_constant__ TrajGateArgs a) {
+    using C = cplx<T>;
+    constexpr int D = 1 << K;
+    __shared__ C W[D * D], tmp[D * D];
+    __shared__ double red[8][4];
+    const int64_t t = blockIdx.y;
+    // ---- compose W = (Paulis on gate sites) (gate on gate sites) (pending Kraus on their sites)
+    for (int idx = threadIdx.x; idx < D * D; idx += blockDim.x) {
+        const int r = idx / D, c = idx % D;
+        W[idx] = mk<T>(r == c ? T(1) : T(0), T(0));
+    }
+    __syncthreads();
+    for (int j = 0; j < a.kp; ++j) {
+        C A[4];
+        const C* kj = kraus + (t * 2 + j) * 4;
+        for (int e = 0; e < 4; ++e) A[e] = kj[e];
+        left_apply_1q<C>(W, D, K, a.ppos[j], A, tmp);
+    }
+    if (a.kg > 0) {
+        // X <- G X with G on gate positions (kg = 1 or 2)
+        const int gd = 1 << a.kg;
+        for (int idx = threadIdx.x; idx < D * D; idx += blockDim.x) {
+            const int r = idx / D, c = idx % D;
+            int gr = 0, rest = r;
+            for (int j = 0; j < a.kg; ++j) {
+                const int bit = 1 << (K - 1 - a.gpos[j]);
+                gr |= ((r & bit) ? 1 : 0) << (a.kg - 1 - j);
+                rest &= ~bit;
+            }
+            C acc = mk<T>(0, 0);
+            for (int gc = 0; gc < gd; ++gc) {
+                int rr = rest;
+                for (int j = 0; j < a.kg; ++j)
+                    if ((gc >> (a.kg - 1 - j)) & 1) rr |= 1 << (K - 1 - a.gpos[j]);
+                cfma(acc, gate[gr * gd + gc], W[rr * D + c]);
+            }
+            tmp[idx] = acc;
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < D * D; idx += blockDim.x) W[idx] = tmp[idx];
+        __syncthreads();
+        if (a.p_dep > 0) {
+            for (int j = 0; j < a.kg; ++j) {
+                const double u = Philox::uniform(a.event, uint32_t(t), 2u * j, a.seed0, a.seed1);
+                // I with 1-p, X, Y, Z with p/3 each
+                int pk = 0;
+                if (u >= 1.0 - a.p_dep) pk = 1 + min(2, int((u - (1.0 - a.p_dep)) / (a.p_dep / 3.0)));
+                if (a.log_paulis && blockIdx.x == 0 && threadIdx.x == 0) pauli_log[t * 2 + j] = uint8_t(pk);
+                if (pk == 0) continue;
+                C P[4];
+                P[0] = P[1] = P[2] = P[3] = mk<T>(0, 0);
+                if (pk == 1) { P[1] = mk<T>(1, 0); P[2] = mk<T>(1, 0); }
+                else if (pk == 2) { P[1] = mk<T>(0, -1); P[2] = mk<T>(0, 1); }
+                else { P[0] = mk<T>(1, 0); P[3] = mk<T>(-1, 0); }
+                left_apply_1q<C>(W, D, K, a.gpos[j], P, tmp);
+            }
+        }
+    }
+    // ---- apply W to every group of the trajectory's state, accumulate |out_r|^2
+    int srt[K > 0 ? K : 1];
+    for (int j = 0; j < K; ++j) srt[j] = a.ubits[j];
+    for (int i = 1; i < K; ++i)
+        for (int j = i; j > 0 && srt[j - 1] > srt[j]; --j) {
+            const int x = srt[j];
+            srt[j] = srt[j - 1];
+            srt[j - 1] = x;
+        }
+    // bucket(r): the gate sites' bits of output row r (2 bits per row, packed)
+    uint32_t bk = 0;
+    for (int r = 0; r < D; ++r) {
+        int b = 0;
+        for (int j = 0; j < a.kg; ++j) b |= ((r >> (K - 1 - a.gpos[j])) & 1) << (a.kg - 1 - j);
+        bk |= uint32_t(b) << (2 * r);
+    }
+    C* s = sv + t * a.stride;
+    const uint64_t groups = uint64_t(1) << (a.n - K), step = uint64_t(a.nblk) * blockDim.x;
+    double p0 = 0, p1 = 0, p2 = 0, p3 = 0;
+    auto add_pop = [&](int r, const C& o) {
+        const double w = double(o.x) * o.x + double(o.y) * o.y;
+        const uint32_t b = (bk >> (2 * r)) & 3u;
+        p0 += b == 0 ? w : 0.0;
+        p1 += b == 1 ? w : 0.0;
+        p2 += b == 2 ? w : 0.0;
+        p3 += b == 3 ? w : 0.0;
+    };
+    for (uint64_t g = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; g < groups; g += step) {
+        uint64_t base = g;
+        for (int j = 0; j < K; ++j) base = ((base >> srt[j]) << (srt[j] + 1)) | (base & ((uint64_t(1) << srt[j]) - 1));
+        C v[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            uint64_t o = 0;
+#pragma unroll
+            for (int j = 0; j < K; ++j) o |= uint64_t((c >> (K - 1 - j)) & 1) << a.ubits[j];
+            v[c] = s[base + o];
+        }
+        if constexpr (K <= 2) {
+#pragma unroll
+            for (int r = 0; r < D; ++r) {
+                C acc = mk<T>(0, 0);
+#pragma unroll
+                for (int c = 0; c < D; ++c) cfma(acc, W[r * D + c], v[c]);
+                uint64_t o = 0;
+#pragma unroll
+                for (int j = 0; j < K; ++j) o |= uint64_t((r >> (K - 1 - j)) & 1) << a.ubits[j];
+                s[base + o] = acc;
+                add_pop(r, acc);
+            }
+        } else {
+#pragma unroll 1
+            for (int r = 0; r < D; ++r) {
+                const C* wr = W + r * D;
+                C acc = mk<T>(0, 0);
+#pragma unroll
+                for (int c = 0; c < D; ++c) cfma(acc, wr[c], v[c]);
+                uint64_t o = 0;
+                for (int j = 0; j < K; ++j) o |= uint64_t((r >> (K - 1 - j)) & 1) << a.ubits[j];
+                s[base + o] = acc;
+                add_pop(r, acc);
+            }
+        }
+    }
+    // block reduction of the 4 joint populations -> partials[(t * nblk + blk) * 4 + b]
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double pv[4] = {p0, p1, p2, p3};
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        double x = pv[b];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) red[warp][b] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double x = 0;
+        for (int w = 0; w < int(blockDim.x / 32); ++w) x += red[w][threadIdx.x];
+        partials[(t * a.nblk + blockIdx.x) * 4 + threadIdx.x] = x;
+    }
+}
+
+struct TrajDecideArgs {
+    int64_t ntraj;
+    int ku, nblk;
+    int kg, gpos[2];   // gate sites as U positions (the damped sites, in order)
+    double gamma;
+    uint32_t seed0, seed1, event;
+};
+
+// One thread per trajectory: joint populations of the gate sites -> sequential
+// amplitude-damping branches -> normalised Kraus operators for the next launch.
+template <typename T>
+__global__ void traj_decide_kernel(const double* __restrict__ partials, cplx<T>* __restrict__ kraus,
+                                   uint8_t* __restrict__ jump_log, const __grid_constant__ TrajDecideArgs a) {
+    const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= a.ntraj) return;
+    double P[4] = {0, 0, 0, 0};  // P[2*b0 + b1] (kg = 2) or P[b0] (kg = 1) over the gate sites' bits
+    for (int blk = 0; blk < a.nblk; ++blk) {
+        const double* p = partials + (t * a.nblk + blk) * 4;
+        for (int b = 0; b < 4; ++b) P[b] += p[b];
+    }
+    const double g = a.gamma;
+    for (int j = 0; j < a.kg; ++j) {
+        // population of site j being 1
+        double tot = 0, p1 = 0;
+        for (int i = 0; i < (1 << a.kg); ++i) {
+            tot += P[i];
+            if ((i >> (a.kg - 1 - j)) & 1) p1 += P[i];
+        }
+        const double pj = tot > 0 ? g * p1 / tot : 0.0;
+        const double u = Philox::uniform(a.event, uint32_t(t), 2u * j + 1u, a.seed0, a.seed1);
+        const bool jump = u < pj;
+        cplx<T>* K = kraus + (t * 2 + j) * 4;
+        if (jump) {
+            // K1 = sqrt(g) |0><1| / sqrt(pj)
+            K[0] = mk<T>(0, 0);
+            K[1] = mk<T>(T(sqrt(g / pj)), 0);
+            K[2] = mk<T>(0, 0);
+            K[3] = mk<T>(0, 0);
+            // K1 annihilates the site-0 components and moves site-1 weight (times g) to site 0
+            for (int i = 0; i < (1 << a.kg); ++i)
+                if ((i >> (a.kg - 1 - j)) & 1) {
+                    P[i & ~(1 << (a.kg - 1 - j))] = g * P[i];
+                    P[i] = 0;
+                }
+        } else {
+            // K0 = diag(1, sqrt(1-g)) / sqrt(1-pj)
+            const double s = 1.0 / sqrt(1.0 - pj);
+            K[0] = mk<T>(T(s), 0);
+            K[1] = mk<T>(0, 0);
+            K[2] = mk<T>(0, 0);
+            K[3] = mk<T>(T(s * sqrt(1.0 - g)), 0);
+            for (int i = 0; i < (1 << a.kg); ++i)
+                if ((i >> (a.kg - 1 - j)) & 1) P[i] *= (1.0 - g);
+        }
+        if (jump_log) jump_log[t * 2 + j] = jump ? 1 : 0;
+    }
+}
+
+}  // namespace qgb
+
+using namespace qgb;
+using namespace qgb_host;
+
+namespace {
+
+template <typename T, int K>
+int launch_gate(void* sv, const void* gate, const void* kraus, double* partials, uint8_t* plog, const TrajGateArgs& a,
+                cudaStream_t st) {
+    dim3 grid(unsigned(a.nblk), unsigned(a.ntraj));
+    traj_gate_kernel<T, K><<<grid, 256, 0, st>>>((cplx<T>*)sv, (const cplx<T>*)gate, (const cplx<T>*)kraus, partials,
+                                                 plog, a);
+    return check_launch("trajectory gate kernel");
+}
+
+template <typename T>
+int dispatch_gate(void* sv, const void* gate, const void* kraus, double* partials, uint8_t* plog, const TrajGateArgs& a,
+                  cudaStream_t st) {
+    switch (a.ku) {
+        case 1: return launch_gate<T, 1>(sv, gate, kraus, partials, plog, a, st);
+        case 2: return launch_gate<T, 2>(sv, gate, kraus, partials, plog, a, st);
+        case 3: return launch_gate<T, 3>(sv, gate, kraus, partials, plog, a, st);
+        case 4: return launch_gate<T, 4>(sv, gate, kraus, partials, plog, a, st);
+    }
+    return set_error(QGB_EINVAL, "union of gate and pending sites has %d bits (1..4 supported)", a.ku);
+}
+
+}  // namespace
+
+extern "C" int qgb_traj_blocks(int n) {
+    // blocks per trajectory: about 16 groups per thread, at most 64 blocks
+    const int64_t groups = int64_t(1) << (n > 4 ? n - 4 : 0);
+    int64_t b = groups / (256 * 16);
+    if (b < 1) b = 1;
+    if (b > 64) b = 64;
+    return int(b);
+}
+
+extern "C" int qgb_traj_step(void* sv, int dtype, int n, int64_t ntraj, int64_t stride, const int* sites, int k,
+                             const void* gate, const int* prev_sites, int kprev, void* kraus, double p_dep,
+                             double gamma, uint64_t seed, uint32_t event, double* partials, uint8_t* pauli_log,
+                             uint8_t* jump_log, void* stream) {
+    if (!sv || !kraus || !partials) return set_error(QGB_EINVAL, "null pointer");
+    if (dtype != QGB_C64 && dtype != QGB_C128) return set_error(QGB_EINVAL, "dtype %d unknown", dtype);
+    if (n < 1 || n > QGB_MAX_QUBITS) return set_error(QGB_EINVAL, "n=%d invalid", n);
+    if (ntraj < 1 || ntraj > 65535) return set_error(QGB_EINVAL, "ntraj %lld not in [1, 65535]", (long long)ntraj);
+    if (ntraj > 1 && stride < (int64_t(1) << n)) return set_error(QGB_EINVAL, "trajectory stride too small");
+    if (k < 0 || k > 2 || kprev < 0 || kprev > 2) return set_error(QGB_EINVAL, "gate and pending widths must be 0..2");
+    if (k > 0 && (!sites || !gate)) return set_error(QGB_EINVAL, "gate sites/matrix missing");
+    if (kprev > 0 && !prev_sites) return set_error(QGB_EINVAL, "pending sites missing");
+    if (p_dep < 0 || p_dep > 1 || gamma < 0 || gamma >= 1) return set_error(QGB_EINVAL, "noise parameters out of range");
+    TrajGateArgs a{};
+    a.n = n;
+    a.ntraj = ntraj;
+    a.stride = ntraj > 1 ? stride : 0;
+    // union U: gate sites first, then pending sites not already present
+    int ub[4], nu = 0;
+    auto add = [&](int site) -> int {
+        if (site < 0 || site >= n) return -1;
+        const int bit = n - 1 - site;
+        for (int i = 0; i < nu; ++i)
+            if (ub[i] == bit) return i;
+        ub[nu] = bit;
+        return nu++;
+    };
+    a.kg = k;
+    for (int j = 0; j < k; ++j) {
+        const int p = add(sites[j]);
+        if (p < 0) return set_error(QGB_EINVAL, "gate site out of range");
+        for (int i = 0; i < j; ++i)
+            if (a.gpos[i] == p) return set_error(QGB_EINVAL, "repeated gate site");
+        a.gpos[j] = p;
+    }
+    a.kp = kprev;
+    for (int j = 0; j < kprev; ++j) {
+        const int p = add(prev_sites[j]);
+        if (p < 0) return set_error(QGB_EINVAL, "pending site out of range");
+        a.ppos[j] = p;
+    }
+    if (nu == 0) return QGB_OK;
+    a.ku = nu;
+    for (int j = 0; j < nu; ++j) a.ubits[j] = ub[j];
+    a.p_dep = k > 0 ? p_dep : 0.0;
+    a.seed0 = uint32_t(seed);
+    a.seed1 = uint32_t(seed >> 32);
+    a.event = event;
+    a.nblk = qgb_traj_blocks(n);
+    a.log_paulis = pauli_log != nullptr;
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = dtype == QGB_C64 ? dispatch_gate<float>(sv, gate, kraus, partials, pauli_log, a, st)
+                              : dispatch_gate<double>(sv, gate, kraus, partials, pauli_log, a, st);
+    if (rc || k == 0) return rc;
+    TrajDecideArgs d{};
+    d.ntraj = ntraj;
+    d.ku = nu;
+    d.nblk = a.nblk;
+    d.kg = k;
+    d.gpos[0] = a.gpos[0];
+    d.gpos[1] = k > 1 ? a.gpos[1] : 0;
+    d.gamma = gamma;
+    d.seed0 = a.seed0;
+    d.seed1 = a.seed1;
+    d.event = event;
+    const unsigned blocks = unsigned((ntraj + 127) / 128);
+    if (dtype == QGB_C64)
+        traj_decide_kernel<float><<<blocks, 128, 0, st>>>(partials, (float2*)kraus, jump_log, d);
+    else
+        traj_decide_kernel<double><<<blocks, 128, 0, st>>>(partials, (double2*)kraus, jump_log, d);
+    return check_launch("trajectory decide kernel");
+}
+
+extern "C" void qgb_philox_uniform(uint32_t event, uint32_t traj, uint32_t stream, uint64_t seed, double* out) {
+    *out = qgb::Philox::uniform(event, traj, stream, uint32_t(seed), uint32_t(seed >> 32));
+}

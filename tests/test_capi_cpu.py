@@ -16,7 +16,7 @@ HEADER = os.path.join(ROOT, "include", "qgb.h")
 
 def _declared():
     text = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:int|size_t|const char\*)\s+(qgb_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|size_t|void|const char\*)\s+(qgb_\w+)\s*\(", text, re.M)))
 
 
 @pytest.fixture(scope="module")
