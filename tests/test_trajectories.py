@@ -83,7 +83,7 @@ def test_trajectory_replay_matches_oracle(dtype, cuda_ok):
     assert jlog.sum() > 0 and plog.sum() > 0  # the noise is strong enough to branch
     tol = 1e-5 if dtype == torch.complex64 else 1e-12
     for t in range(T):
-        exp = _replay(gates, n, t, seed, p, gamma, plog, jlog)
+        exp = _replay(sim.gates, n, t, seed, p, gamma, plog, jlog)  # the simulator's (layer) order
         assert np.max(np.abs(states[t] - exp)) < tol
 
 
