@@ -132,6 +132,19 @@ int qgb_partial_overlap(const void* a, const void* b, int dtype, int n, const in
                         int64_t batch, int64_t sv_stride, double* out, void* scratch,
                         size_t scratch_bytes, void* stream);
 
+/* One step of the adjoint (reverse-mode) gradient sweep for a gate U on
+ * sites indices[0..k), k <= 2, in a single pass over two distinct vectors:
+ * phi <- U^dagger phi (uncompute), then, if grad_out is not NULL,
+ * grad_out[2*(r*2^k+c)] (+1) = re (im) of sum_rest lam[r,rest] conj(phi[c,rest])
+ * with the updated phi (float64, device, 2*4^k doubles; torch's gradient of a
+ * real loss is twice this when lam is the loss's dL/d conj(psi)), and
+ * lam <- U^dagger lam. Together with qgb_pauli_apply it replaces the
+ * autograd tape of the reference's torch path (core/param_gates.py:21-49,
+ * applications/compilation.py:73-133) with O(1) state memory; the reduction is
+ * partial_overlap (tensorQ/statevector_sim.py:155-180). */
+int qgb_adjoint_step(void* phi, void* lam, int dtype, int n, const int* indices, int k, const void* op,
+                     double* grad_out, void* scratch, size_t scratch_bytes, void* stream);
+
 /* ---- noisy trajectories -------------------------------------------------- */
 
 /* Blocks per trajectory used by qgb_traj_step (sizes its `partials`: at least

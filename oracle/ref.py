@@ -64,6 +64,20 @@ def op_action(op, indices, sv, local_dim=2):
     return out.reshape(local_dim ** n) if sv.ndim == 1 else out
 
 
+def op_action_torch(op, indices, state):
+    """The torch-backend form of ``op_action`` (``tensorQ/statevector_sim.py:124-140``
+    with ``ncon_torch`` on torch tensors): differentiable by torch autograd.
+    ``state`` is the rank-n tensor ``[2]*n``."""
+    k = len(indices)
+    n = state.ndim
+    op = op.reshape(*[2] * 2 * k)
+    sorted_idx = sorted(indices)
+    order = [list(indices).index(i) for i in sorted_idx]
+    op = permute(op, order + [i + k for i in order])
+    gi, si = locs_to_indices(sorted_idx, n)
+    return ncon((op, state), (gi, si))
+
+
 def construct_layers(gates):
     """Greedy ASAP layering, ``core/circuits.py:42-63``."""
     layers = []

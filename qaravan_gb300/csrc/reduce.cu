@@ -269,6 +269,74 @@ __global__ void __launch_bounds__(kRedThreads) dm_trace_kernel(const cplx<T>* __
     block_reduce_store<1>(acc, partials + int64_t(blockIdx.y) * gridDim.x + blockIdx.x, gridDim.x);
 }
 
+// Adjoint reverse step for one gate U on K <= 2 sites, one pass over two vectors:
+//   phi <- U^dagger phi,  grad[r][c] += lam[r] * conj(phi_new[c]),  lam <- U^dagger lam
+// (slots 2*(r*D+c) (+1) = re/im; the host scales by 2, torch's convention).
+struct AdjointArgs {
+    int n;
+    int sorted[2];
+    uint32_t off[4];
+    int want_grad;
+};
+
+template <typename T, int K>
+__global__ void __launch_bounds__(kRedThreads) adjoint_kernel(cplx<T>* __restrict__ phi, cplx<T>* __restrict__ lam,
+                                                              const cplx<T>* __restrict__ U,
+                                                              const __grid_constant__ AdjointArgs a,
+                                                              double* __restrict__ partials) {
+    constexpr int D = 1 << K;
+    using C = cplx<T>;
+    C ud[D * D];  // U^dagger
+#pragma unroll
+    for (int r = 0; r < D; ++r)
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            const C u = U[c * D + r];
+            ud[r * D + c] = mk<T>(u.x, -u.y);
+        }
+    const uint64_t groups = uint64_t(1) << (a.n - K), stride = uint64_t(gridDim.x) * blockDim.x;
+    double acc[2 * D * D];
+#pragma unroll
+    for (int j = 0; j < 2 * D * D; ++j) acc[j] = 0.0;
+    for (uint64_t g = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; g < groups; g += stride) {
+        uint64_t base = g;
+#pragma unroll
+        for (int j = 0; j < K; ++j) base = ((base >> a.sorted[j]) << (a.sorted[j] + 1)) | (base & ((uint64_t(1) << a.sorted[j]) - 1));
+        C p[D], l[D], pn[D], ln[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            p[c] = phi[base + a.off[c]];
+            l[c] = lam[base + a.off[c]];
+        }
+#pragma unroll
+        for (int r = 0; r < D; ++r) {
+            C x = mk<T>(0, 0), y = mk<T>(0, 0);
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                cfma(x, ud[r * D + c], p[c]);
+                cfma(y, ud[r * D + c], l[c]);
+            }
+            pn[r] = x;
+            ln[r] = y;
+        }
+        if (a.want_grad) {
+#pragma unroll
+            for (int r = 0; r < D; ++r)
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    acc[2 * (r * D + c)] += double(l[r].x) * pn[c].x + double(l[r].y) * pn[c].y;
+                    acc[2 * (r * D + c) + 1] += double(l[r].y) * pn[c].x - double(l[r].x) * pn[c].y;
+                }
+        }
+#pragma unroll
+        for (int r = 0; r < D; ++r) {
+            phi[base + a.off[r]] = pn[r];
+            lam[base + a.off[r]] = ln[r];
+        }
+    }
+    if (a.want_grad) block_reduce_store<2 * D * D>(acc, partials + blockIdx.x, gridDim.x);
+}
+
 // out = sum_t coeff[t] P_t sv
 struct PauliApplyArgs {
     int n, nterms;
@@ -564,4 +632,43 @@ extern "C" int qgb_pauli_apply(const void* sv, void* out, int dtype, int n, cons
     if (dtype == QGB_C64) pauli_apply_kernel<float><<<grid, 256, 0, st>>>((const float2*)sv, (float2*)out, sv_stride, a);
     else pauli_apply_kernel<double><<<grid, 256, 0, st>>>((const double2*)sv, (double2*)out, sv_stride, a);
     return check_launch("pauli apply");
+}
+
+extern "C" int qgb_adjoint_step(void* phi, void* lam, int dtype, int n, const int* indices, int k, const void* op,
+                                double* grad_out, void* scratch, size_t scratch_bytes, void* stream) {
+    int rc = check_common(phi, dtype, n, 1, 0);
+    if (rc) return rc;
+    if (!lam || !op || !indices) return set_error(QGB_EINVAL, "null pointer");
+    if (lam == phi) return set_error(QGB_EINVAL, "the two vectors must be distinct");
+    if (k < 1 || k > 2 || k > n) return set_error(QGB_EINVAL, "adjoint steps support gates on 1 or 2 sites (k=%d)", k);
+    const int slots = 2 << (2 * k);
+    if (grad_out && (!scratch || scratch_bytes < red_scratch(n, slots, 1)))
+        return set_error(QGB_ESCRATCH, "scratch too small");
+    AdjointArgs a{};
+    a.n = n;
+    a.want_grad = grad_out != nullptr;
+    int pos[2];
+    for (int j = 0; j < k; ++j) {
+        if (indices[j] < 0 || indices[j] >= n) return set_error(QGB_EINVAL, "site out of range");
+        pos[j] = n - 1 - indices[j];
+        a.sorted[j] = pos[j];
+    }
+    if (k == 2) {
+        if (pos[0] == pos[1]) return set_error(QGB_EINVAL, "repeated site");
+        if (a.sorted[0] > a.sorted[1]) { const int t = a.sorted[0]; a.sorted[0] = a.sorted[1]; a.sorted[1] = t; }
+    }
+    for (int r = 0; r < (1 << k); ++r) a.off[r] = uint32_t(matrix_offset(r, pos, k));
+    cudaStream_t st = (cudaStream_t)stream;
+    const unsigned grid = unsigned(red_blocks(n));
+    double* part = (double*)scratch;
+    if (dtype == QGB_C64) {
+        if (k == 1) adjoint_kernel<float, 1><<<grid, kRedThreads, 0, st>>>((float2*)phi, (float2*)lam, (const float2*)op, a, part);
+        else adjoint_kernel<float, 2><<<grid, kRedThreads, 0, st>>>((float2*)phi, (float2*)lam, (const float2*)op, a, part);
+    } else {
+        if (k == 1) adjoint_kernel<double, 1><<<grid, kRedThreads, 0, st>>>((double2*)phi, (double2*)lam, (const double2*)op, a, part);
+        else adjoint_kernel<double, 2><<<grid, kRedThreads, 0, st>>>((double2*)phi, (double2*)lam, (const double2*)op, a, part);
+    }
+    if ((rc = check_launch("adjoint step"))) return rc;
+    if (!grad_out) return QGB_OK;
+    return finish(part, red_blocks(n), slots, 1, nullptr, grad_out, st);
 }
