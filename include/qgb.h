@@ -173,6 +173,31 @@ int qgb_traj_step(void* sv, int dtype, int n, int64_t ntraj, int64_t stride, con
 /* The Philox uniform the trajectory kernels draw (host-side, for replays). */
 void qgb_philox_uniform(uint32_t event, uint32_t traj, uint32_t stream, uint64_t seed, double* out);
 
+/* ---- batches of small uneven circuits ------------------------------------ */
+
+/* Layout sizes of the two device tables qgb_batch_small reads:
+ *   circuit (qgb_batch_circuit_bytes() bytes): int64 offset (elements into
+ *     `states`), int64 out_offset (doubles into `out`), int32 nbits, int32
+ *     op_begin, int32 op_end, int32 flags (bit 0: start from basis state 0),
+ *     int32 dm_sites (> 0: the vector is vec(rho) of that many qubits, <= 7),
+ *     int32 pad;
+ *   op (qgb_batch_op_bytes() bytes): int32 k, int32 pos[6] (flat bits of the
+ *     circuit's vector, matrix order), int64 mat (element offset in `mats`). */
+size_t qgb_batch_circuit_bytes(void);
+size_t qgb_batch_op_bytes(void);
+
+/* Runs `ncirc` independent circuits in one launch, one CTA per circuit: each
+ * vector (at most 2^max_bits entries, max_bits <= 14 for complex64 and 13 for
+ * complex128) is staged in shared memory once, the circuit's ops
+ * [op_begin, op_end) are applied in order, and it is written back -- the
+ * DensityMatrixSim / StatevectorSim run loop (core/base_sim.py:30-53) for
+ * many small circuits at once. If `out` is not NULL, every density-matrix
+ * circuit also writes Re Tr(rho), Tr(rho^2) and Re Tr(rho Z_i) (i < dm_sites)
+ * to out[out_offset ..] in float64 (DensityMatrixSim.one_local_expectation,
+ * tensorQ/density_matrix_sim.py:60-70). Tables live in device memory. */
+int qgb_batch_small(void* states, int dtype, const void* circuits, int ncirc, const void* ops, const void* mats,
+                    int max_bits, int max_k, double* out, void* stream);
+
 /* ---- density matrix ---------------------------------------------------- */
 
 /* Replaces DensityMatrixSim.apply_gate (tensorQ/density_matrix_sim.py:38-42)

@@ -58,6 +58,9 @@ SIGNATURES = {
     "qgb_pauli_apply": (C.c_int, [_vp, _vp, _i, _i, _cp, _dp, _i, _i64, _i64, _vp]),
     "qgb_partial_overlap": (C.c_int, [_vp, _vp, _i, _i, _ip, _i, _i64, _i64, _vp, _vp, _sz, _vp]),
     "qgb_adjoint_step": (C.c_int, [_vp, _vp, _i, _i, _ip, _i, _vp, _vp, _vp, _sz, _vp]),
+    "qgb_batch_circuit_bytes": (C.c_size_t, []),
+    "qgb_batch_op_bytes": (C.c_size_t, []),
+    "qgb_batch_small": (C.c_int, [_vp, _i, _vp, _i, _vp, _vp, _i, _i, _vp, _vp]),
     "qgb_traj_blocks": (C.c_int, [_i]),
     "qgb_traj_step": (C.c_int, [_vp, _i, _i, _i64, _i64, _ip, _i, _vp, _ip, _i, _vp, C.c_double, C.c_double,
                                 _u64, C.c_uint32, _vp, _vp, _vp, _vp]),

@@ -51,10 +51,22 @@ class _Runner:
         self.scratch = Scratch(self.device)
         self._sites = [_lib.int_array(g.indices) for g in gates]
 
+    def host_matrices(self, mats):
+        """All gate matrices as complex128 NumPy arrays (one host transfer)."""
+        flat = torch.cat([m.detach().reshape(-1).to("cpu", torch.complex128) for m in mats]).numpy()
+        out, o = [], 0
+        for m in mats:
+            k = m.numel()
+            d = int(round(k ** 0.5))
+            out.append(flat[o:o + k].reshape(d, d))
+            o += k
+        return out, flat
+
     def forward_state(self, mats):
         n = self.n
-        ops = [Op([n - 1 - q for q in g.indices], m.detach().to("cpu", torch.complex128).numpy())
-               for g, m in zip(self.gates, mats)]
+        host, flat = self.host_matrices(mats)
+        self._flat = flat
+        ops = [Op([n - 1 - q for q in g.indices], m) for g, m in zip(self.gates, host)]
         kcap = 5 if self.dtype == torch.complex64 else 4
         isz = torch.empty(0, dtype=self.dtype).element_size()
         plan = compile_ops(ops, n, mode=self.sim.mode, width=self.sim.fusion_width, tile_bits=self.sim.tile_bits,
@@ -72,23 +84,23 @@ class _Runner:
         st = _lib.stream_ptr(self.device)
         phi = psi.detach().clone()
         lam = lam.contiguous()
-        dev_mats = torch.stack([m.detach().reshape(-1).to(self.device, self.dtype) for m in mats]) \
-            if len({m.numel() for m in mats}) == 1 else None
+        # every gate matrix in one pinned upload; per-gate element offsets
+        flat = getattr(self, "_flat", None)
+        if flat is None:
+            _, flat = self.host_matrices(mats)
+        dev = torch.from_numpy(flat).to(self.dtype).pin_memory().to(self.device, non_blocking=True)
+        isz = dev.element_size()
+        offs = np.cumsum([0] + [m.numel() for m in mats])
         grads_dev = torch.empty(len(self.gates), 32, dtype=torch.float64, device=self.device)
         nbytes = L.qgb_reduce_scratch_bytes(n, 32, 1)
         scr = self.scratch.get(nbytes)
-        keep = []
+        base, gbase = dev.data_ptr(), grads_dev.data_ptr()
         for i in range(len(self.gates) - 1, -1, -1):
             g = self.gates[i]
-            if dev_mats is not None:
-                mptr = dev_mats[i].data_ptr()
-            else:
-                mt = mats[i].detach().reshape(-1).to(self.device, self.dtype).contiguous()
-                keep.append(mt)
-                mptr = mt.data_ptr()
-            out = grads_dev[i].data_ptr() if need[i] else None
+            out = gbase + i * 32 * 8 if need[i] else None
             _lib.check(L.qgb_adjoint_step(phi.data_ptr(), lam.data_ptr(), self.code, n, self._sites[i],
-                                          len(g.indices), mptr, out, scr.data_ptr(), nbytes, st), "adjoint_step")
+                                          len(g.indices), base + int(offs[i]) * isz, out, scr.data_ptr(), nbytes, st),
+                       "adjoint_step")
         host = grads_dev.cpu().numpy()
         out = []
         for i, g in enumerate(self.gates):

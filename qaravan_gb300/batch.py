@@ -1,0 +1,194 @@
+"""Uneven batches of noisy density-matrix circuits.
+
+The reference runs one ``DensityMatrixSim`` at a time, every op a full ncon
+contraction over the rank-2n tensor (``tensorQ/density_matrix_sim.py:38-42``,
+``core/base_sim.py:30-53``). ``DensityMatrixBatch`` runs many circuits of
+different qubit counts and depths together:
+
+* every circuit whose vec(rho) fits in shared memory (complex64: up to 7
+  qubits, 2^14 entries; complex128: up to 6) is one CTA of a single
+  ``qgb_batch_small`` launch that stages the whole vector once, applies all of
+  its fused ops, and writes trace, purity and ``Re Tr(rho Z_i)`` in float64
+  from its epilogue;
+* larger circuits run their compiled tile-sweep plans (tile size and fusion
+  width from ``qaravan_gb300.autotune``) on parallel CUDA streams, followed by
+  float64 reductions;
+* ``run(graph=True)`` captures all of it -- the batched launch, every stream's
+  sweeps and reductions -- in one CUDA graph and replays it.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib, autotune
+from .compiler import compile_ops, fuse
+from .engine import Executor
+
+
+def _circuit_dtype(dtype):
+    return np.dtype([("offset", "<i8"), ("out_offset", "<i8"), ("nbits", "<i4"), ("op_begin", "<i4"),
+                     ("op_end", "<i4"), ("flags", "<i4"), ("dm_sites", "<i4"), ("pad", "<i4")])
+
+
+_OP_DTYPE = np.dtype([("k", "<i4"), ("pos", "<i4", (6,)), ("pad", "<i4"), ("mat", "<i8")])
+
+
+class DensityMatrixBatch:
+    """Run ``DensityMatrixSim``-like circuits together.
+
+    ``sims``: list of ``DensityMatrixSim`` objects (their circuits, noise
+    models and initial state |0...0> are used; Reset is supported on the
+    per-stream path only)."""
+
+    def __init__(self, sims, dtype=torch.complex64, device="cuda", width=4, small_max_bits=None, max_streams=8):
+        self.sims = list(sims)
+        self.dtype = dtype
+        self.device = torch.device(device)
+        self.code = _lib.dtype_code(dtype)
+        self.isz = 8 if dtype == torch.complex64 else 16
+        self.small_max = small_max_bits if small_max_bits is not None else (14 if self.isz == 8 else 13)
+        self.width = min(width, 4)
+        L = _lib.lib()
+        if L.qgb_batch_circuit_bytes() != _circuit_dtype(dtype).itemsize or L.qgb_batch_op_bytes() != _OP_DTYPE.itemsize:
+            raise _lib.QgbError("batch table layout mismatch with the library")
+        self.nmax = max(s.num_sites for s in self.sims)
+        self.ncols = 2 + self.nmax
+        self.out = torch.zeros(len(self.sims), self.ncols, dtype=torch.float64, device=self.device)
+        small, large = [], []
+        for i, s in enumerate(self.sims):
+            ops = s.op_sequence()
+            nb = 2 * s.num_sites
+            (small if (nb <= self.small_max and None not in ops) else large).append((i, s, ops))
+        self._prep_small(small)
+        self._prep_large(large, max_streams)
+        self.graph = None
+
+    # ------------------------------------------------------------ small path
+    def _prep_small(self, small):
+        self.small = small
+        if not small:
+            return
+        circs = np.zeros(len(small), dtype=_circuit_dtype(self.dtype))
+        op_rows, mats, moff = [], [], 0
+        off = 0
+        max_bits, max_k = 1, 1
+        for j, (i, s, ops) in enumerate(small):
+            nb = 2 * s.num_sites
+            blocks = fuse(ops, max(self.width, max(len(o.bits) for o in ops))) if ops else []
+            if any(len(b.bits) > 4 for b in blocks):
+                blocks = fuse(ops, max(len(o.bits) for o in ops))
+            begin = len(op_rows)
+            for b in blocks:
+                row = np.zeros((), dtype=_OP_DTYPE)
+                row["k"] = len(b.bits)
+                row["pos"][:len(b.bits)] = b.bits
+                row["mat"] = moff
+                op_rows.append(row)
+                mats.append(b.matrix.reshape(-1))
+                moff += b.matrix.size
+                max_k = max(max_k, len(b.bits))
+            circs[j] = (off, i * self.ncols, nb, begin, len(op_rows), 1, s.num_sites, 0)
+            off += 4 ** s.num_sites
+            off += off & 1  # 16-byte alignment for complex64
+            max_bits = max(max_bits, nb)
+        if max_k > 4:
+            raise NotImplementedError("batched small circuits take fused ops of at most 4 bits")
+        self.small_states = torch.zeros(max(off, 2), dtype=self.dtype, device=self.device)
+        self.small_circs = torch.from_numpy(circs.view(np.uint8).copy()).to(self.device)
+        ops_arr = np.array(op_rows, dtype=_OP_DTYPE) if op_rows else np.zeros(1, dtype=_OP_DTYPE)
+        self.small_ops = torch.from_numpy(ops_arr.view(np.uint8).copy()).to(self.device)
+        host = np.concatenate(mats) if mats else np.zeros(2, np.complex128)
+        self.small_mats = torch.from_numpy(host).to(self.dtype).to(self.device)
+        self.small_max_bits, self.small_max_k = max_bits, max_k
+        self.small_state_offsets = {i: int(circs[j]["offset"]) for j, (i, s, ops) in enumerate(small)}
+
+    # ------------------------------------------------------------ large path
+    def _prep_large(self, large, max_streams):
+        self.large = []
+        for i, s, ops in large:
+            nb = 2 * s.num_sites
+            tile, width = autotune.choose(nb, self.dtype)
+            plan = compile_ops(ops, nb, mode="sweep", width=width, tile_bits=tile,
+                               max_sweep_k=5 if self.isz == 8 else 4, itemsize=self.isz)
+            ex = Executor(plan, self.dtype, self.device, mode_normalize="dm")
+            state = torch.empty(4 ** s.num_sites, dtype=self.dtype, device=self.device)
+            L = _lib.lib()
+            nbytes = max(L.qgb_reduce_scratch_bytes(nb, max(s.num_sites, 1), 1), 8)
+            scratch = torch.empty(nbytes // 8 + 1, dtype=torch.float64, device=self.device)
+            self.large.append((i, s, ex, state, scratch, nbytes))
+        n_streams = min(max_streams, len(self.large))
+        self.streams = [torch.cuda.Stream(self.device) for _ in range(n_streams)]
+
+    def _launch_large(self, item):
+        i, s, ex, state, scratch, nbytes = item
+        L = _lib.lib()
+        n = s.num_sites
+        st = _lib.stream_ptr(self.device)
+        _lib.check(L.qgb_init_basis(state.data_ptr(), self.code, 2 * n, 0, 1, 0, st), "init")
+        ex.run(state)
+        base = self.out.data_ptr() + i * self.ncols * 8
+        _lib.check(L.qgb_dm_trace(state.data_ptr(), self.code, n, 1, 0, base, scratch.data_ptr(), nbytes, st),
+                   "dm_trace")
+        _lib.check(L.qgb_norm2(state.data_ptr(), self.code, 2 * n, 1, 0, base + 8, scratch.data_ptr(), nbytes, st),
+                   "norm2")
+        zs = "".join('i' * q + 'z' + 'i' * (n - q - 1) for q in range(n)).encode()
+        _lib.check(L.qgb_dm_pauli_expectation(state.data_ptr(), self.code, n, zs, None, n, 1, 0, base + 16,
+                                              scratch.data_ptr(), nbytes, st), "dm_pauli_expectation")
+
+    def _launch_all(self):
+        L = _lib.lib()
+        main = torch.cuda.current_stream(self.device)
+        for s in self.streams:
+            s.wait_stream(main)
+        for j, item in enumerate(self.large):
+            with torch.cuda.stream(self.streams[j % len(self.streams)]):
+                self._launch_large(item)
+        if self.small:
+            _lib.check(L.qgb_batch_small(self.small_states.data_ptr(), self.code, self.small_circs.data_ptr(),
+                                         len(self.small), self.small_ops.data_ptr(), self.small_mats.data_ptr(),
+                                         self.small_max_bits, self.small_max_k, self.out.data_ptr(),
+                                         _lib.stream_ptr(self.device)), "batch_small")
+        for s in self.streams:
+            main.wait_stream(s)
+
+    @property
+    def launches(self):
+        n = 1 if self.small else 0
+        for item in self.large:
+            n += 1 + item[2].plan.n_sweeps + 3 * 2 + 1
+        return n
+
+    def run(self, graph=False):
+        if not graph:
+            self._launch_all()
+            return self
+        if self.graph is None:
+            self._launch_all()
+            torch.cuda.synchronize(self.device)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, capture_error_mode="thread_local"):
+                self._launch_all()
+            self.graph = g
+        self.graph.replay()
+        return self
+
+    def results(self):
+        """Per circuit: trace, purity Tr(rho^2) and Re Tr(rho Z_i) (float64)."""
+        out = self.out.cpu().numpy()
+        res = []
+        for i, s in enumerate(self.sims):
+            n = s.num_sites
+            res.append({"trace": out[i, 0], "purity": out[i, 1], "z": out[i, 2:2 + n].copy()})
+        return res
+
+    def density_matrix(self, i):
+        n = self.sims[i].num_sites
+        d = 2 ** n
+        if i in getattr(self, "small_state_offsets", {}):
+            o = self.small_state_offsets[i]
+            return self.small_states[o:o + d * d].reshape(d, d)
+        for item in self.large:
+            if item[0] == i:
+                return item[3].reshape(d, d)
+        raise KeyError(i)

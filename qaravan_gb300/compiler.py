@@ -24,6 +24,7 @@ site ``q`` is bit ``n-1-q``.
 """
 from __future__ import annotations
 
+import functools
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -74,12 +75,10 @@ class Plan:
 
 # ----------------------------------------------------------------- algebra
 
-def embed(mat, bits, target):
-    """Matrix of ``mat`` (acting on ``bits``) on the larger bit list ``target``."""
-    bits, target = list(bits), list(target)
+@functools.lru_cache(maxsize=4096)
+def _embed_index(bits, target):
+    """Index maps of ``embed``: (row/col sub-index into the small matrix, same-rest mask)."""
     K, k = len(target), len(bits)
-    if bits == target:
-        return np.asarray(mat, dtype=np.complex128)
     pos = [target.index(b) for b in bits]  # position j in target order (0 = MSB)
     idx = np.arange(2 ** K)
     sub = np.zeros(2 ** K, dtype=np.int64)
@@ -90,9 +89,16 @@ def embed(mat, bits, target):
         if p not in pos:
             other_mask |= 1 << (K - 1 - p)
     rest = idx & other_mask
-    same = rest[:, None] == rest[None, :]
-    full = np.where(same, np.asarray(mat, dtype=np.complex128)[sub[:, None], sub[None, :]], 0)
-    return full
+    return sub[:, None], sub[None, :], rest[:, None] == rest[None, :]
+
+
+def embed(mat, bits, target):
+    """Matrix of ``mat`` (acting on ``bits``) on the larger bit list ``target``."""
+    bits, target = tuple(bits), tuple(target)
+    if bits == target:
+        return np.asarray(mat, dtype=np.complex128)
+    rows, cols, same = _embed_index(bits, target)
+    return np.where(same, np.asarray(mat, dtype=np.complex128)[rows, cols], 0)
 
 
 def _union(a, b):

@@ -75,6 +75,26 @@ def hea_circuit(n, layers, params):
     return Circuit(gl, n=n)
 
 
+def noisy_brickwork_circuit(n, depth, seed, p=1e-3):
+    """Haar brickwork with a single-qubit depolarising channel (``PauliNoise`` with the
+    p/3 convention) on both sites after every two-qubit gate, as explicit ``ID``
+    noise carriers in a built layer list (one op per layer, the order the
+    density-matrix oracle applies them)."""
+    from .gates import ID
+    from .noise import depolarizing
+    gl = brickwork_gates(n, depth, seed)
+    dep = depolarizing(p)
+    seq = []
+    for g in gl:
+        seq.append(g)
+        if len(g.indices) == 2:
+            seq.extend(ID(2, 0.0, [q], nm=dep) for q in g.indices)
+    c = Circuit(gl, n=n)
+    c.layers = [[g] for g in seq]
+    c.built = True
+    return c
+
+
 def uneven_dm_specs(count, seed, n_range=(6, 14), depth_range=(10, 40)):
     """(n, depth, circuit seed) triples for the uneven density-matrix batch."""
     rng = np.random.default_rng(seed)

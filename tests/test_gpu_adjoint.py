@@ -74,7 +74,7 @@ def test_matrix_gradients_match_oracle_reverse_sweep():
     exp = ref.matrix_gradients(seq, n, terms)
     by_id = {id(g): e for g, e in zip(seq, exp)}
     for g, t in zip(gates, tg):
-        assert np.max(np.abs(t.grad.numpy() - by_id[id(g)])) < 1e-10
+        assert np.max(np.abs(t.matrix.grad.numpy() - by_id[id(g)])) < 1e-10
 
 
 def test_state_function_with_arbitrary_loss():
