@@ -106,14 +106,19 @@ template <typename T, int KMAX>
 int launch_small(void* states, const void* circs, int ncirc, const void* ops, const void* mats, int max_bits,
                  double* out, cudaStream_t st) {
     const size_t smem = sizeof(cplx<T>) * ((size_t(1) << max_bits) + stage_elems<KMAX>());
-    if (smem > 227 * 1024) return set_error(QGB_EINVAL, "vectors of 2^%d entries do not fit in shared memory", max_bits);
     auto kern = batch_small_kernel<T, KMAX>;
-    static bool attr = false;
-    if (!attr) {
-        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) != cudaSuccess)
+    static size_t dyn_max = 0;
+    if (dyn_max == 0) {
+        // the epilogue's reduction buffer is static shared memory: opt in to the rest
+        cudaFuncAttributes fa;
+        if (cudaFuncGetAttributes(&fa, kern) != cudaSuccess) return check_launch("batch attributes");
+        dyn_max = 227 * 1024 - fa.sharedSizeBytes;
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(dyn_max)) != cudaSuccess) {
+            dyn_max = 0;
             return check_launch("batch attribute");
-        attr = true;
+        }
     }
+    if (smem > dyn_max) return set_error(QGB_EINVAL, "vectors of 2^%d entries do not fit in shared memory", max_bits);
     const int threads = max_bits >= 12 ? 512 : 256;
     kern<<<unsigned(ncirc), threads, smem, st>>>((cplx<T>*)states, (const BatchCircuit*)circs, (const BatchOp*)ops,
                                                  (const cplx<T>*)mats, out, max_bits);
