@@ -50,13 +50,14 @@ def _peaks():
         return 6800.0, "fallback"
 
 
-def _profile_traffic():
-    """dram bytes per sweep launch from the committed ncu summary (None if absent)."""
-    path = os.path.join(ROOT, "profiles", "sweep_kernel_28q.txt")
+def _profile_traffic(kernel):
+    """DRAM bytes per launch of `kernel` at the full workload, from the committed ncu
+    summary profiles/roofline_traffic.txt (lines "<kernel>: <bytes>"; None if absent)."""
+    path = os.path.join(ROOT, "profiles", "roofline_traffic.txt")
     try:
         for line in open(path):
-            if line.startswith("traffic_bytes_per_full_launch:"):
-                return float(line.split(":")[1])
+            if line.startswith(kernel + ":"):
+                return float(line.split(":", 1)[1].split()[0])
     except OSError:
         pass
     return None
@@ -123,15 +124,26 @@ def workload_gates(n=N_QUBITS, depth=DEPTH, seed=SEED):
     return workloads.brickwork_gates(n, depth, seed)
 
 
+def _mixed_sample(gates, n, count):
+    """Alternate SU(2) and SU(4) gates of the first depth unit (the circuit's 1:1 mix)."""
+    ones = [g for g in gates[:2 * n] if len(g.indices) == 1]
+    twos = [g for g in gates[:2 * n] if len(g.indices) == 2]
+    out = []
+    for a, b in zip(ones, twos):
+        out += [a, b]
+    return out[:count]
+
+
 def cpu_baseline(gates, n, budget_s=12.0, min_gates=2, max_gates=8):
-    """Reference algorithm (oracle op_action, complex128) on a bounded prefix of the circuit."""
+    """Reference algorithm (oracle op_action, complex128) on a bounded sample of the circuit's gates."""
     import torch
     from oracle import ref
     threads = os.cpu_count() or 1
     torch.set_num_threads(threads)
     state = ref.initial_sv(n)
+    sample = _mixed_sample(gates, n, max_gates)
     done, t0 = 0, time.perf_counter()
-    for g in gates[:max_gates]:
+    for g in sample:
         state = ref.op_action(g.matrix, g.indices, state)
         done += 1
         if done >= min_gates and time.perf_counter() - t0 > budget_s:
@@ -139,9 +151,198 @@ def cpu_baseline(gates, n, budget_s=12.0, min_gates=2, max_gates=8):
     dt = time.perf_counter() - t0
     del state
     return {"value": done / dt, "unit": "gates/s", "cores": threads, "kind": "port",
-            "sample": f"first {done} gates ({sum(len(g.indices) == 1 for g in gates[:done])} SU(2), "
-                      f"{sum(len(g.indices) == 2 for g in gates[:done])} SU(4)) of the {n}-qubit circuit, "
+            "sample": f"{done} gates alternating SU(2)/SU(4) from the first depth unit of the {n}-qubit circuit, "
                       f"complex128 tensordot+transpose (reference op_action via oracle/), {dt:.1f} s"}
+
+
+def _event_ms(fn, warmup=1, steps=1):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / steps
+
+
+def section_variants(n, gates):
+    """Unfused (one HBM pass per gate), fused dense blocks of width 2..6, and the
+    complex128 sweep path, on the same 28-qubit circuit (one timed run each)."""
+    import torch
+    from qaravan_gb300 import StatevectorSim, _lib
+    from qaravan_gb300.circuits import Circuit
+    circ = Circuit(gates, n=n)
+    out = {}
+    for name, dtype, mode, width, tile in [("c64_unfused", torch.complex64, "gate", 2, 14),
+                                           ("c64_fused_w2", torch.complex64, "fused", 2, 14),
+                                           ("c64_fused_w4", torch.complex64, "fused", 4, 14),
+                                           ("c64_fused_w6", torch.complex64, "fused", 6, 14),
+                                           ("c64_sweep_w3_t12", torch.complex64, "sweep", 3, 12),
+                                           ("c64_sweep_w4_t14", torch.complex64, "sweep", 4, 14),
+                                           ("c128_sweep_w3_t13", torch.complex128, "sweep", 3, 13)]:
+        try:
+            ex = StatevectorSim(circ, dtype=dtype, mode=mode, fusion_width=width, tile_bits=tile).compile()
+            st = torch.empty(2 ** n, dtype=dtype, device="cuda")
+            code = _lib.dtype_code(dtype)
+
+            def step():
+                _lib.check(_lib.lib().qgb_init_basis(st.data_ptr(), code, n, 0, 1, 0, _lib.stream_ptr()), "init")
+                ex.run(st)
+            ms = _event_ms(step, 1, 1)
+            out[name] = {"gates_per_s": round(len(gates) / (ms / 1e3), 1), "ms": round(ms, 2),
+                         "hbm_passes": ex.plan.n_sweeps}
+            del st, ex
+        except Exception as e:  # a variant that does not fit is reported, not fatal
+            out[name] = {"error": str(e)[:200]}
+        torch.cuda.empty_cache()
+    return out
+
+
+def _torch_reference_energy(n, layers, params, terms, device):
+    """The reference's torch-backend path on this GPU, for the autograd comparison:
+    gate matrices by torch.linalg.matrix_exp (core/param_gates.py:51-80), cast to
+    complex64 on the device (to_backend, tensorQ/statevector_sim.py:19-24),
+    op_action as permute + tensordot (tensorQ/statevector_sim.py:124-140), and
+    torch autograd through every op. <H> by Pauli-X flips and Z signs."""
+    import torch
+    from qaravan_gb300.gates import CNOT
+    Y = torch.tensor([[0, -1j], [1j, 0]], dtype=torch.complex128)
+    Zm = torch.tensor([[1, 0], [0, -1]], dtype=torch.complex128)
+    th = torch.tensor(params, dtype=torch.float64, requires_grad=True)
+    st = torch.zeros([2] * n, dtype=torch.complex64, device=device)
+    st.view(-1)[0] = 1
+
+    def apply(m, idx, s):
+        k = len(idx)
+        t = torch.tensordot(m.reshape([2] * 2 * k), s, dims=(list(range(k, 2 * k)), list(idx)))
+        rest = [a for a in range(n) if a not in idx]
+        order = list(idx) + rest
+        inv = [order.index(a) for a in range(n)]
+        return t.permute(*inv)
+
+    for l in range(layers):
+        for q in range(n):
+            st = apply(torch.linalg.matrix_exp(-1j * th[l, q, 0] * Y).to(device, torch.complex64), [q], st)
+            st = apply(torch.linalg.matrix_exp(-1j * th[l, q, 1] * Zm).to(device, torch.complex64), [q], st)
+        for q in range(n - 1):
+            g = CNOT([q + 1, q], n)
+            st = apply(torch.tensor(g.matrix, dtype=torch.complex64, device=device), g.indices, st)
+    e = 0
+    p = (st.abs() ** 2).to(torch.float64)
+    for c, s in terms:
+        if 'x' in s:
+            q = s.index('x')
+            e = e + c * torch.real(torch.vdot(st.reshape(-1), torch.flip(st, dims=[q]).reshape(-1))).to(torch.float64)
+        else:
+            q = s.index('z')
+            sign = torch.ones([2] * n, dtype=torch.float64, device=device)
+            idx = [slice(None)] * n
+            idx[q] = 1
+            sign[tuple(idx)] *= -1
+            if s.count('z') == 2:
+                idx = [slice(None)] * n
+                idx[q + 1] = 1
+                sign[tuple(idx)] *= -1
+            e = e + c * (p * sign).sum()
+    return e, th
+
+
+def section_adjoint(n=24, layers=40, base_layers=4):
+    """Adjoint gradient of the TFI energy of the hardware-efficient ansatz (complex64)
+    vs plain forward + torch autograd of the reference's torch path, same GPU."""
+    import torch
+    from qaravan_gb300 import StatevectorSim, workloads
+    from qaravan_gb300.adjoint import adjoint_energy
+    from qaravan_gb300.hamiltonians import TFI
+    terms = TFI(n, 1, 1).pauli_sum()
+    out = {"qubits": n, "layers": layers, "params": 2 * n * layers, "dtype": "c64"}
+
+    def adjoint_run(L):
+        th = torch.tensor(workloads.hea_params(n, L, 1), dtype=torch.float64, requires_grad=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim = StatevectorSim(workloads.hea_circuit(n, L, th), dtype=torch.complex64)
+        e = adjoint_energy(sim, terms)
+        e.backward()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, float(e.item()), th.grad.numpy().copy()
+
+    adjoint_run(2)
+    torch.cuda.reset_peak_memory_stats()
+    base = torch.cuda.memory_allocated()
+    t_full, e_full, _ = adjoint_run(layers)
+    out["adjoint_s_per_gradient"] = round(t_full, 4)
+    out["adjoint_grads_per_s"] = round(1.0 / t_full, 3)
+    out["adjoint_peak_state_multiples"] = round((torch.cuda.max_memory_allocated() - base) / (2 ** n * 8), 2)
+    out["energy"] = e_full
+    # the reference's torch path at a depth that fits, same depth for the adjoint
+    t_adj_b, e_adj_b, g_adj_b = adjoint_run(base_layers)
+    params = workloads.hea_params(n, base_layers, 1)
+    torch.cuda.synchronize()
+    torch.cuda.reset_peak_memory_stats()
+    base = torch.cuda.memory_allocated()
+    t0 = time.perf_counter()
+    e_ref, th = _torch_reference_energy(n, base_layers, params, terms, "cuda")
+    e_ref.backward()
+    torch.cuda.synchronize()
+    t_ref = time.perf_counter() - t0
+    peak = torch.cuda.max_memory_allocated() - base
+    g_ref = th.grad.numpy()
+    free_total = torch.cuda.get_device_properties(0).total_memory
+    out["torch_autograd"] = {
+        "layers": base_layers, "s_per_gradient": round(t_ref, 4), "peak_gb": round(peak / 1e9, 2),
+        "predicted_peak_gb_at_full_depth": round(peak * layers / base_layers / 1e9, 1),
+        "fits_at_full_depth": bool(peak * layers / base_layers < free_total)}
+    out["adjoint_at_same_depth_s"] = round(t_adj_b, 4)
+    out["speedup_vs_autograd_same_depth"] = round(t_ref / t_adj_b, 2)
+    out["max_rel_grad_diff_vs_autograd"] = float(abs(g_adj_b - g_ref).max() / max(abs(g_ref).max(), 1e-30))
+    out["energy_diff_vs_autograd"] = abs(e_adj_b - float(e_ref.item()))
+    return out
+
+
+def section_trajectories(n=20, ntraj=1024, steps=40):
+    """1024 noisy TFI Trotter trajectories (depolarising 1e-3 + amplitude damping 5e-4
+    after every gate), one CUDA graph; mean <Z_i>, <Z_i Z_i+1>."""
+    import torch
+    from qaravan_gb300 import workloads
+    from qaravan_gb300.trajectories import TrajectorySim, z_terms
+    circ = workloads.tfi_trotter_circuit(n, 0.05, steps)
+    sim = TrajectorySim(circ, ntraj, p_dep=1e-3, gamma=5e-4, seed=2026)
+    ms = _event_ms(lambda: sim.run(graph=True), 1, 2)
+    mean, _ = sim.mean_expectations(z_terms(n))
+    m = mean.cpu().numpy()
+    ng = len(sim.gates)
+    return {"qubits": n, "trajectories": ntraj, "gates": ng, "ms_per_run": round(ms, 2),
+            "trajectories_per_s": round(ntraj / (ms / 1e3), 1),
+            "trajectory_gates_per_s": round(ntraj * ng / (ms / 1e3), 1), "launches_per_run": sim.launches,
+            "mean_z_first": float(m[0]), "mean_zz_first": float(m[n])}
+
+
+def section_dm_batch(count=256, seed=7):
+    """256 noisy brickwork density matrices, 6-14 qubits, depth 10-40, one CUDA graph."""
+    import torch
+    from qaravan_gb300 import DensityMatrixSim, workloads
+    from qaravan_gb300.batch import DensityMatrixBatch
+    specs = workloads.uneven_dm_specs(count, seed)
+    t0 = time.perf_counter()
+    sims = [DensityMatrixSim(workloads.noisy_brickwork_circuit(n, d, s, p=1e-3), dtype=torch.complex64)
+            for n, d, s in specs]
+    batch = DensityMatrixBatch(sims, dtype=torch.complex64)
+    compile_s = time.perf_counter() - t0
+    ms = _event_ms(lambda: batch.run(graph=True), 1, 1)
+    res = batch.results()
+    out = {"circuits": count, "small_batched": len(batch.small), "stream_parallel": len(batch.large),
+           "compile_s": round(compile_s, 2), "ms_per_batch": round(ms, 1),
+           "circuits_per_s": round(count / (ms / 1e3), 2),
+           "max_trace_error": float(max(abs(r["trace"] - 1) for r in res)),
+           "state_gb": round(sum(4 ** n * 8 for n, _, _ in specs) / 1e9, 1)}
+    del batch, sims
+    torch.cuda.empty_cache()
+    return out
 
 
 def dist_init():
@@ -187,6 +388,8 @@ def gpu_arm(args):
     sim = StatevectorSim(circ, dtype=dtype, mode=args.mode, fusion_width=args.width, tile_bits=args.tile,
                          low_bits=args.low)
     ex = sim.compile()
+    ex_kmax = max([len(st.bits) for st in ex.plan.steps if hasattr(st, "bits")] +
+                  [len(p) for st in ex.plan.steps if hasattr(st, "ops") for p, _ in st.ops] + [2])
     state = torch.empty(2 ** n, dtype=dtype, device="cuda")
     L = _lib.lib()
     code = _lib.dtype_code(dtype)
@@ -231,8 +434,10 @@ def gpu_arm(args):
     if dom:
         mean_ms = statistics.mean(durs[dom])
         achieved = alg_bytes / (mean_ms / 1e3) / 1e9
-        tr = _profile_traffic() if (n == N_QUBITS and dtype == torch.complex64 and args.mode == "sweep") else None
-        roof = {"bound": "hbm", "kernel": f"qgb::{'sweep' if dom == 'sweep' else 'dense_reg'}_kernel",
+        kname = {"sweep": f"sweep_ldst_kernel<{'float' if itemsize == 8 else 'double'},{ex_kmax}>",
+                 "dense": f"dense_reg_kernel<{'float' if itemsize == 8 else 'double'},{ex_kmax}>"}[dom]
+        tr = _profile_traffic(f"{kname}@{n}q") if args.depth == DEPTH else None
+        roof = {"bound": "hbm", "kernel": f"qgb::{kname}",
                 "achieved": round(achieved, 1), "peak": peak, "peak_source": f"hbm_gbs of {peak_kind}",
                 "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": tr,
                 "alg_bytes_per_launch": alg_bytes, "mean_launch_ms": round(mean_ms, 4),
@@ -264,8 +469,21 @@ def gpu_arm(args):
 
     if rank != 0:
         return
-    cpu = None if args.no_cpu else cpu_baseline(gates, n, budget_s=args.cpu_budget)
     launches = args.steps * (1 + ex.launches)
+    del state, ex, sim
+    torch.cuda.empty_cache()
+    sections = {}
+    wanted = args.sections.split(",") if args.sections != "all" else ["variants", "adjoint", "trajectories",
+                                                                       "dm_batch"]
+    for name, fn in [("variants", lambda: section_variants(n, gates)), ("adjoint", section_adjoint),
+                     ("trajectories", section_trajectories), ("dm_batch", section_dm_batch)]:
+        if name in wanted:
+            try:
+                sections[name] = fn()
+            except Exception as e:  # secondary sections never suppress the headline line
+                sections[name] = {"error": f"{type(e).__name__}: {str(e)[:300]}"}
+            torch.cuda.empty_cache()
+    cpu = None if args.no_cpu else cpu_baseline(gates, n, budget_s=args.cpu_budget)
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": "gates/s", "n_gates": gates_per_step,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
@@ -279,7 +497,7 @@ def gpu_arm(args):
                    "parallelism": f"replicas x{world}"},
         "hbm_gbs_effective": round(passes * alg_bytes / (ms_step / 1e3) / 1e9, 1),
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks.summary(),
-        "gpu_launches": launches,
+        "gpu_launches": launches, "sections": sections,
     }
     print(json.dumps(out), flush=True)
 
@@ -295,7 +513,7 @@ def reference_arm(args):
     import torch
     threads = os.cpu_count() or 1
     torch.set_num_threads(threads)
-    sample = gates[: args.ref_gates]
+    sample = _mixed_sample(gates, n, args.ref_gates)
     state = ref.initial_sv(n)
     for g in sample[:1] * args.warmup:
         state = ref.op_action(g.matrix, g.indices, state)
@@ -308,7 +526,7 @@ def reference_arm(args):
     total = sum(times)
     value = args.steps * len(sample) / total
     cpu = {"value": round(value, 4), "unit": "gates/s", "cores": threads, "kind": "port",
-           "sample": f"{len(sample)} gates (SU(2) + SU(4)) of the {n}-qubit brickwork per step, complex128, "
+           "sample": f"{len(sample)} gates (alternating SU(2), SU(4)) of the {n}-qubit brickwork per step, complex128, "
                      f"reference op_action restated in oracle/"}
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "gates/s", "n_gpus": 1,
@@ -330,7 +548,7 @@ def main():
     p.add_argument("--qubits", type=int, default=N_QUBITS)
     p.add_argument("--depth", type=int, default=DEPTH)
     p.add_argument("--dtype", default="c64", choices=["c64", "c128"])
-    p.add_argument("--mode", default="sweep", choices=["gate", "fused", "sweep"])
+    p.add_argument("--mode", default="fused", choices=["gate", "fused", "sweep"])
     p.add_argument("--width", type=int, default=4)
     p.add_argument("--tile", type=int, default=14)
     p.add_argument("--low", type=int, default=None)
@@ -339,6 +557,8 @@ def main():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-budget", type=float, default=12.0)
     p.add_argument("--ref-gates", type=int, default=2)
+    p.add_argument("--sections", default="all",
+                   help="comma list of variants,adjoint,trajectories,dm_batch; 'none' for the headline only")
     args = p.parse_args()
     if args.impl == "reference":
         reference_arm(args)

@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(256) dense_reg_kernel(cplx<T>* __restrict__ sv
                                                         const __grid_constant__ DenseArgs a) {
     constexpr int D = 1 << K;
     using C = cplx<T>;
-    __shared__ C M[D * D];
+    __shared__ __align__(16) C M[D * D];
     const int64_t b = blockIdx.y;
     const C* opb = op + b * a.op_stride;
     for (int i = threadIdx.x; i < D * D; i += blockDim.x) M[i] = opb[i];
@@ -54,6 +54,35 @@ __global__ void __launch_bounds__(256) dense_reg_kernel(cplx<T>* __restrict__ sv
 #pragma unroll
                 for (int c = 0; c < D; ++c) cfma(acc, m[r * D + c], v[c]);
                 s[base + a.off_out[r]] = acc;
+            }
+        }
+    } else if (sizeof(T) == 4 && a.groups >= 2) {
+        // complex64, K = 3, 4: each thread takes groups g and g + groups/2 together so that
+        // every matrix element (two per 16-byte shared-memory load) feeds two groups
+        const uint64_t half = a.groups >> 1;
+        for (uint64_t g = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; g < half; g += stride) {
+            const uint64_t b0 = insert_zeros(g, a.sorted, K), b1 = insert_zeros(g + half, a.sorted, K);
+            C v0[D], v1[D];
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                v0[c] = s[b0 + a.off_in[c]];
+                v1[c] = s[b1 + a.off_in[c]];
+            }
+#pragma unroll 1
+            for (int r = 0; r < D; ++r) {
+                const float4* m4 = reinterpret_cast<const float4*>(M + r * D);
+                C a0 = mk<T>(0, 0), a1 = mk<T>(0, 0);
+#pragma unroll
+                for (int c = 0; c < D; c += 2) {
+                    const float4 q = m4[c >> 1];
+                    const C e0 = mk<T>(T(q.x), T(q.y)), e1 = mk<T>(T(q.z), T(q.w));
+                    cfma(a0, e0, v0[c]);
+                    cfma(a1, e0, v1[c]);
+                    cfma(a0, e1, v0[c + 1]);
+                    cfma(a1, e1, v1[c + 1]);
+                }
+                s[b0 + a.off_out[r]] = a0;
+                s[b1 + a.off_out[r]] = a1;
             }
         }
     } else {

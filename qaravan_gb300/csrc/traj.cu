@@ -172,14 +172,15 @@ __global__ void __launch_bounds__(256) traj_gate_kernel(cplx<T>* __restrict__ sv
     }
     C* s = sv + t * a.stride;
     const uint64_t groups = uint64_t(1) << (a.n - K), step = uint64_t(a.nblk) * blockDim.x;
-    double p0 = 0, p1 = 0, p2 = 0, p3 = 0;
+    // per-thread partial sums in the state's precision (a few dozen terms each; float64 across threads)
+    T p0 = 0, p1 = 0, p2 = 0, p3 = 0;
     auto add_pop = [&](int r, const C& o) {
-        const double w = double(o.x) * o.x + double(o.y) * o.y;
+        const T w = o.x * o.x + o.y * o.y;
         const uint32_t b = (bk >> (2 * r)) & 3u;
-        p0 += b == 0 ? w : 0.0;
-        p1 += b == 1 ? w : 0.0;
-        p2 += b == 2 ? w : 0.0;
-        p3 += b == 3 ? w : 0.0;
+        p0 += b == 0 ? w : T(0);
+        p1 += b == 1 ? w : T(0);
+        p2 += b == 2 ? w : T(0);
+        p3 += b == 3 ? w : T(0);
     };
     for (uint64_t g = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; g < groups; g += step) {
         uint64_t base = g;
@@ -220,7 +221,7 @@ __global__ void __launch_bounds__(256) traj_gate_kernel(cplx<T>* __restrict__ sv
     }
     // block reduction of the 4 joint populations -> partials[(t * nblk + blk) * 4 + b]
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double pv[4] = {p0, p1, p2, p3};
+    double pv[4] = {double(p0), double(p1), double(p2), double(p3)};
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
         double x = pv[b];
