@@ -112,6 +112,23 @@ int qgb_pauli_expectation(const void* sv, int dtype, int n, const char* paulis, 
                           int nterms, int64_t batch, int64_t sv_stride, double* out, void* scratch,
                           size_t scratch_bytes, void* stream);
 
+/* Allocation-free form of qgb_pauli_expectation for one state (no counterpart
+ * in the reference): for callers that must not allocate device memory --
+ * real-time loops that may not stall on the allocator, plugins whose host
+ * application owns all device memory through its own pool and forbids
+ * cudaMalloc/cudaFree beside it, GPUs whose memory is already fully reserved
+ * so that even a small allocation would fail. Instead of a caller buffer it
+ * uses one fixed 1 MiB device array inside the library (held on every device
+ * the library is used on until the process exits), so it accepts at most 64
+ * terms and at most 131072 / blocks(n) terms in total (blocks(n) =
+ * min(1216, max(1, 2^n / 4096))), and returns QGB_EINVAL beyond that. The
+ * first call on a device looks up the array's address (cudaGetSymbolAddress,
+ * that device current) -- make it before any stream capture. Calls share the
+ * array: calls that overlap on the GPU race. Results equal
+ * qgb_pauli_expectation's (out: nterms float64, device). */
+int qgb_pauli_expectation_noalloc(const void* sv, int dtype, int n, const char* paulis, const double* coeff,
+                                  int nterms, double* out, void* stream);
+
 /* <a_b|b_b> = sum conj(a) b for every state b: out[2b], out[2b+1] = real,
  * imaginary part (float64). With b = (x)_q O_q a it gives
  * StatevectorSim.local_expectation / one_local_expectation (:63-73, :81-94). */

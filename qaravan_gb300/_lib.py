@@ -54,6 +54,7 @@ SIGNATURES = {
     "qgb_reduce_scratch_bytes": (C.c_size_t, [_i, _i, _i64]),
     "qgb_norm2": (C.c_int, [_vp, _i, _i, _i64, _i64, _vp, _vp, _sz, _vp]),
     "qgb_pauli_expectation": (C.c_int, [_vp, _i, _i, _cp, _dp, _i, _i64, _i64, _vp, _vp, _sz, _vp]),
+    "qgb_pauli_expectation_noalloc": (C.c_int, [_vp, _i, _i, _cp, _dp, _i, _vp, _vp]),
     "qgb_inner_product": (C.c_int, [_vp, _vp, _i, _i, _i64, _i64, _vp, _vp, _sz, _vp]),
     "qgb_pauli_apply": (C.c_int, [_vp, _vp, _i, _i, _cp, _dp, _i, _i64, _i64, _vp]),
     "qgb_partial_overlap": (C.c_int, [_vp, _vp, _i, _i, _ip, _i, _i64, _i64, _vp, _vp, _sz, _vp]),

@@ -672,3 +672,108 @@ extern "C" int qgb_adjoint_step(void* phi, void* lam, int dtype, int n, const in
     if (!grad_out) return QGB_OK;
     return finish(part, red_blocks(n), slots, 1, nullptr, grad_out, st);
 }
+
+// ---------------------------------------------------------------------------
+// Pauli expectation for callers that cannot allocate device memory.
+//
+// Some callers of this library run where cudaMalloc is off limits: real-time
+// loops that must never stall on the allocator, plugins whose host application
+// owns all device memory through its own pool and forbids allocations beside
+// it, or GPUs whose memory is already fully reserved, where even a small
+// allocation fails. qgb_pauli_expectation needs a caller-provided scratch
+// buffer for its per-block partial sums; this variant takes its partial sums
+// from one fixed array in device memory that is part of the library image
+// (1 MiB, allocated once when the library is loaded on a device and held until
+// the process exits), so a call allocates nothing -- neither device memory nor
+// host heap memory. The array's device address is looked up with
+// cudaGetSymbolAddress the first time the entry point runs on a device (with
+// that device current) and cached per device; make that first call before any
+// stream capture. Every partial-sum slot a call reads was written earlier in
+// the same call, so nothing needs clearing between calls; but all calls share
+// the one array, so two calls whose kernels overlap on the GPU (different
+// streams, or different host threads) race and give wrong results.
+namespace {
+
+constexpr size_t kNoAllocScratchDoubles = size_t(1) << 17;  // 1 MiB of float64 partial sums
+constexpr int kNoAllocMaxTerms = 64;
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
+
+void* noalloc_scratch_address(int* rc) {
+    static void* addr[kNoAllocMaxDevices] = {nullptr};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        *rc = set_error(QGB_ECUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+        return nullptr;
+    }
+    if (dev < 0 || dev >= kNoAllocMaxDevices) {
+        *rc = set_error(QGB_EINVAL, "device %d beyond the %d devices the scratch cache covers", dev, kNoAllocMaxDevices);
+        return nullptr;
+    }
+    if (!addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            *rc = set_error(QGB_ECUDA, "cudaGetSymbolAddress of the fixed scratch array: %s", cudaGetErrorString(e));
+            return nullptr;
+        }
+        addr[dev] = p;
+    }
+    *rc = QGB_OK;
+    return addr[dev];
+}
+
+}  // namespace
+
+extern "C" int qgb_pauli_expectation_noalloc(const void* sv, int dtype, int n, const char* paulis, const double* coeff,
+                                             int nterms, double* out, void* stream) {
+    int rc = check_common(sv, dtype, n, 1, 0);
+    if (rc) return rc;
+    if (!out || !paulis) return set_error(QGB_EINVAL, "null pointer");
+    if (n > 64) return set_error(QGB_EINVAL, "Pauli strings limited to 64 sites");
+    if (nterms < 1 || nterms > kNoAllocMaxTerms)
+        return set_error(QGB_EINVAL, "%d terms requested; the allocation-free variant takes 1..%d (use "
+                         "qgb_pauli_expectation for more)", nterms, kNoAllocMaxTerms);
+    const size_t need = size_t(red_blocks(n)) * size_t(nterms);
+    if (need > kNoAllocScratchDoubles)
+        return set_error(QGB_EINVAL, "%d terms on %d qubits need %zu partial sums; the fixed scratch holds %zu "
+                         "(use qgb_pauli_expectation with a caller buffer)", nterms, n, need, kNoAllocScratchDoubles);
+    ParsedPauli ps[kNoAllocMaxTerms];  // parsed on the stack: no heap allocation
+    for (int t = 0; t < nterms; ++t) {
+        ParsedPauli p{0, 0, 0};
+        for (int q = 0; q < n; ++q) {
+            const uint64_t bit = 1ull << (n - 1 - q);
+            switch (paulis[size_t(t) * n + q]) {
+                case 'i': case 'I': break;
+                case 'x': case 'X': p.x |= bit; break;
+                case 'y': case 'Y': p.x |= bit; p.z |= bit; p.ny++; break;
+                case 'z': case 'Z': p.z |= bit; break;
+                default: return set_error(QGB_EINVAL, "invalid Pauli character in term %d", t);
+            }
+        }
+        ps[t] = p;
+    }
+    double* partials = (double*)noalloc_scratch_address(&rc);
+    if (!partials) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    int t = 0;
+    while (t < nterms) {
+        PauliGroup g{};
+        g.xmask = ps[t].x;
+        g.slot0 = t;
+        g.nterms = 0;
+        while (t < nterms && ps[t].x == g.xmask && g.nterms < 32) {
+            g.zmask[g.nterms] = ps[t].z;
+            g.ny[g.nterms] = ps[t].ny;
+            g.coeff[g.nterms] = coeff ? coeff[t] : 1.0;
+            ++g.nterms;
+            ++t;
+        }
+        if (dtype == QGB_C64) launch_group_nt<float>(sv, n, 0, g, nterms, partials, 1, false, st);
+        else launch_group_nt<double>(sv, n, 0, g, nterms, partials, 1, false, st);
+        if ((rc = check_launch("pauli expectation (no-alloc)"))) return rc;
+    }
+    return finish(partials, red_blocks(n), nterms, 1, nullptr, out, st);
+}
