@@ -436,6 +436,10 @@ def gpu_arm(args):
         achieved = alg_bytes / (mean_ms / 1e3) / 1e9
         kname = {"sweep": f"sweep_ldst_kernel<{'float' if itemsize == 8 else 'double'},{ex_kmax}>",
                  "dense": f"dense_reg_kernel<{'float' if itemsize == 8 else 'double'},{ex_kmax}>"}[dom]
+        tc_mode = _lib.lib().qgb_get_dense_impl()
+        if dom == "dense" and itemsize == 8 and n >= 13 and (ex_kmax >= 5 and tc_mode >= 1 or
+                                                            ex_kmax == 4 and tc_mode == 2):
+            kname = f"dense_tc_kernel<{ex_kmax}>"
         tr = _profile_traffic(f"{kname}@{n}q") if args.depth == DEPTH else None
         roof = {"bound": "hbm", "kernel": f"qgb::{kname}",
                 "achieved": round(achieved, 1), "peak": peak, "peak_source": f"hbm_gbs of {peak_kind}",

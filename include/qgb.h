@@ -89,6 +89,15 @@ int qgb_apply_sweep(void* sv, int dtype, int n, const qgb_sweep* sweep, const vo
  * (runs of at least 128 bytes). Process-wide; both give identical results. */
 int qgb_set_sweep_impl(int impl);
 
+/* Selects the kernel for complex64 dense blocks of k >= 4 qubits on at least
+ * 2^(k+7) amplitudes: 0 = CUDA-core kernels only, 1 = tensor cores (tcgen05,
+ * split-tf32 operands with fp32 accumulation) for k = 5, 6, 2 (default) =
+ * tensor cores for k = 4, 5, 6. Process-wide; the environment variable
+ * QGB_DENSE_IMPL sets the initial value. Results agree to fp32 rounding.
+ * qgb_get_dense_impl returns the current selection. */
+int qgb_set_dense_impl(int impl);
+int qgb_get_dense_impl(void);
+
 /* Writes |bits> (StatevectorSim.initialize_state, :31-48) to `batch` states. */
 int qgb_init_basis(void* sv, int dtype, int n, uint64_t index, int64_t batch, int64_t sv_stride,
                    void* stream);

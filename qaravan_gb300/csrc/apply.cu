@@ -273,6 +273,10 @@ int apply_dense_bits(void* sv, int dtype, int nbits, const int* in_bits, const i
     a.batch = batch;
     a.sv_stride = sv_stride;
     a.groups = uint64_t(1) << (nbits - k);
+    if (dtype == QGB_C64) {
+        const int rc = try_dense_tc(sv, op, nbits, a.sorted, in_bits, out_bits, k, op_stride, batch, sv_stride, st);
+        if (rc != QGB_EDECLINE) return rc;
+    }
     return dtype == QGB_C64 ? dispatch_dense<float>(sv, op, a, st) : dispatch_dense<double>(sv, op, a, st);
 }
 

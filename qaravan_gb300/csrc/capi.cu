@@ -64,5 +64,8 @@ extern "C" int qgb_check_status(void* stream) {
     const int sweep = qgb_host::sweep_status_read_clear();
     if (sweep < 0) return qgb_host::set_error(QGB_ECUDA, "sweep status read failed");
     if (sweep != 0) return qgb_host::set_error(QGB_ETIMEOUT, "a sweep's tile-load wait gave up (code %d)", sweep);
+    const int tc = qgb_host::tc_status_read_clear();
+    if (tc < 0) return qgb_host::set_error(QGB_ECUDA, "tensor-core status read failed");
+    if (tc != 0) return qgb_host::set_error(QGB_ETIMEOUT, "a tensor-core completion wait gave up (code %d)", tc);
     return QGB_OK;
 }

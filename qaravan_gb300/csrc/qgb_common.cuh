@@ -67,4 +67,10 @@ namespace qgb_host {
 int set_error(int code, const char* fmt, ...);
 int check_launch(const char* what);
 int sm_count();
+// Internal status (never returned through the C ABI): a specialised kernel
+// declines an op, and the caller runs the general kernel instead.
+constexpr int QGB_EDECLINE = 1000;
+int try_dense_tc(void* sv, const void* op, int nbits, const int* sorted, const int* in_bits, const int* out_bits,
+                 int k, int64_t op_stride, int64_t batch, int64_t sv_stride, cudaStream_t st);
+int tc_status_read_clear();
 }  // namespace qgb_host
