@@ -10,9 +10,10 @@ between steps). One step = initialise |0...0> and apply the whole circuit.
 * ``e2e``: the same metric through the public API with host inputs: build
   ``StatevectorSim`` from host NumPy gate matrices (compile + pinned H2D of
   the fused matrices), run, and read one float64 observable back (D2H).
-* ``roofline``: the dominant kernel (the fused tile sweep) -- algorithmic
-  bytes per launch (one read + one write of the 2^28 x 8 B state) over its
-  mean CUDA-event duration, against the measured HBM copy bandwidth.
+* ``roofline``: the dominant kernel (by default the tensor-core 6-qubit block
+  kernel, dense_tc_kernel<6>) -- algorithmic bytes per launch (one read + one
+  write of the 2^28 x 8 B state) over its mean CUDA-event duration, against
+  the measured HBM copy bandwidth.
 * ``cpu_baseline``: the reference's algorithm (``op_action`` = ncon via
   tensordot + transpose, complex128, ``oracle/``) on a bounded sample of the
   same circuit's gates on the host cores.
@@ -170,21 +171,29 @@ def _event_ms(fn, warmup=1, steps=1):
 
 
 def section_variants(n, gates):
-    """Unfused (one HBM pass per gate), fused dense blocks of width 2..6, and the
-    complex128 sweep path, on the same 28-qubit circuit (one timed run each)."""
+    """Unfused (one HBM pass per gate), fused dense blocks of width 2..6 on the
+    CUDA cores and (4..6) on the tensor cores, shared-memory tile sweeps, and
+    the complex128 sweep path, on the same 28-qubit circuit (one timed run each)."""
     import torch
     from qaravan_gb300 import StatevectorSim, _lib
     from qaravan_gb300.circuits import Circuit
     circ = Circuit(gates, n=n)
     out = {}
-    for name, dtype, mode, width, tile in [("c64_unfused", torch.complex64, "gate", 2, 14),
-                                           ("c64_fused_w2", torch.complex64, "fused", 2, 14),
-                                           ("c64_fused_w4", torch.complex64, "fused", 4, 14),
-                                           ("c64_fused_w6", torch.complex64, "fused", 6, 14),
-                                           ("c64_sweep_w3_t12", torch.complex64, "sweep", 3, 12),
-                                           ("c64_sweep_w4_t14", torch.complex64, "sweep", 4, 14),
-                                           ("c128_sweep_w3_t13", torch.complex128, "sweep", 3, 13)]:
+    L = _lib.lib()
+    before = L.qgb_get_dense_impl()
+    for name, dtype, mode, width, tile, impl in [
+            ("c64_unfused", torch.complex64, "gate", 2, 14, 0),
+            ("c64_fused_w2", torch.complex64, "fused", 2, 14, 0),
+            ("c64_fused_w4_cudacores", torch.complex64, "fused", 4, 14, 0),
+            ("c64_fused_w6_cudacores", torch.complex64, "fused", 6, 14, 0),
+            ("c64_fused_w4_tensorcores", torch.complex64, "fused", 4, 14, 2),
+            ("c64_fused_w5_tensorcores", torch.complex64, "fused", 5, 14, 2),
+            ("c64_fused_w6_tensorcores", torch.complex64, "fused", 6, 14, 2),
+            ("c64_sweep_w3_t12", torch.complex64, "sweep", 3, 12, 0),
+            ("c64_sweep_w4_t14", torch.complex64, "sweep", 4, 14, 0),
+            ("c128_sweep_w3_t13", torch.complex128, "sweep", 3, 13, 0)]:
         try:
+            _lib.check(L.qgb_set_dense_impl(impl))
             ex = StatevectorSim(circ, dtype=dtype, mode=mode, fusion_width=width, tile_bits=tile).compile()
             st = torch.empty(2 ** n, dtype=dtype, device="cuda")
             code = _lib.dtype_code(dtype)
@@ -199,6 +208,7 @@ def section_variants(n, gates):
         except Exception as e:  # a variant that does not fit is reported, not fatal
             out[name] = {"error": str(e)[:200]}
         torch.cuda.empty_cache()
+    _lib.check(L.qgb_set_dense_impl(before))
     return out
 
 
@@ -553,7 +563,7 @@ def main():
     p.add_argument("--depth", type=int, default=DEPTH)
     p.add_argument("--dtype", default="c64", choices=["c64", "c128"])
     p.add_argument("--mode", default="fused", choices=["gate", "fused", "sweep"])
-    p.add_argument("--width", type=int, default=4)
+    p.add_argument("--width", type=int, default=6)
     p.add_argument("--tile", type=int, default=14)
     p.add_argument("--low", type=int, default=None)
     p.add_argument("--e2e-steps", type=int, default=3)

@@ -15,31 +15,45 @@
 // (row/column permuted) gate matrix. That is 8 * D real flops per amplitude,
 // the same count as the complex product.
 //
-// Precision. kind::tf32 multiplies 19-bit operands, so every operand is split
-// as x = hi + lo with hi = x rounded to the nearest tf32 value and lo = x - hi
-// (exact in fp32, |lo| <= 2^-11 |x|); Y = Xhi*Wlo + Xlo*Whi + Xhi*Whi with
-// fp32 accumulation. The dropped Xlo*Wlo term and the tf32 reading of the lo
-// parts are below 2^-21 relative each: the result agrees with an fp32 dot
+// Precision. kind::f16 multiplies fp16 operands (11 significant bits, the
+// tf32 precision at twice its rate and half its tensor-memory footprint), so
+// every operand is scaled by a power of two and split as x = hi + lo with
+// hi = fp16(x) and lo = fp16(x - hi); Y = Xhi*Wlo + Xlo*Whi + Xhi*Whi with fp32
+// accumulation (the dropped Xlo*Wlo term is below 2^-21 relative). Each group
+// row gets its own scale 2^s with max |x| 2^s in [2^14, 2^15) (the two warps
+// that share a row agree on s through a named barrier), the matrix one scale
+// for the launch, so no operand overflows fp16 and only components below
+// 2^-24 of their row's largest fall into fp16's subnormal range; the
+// accumulator is scaled back in the drain. The result agrees with an fp32 dot
 // product to its own rounding level (about 1e-7 relative to the group norm).
 //
-// Data path per CTA (256 threads = 8 warps, one CTA per SM):
-//   * tensor memory (TMEM) holds Xhi, Xlo (the A operands, lane = group row,
-//     one 32-bit column per real component) and two accumulators D0/D1;
-//   * shared memory holds Whi, Wlo as the B operand, K-major, no swizzle:
+// Data path per CTA (one CTA per SM; 8 data warps + 1 MMA warp):
+//   * a tile is 8192 amplitudes (64 KB): the k target bits and the 13 - k
+//     lowest other bits (so runs of >= 128 contiguous amplitudes); the data
+//     warps copy tiles into two shared-memory buffers with cp.async in memory
+//     order (coalesced whatever the targets), two tiles ahead, 16-byte granules
+//     XOR-swizzled by the granule row so that row-wise reads spread over banks;
+//   * tensor memory (TMEM) holds, per block of 128 groups, two X buffers (hi
+//     and lo rows, the A operands: lane = group row, one 32-bit column per
+//     fp16 (re, im) pair) and two fp32 accumulators; tiles alternate between
+//     buffer pair 0 and 1 (shared memory, X, accumulator);
+//   * shared memory also holds Whi, Wlo as the B operand, K-major, no swizzle:
 //     8-row x 16-byte core matrices, K-adjacent cores 128 B apart (leading
 //     byte offset) and N-adjacent cores 256 B apart (stride byte offset);
-//   * warps w and w+4 share TMEM lane quarter w (groups 32w..32w+31); warp
-//     w+4h loads, splits and stores components [h*D/2, (h+1)*D/2) of its
-//     group, and later reads the same half of the result row;
-//   * a tile is 8192 amplitudes: 128 / (2D) blocks of 128 groups, each block
-//     with its own Xhi, Xlo, D0, D1 columns (512 columns in all, any k);
-//   * one thread issues the 3 * (2D/8) MMAs per block (M = 128, N = 2D, K = 8)
-//     and commits them to an mbarrier; while they run, the CTA loads the tile
-//     after next into registers (two register buffers) and drains the previous
-//     tile's accumulator to HBM.
+//   * warps w and w+4 share TMEM lane quarter w (groups 32w..32w+31 of each
+//     block); warp w+4h reads, scales, splits and stages components
+//     [h*D/2, (h+1)*D/2) of its groups, and later drains the same half of the
+//     result rows straight to HBM;
+//   * the MMA warp waits on an mbarrier that the 8 data warps arrive at once a
+//     tile's X rows are staged, issues the 3 * (2D/16) MMAs per block
+//     (M = 128, N = 2D, K = 16) and commits them to a second mbarrier, which the
+//     data warps wait on before draining. So the MMAs of tile i run while the
+//     data warps drain tile i - 1 and stage tile i + 1.
 // Every wait on the mbarrier is bounded (about 2 s of %globaltimer); a wait
 // that runs out sets a device status word read by qgb_check_status, and the
 // CTA frees its tensor memory and returns.
+#include <cuda_fp16.h>
+
 #include <cstdio>
 #include <cstdlib>
 
@@ -51,18 +65,24 @@ __device__ int g_tc_status = 0;
 
 struct TcArgs {
     int k;
-    int vec2;                         // 1: target bit 0 present, components (2m, 2m+1) adjacent
-    int sorted[QGB_MAX_K];            // target bits, ascending
-    int perm_in[1 << QGB_MAX_K];      // memory-order input component j -> matrix column
-    int perm_out[1 << QGB_MAX_K];     // memory-order output component i -> matrix row
-    uint64_t off[1 << (QGB_MAX_K - 1)];  // offsets of the low-half components (bits sorted[0..k-2])
-    uint64_t hstride;                 // offset of the upper half (bit sorted[k-1])
-    uint64_t tiles_per_state;         // groups / 128
-    uint64_t tiles;                   // tiles_per_state * batch
+    int vec2;                            // global bit 0 is a target: components (2m, 2m+1) adjacent
+    int L;                               // tile bits 0..L-1 are global bits 0..L-1 (L >= 7)
+    int tile_bits[13];                   // global bit of each tile bit, ascending
+    int pos_g[13];                       // tile positions of the 13 - k group bits, ascending
+    int perm_in[1 << QGB_MAX_K];         // memory-order input component j -> matrix column
+    int perm_out[1 << QGB_MAX_K];        // memory-order output component i -> matrix row
+    uint32_t ut[1 << (QGB_MAX_K - 1)];   // tile-index offsets of the low-half components
+    uint32_t ut_h;                       // tile-index offset of the upper half (target sorted[k-1])
+    uint64_t off[1 << (QGB_MAX_K - 1)];  // global offsets of the low-half components
+    uint64_t hstride;                    // global offset of the upper half
+    uint64_t hoff[64];                   // global offset of tile bits L..12, indexed by u >> L
+    uint64_t tiles_per_state;            // 2^(n - 13)
+    uint64_t tiles;                      // tiles_per_state * batch
     int64_t sv_stride;
 };
 
-constexpr int kTcThreads = 256;
+constexpr int kTcDataThreads = 256;           // 8 data warps
+constexpr int kTcThreads = kTcDataThreads + 32;  // + the MMA warp
 constexpr unsigned long long kTcWaitNs = 2000000000ull;
 
 template <int K> struct TcGeom {
@@ -70,14 +90,14 @@ template <int K> struct TcGeom {
     static constexpr int H = D / 2;      // components per thread and group
     static constexpr int R = 2 * D;      // real width: MMA N and total K
     static constexpr int NB = 128 / R;   // 128-row blocks per tile: every tile is 8192 amplitudes (64 KB)
-    static constexpr int BCOLS = 4 * R;  // TMEM columns per block: Xhi, Xlo, D0, D1
+    static constexpr int BCOLS = 4 * R;  // TMEM columns per block: X0 (hi, lo), X1 (hi, lo), D0, D1
     static constexpr int NCOLS = NB * BCOLS;  // 512: one CTA per SM
-    static constexpr uint32_t B_BYTES = uint32_t(R) * R * 4;
-    static constexpr size_t SMEM = 2 * size_t(B_BYTES) + 128;
-    // kind::tf32 instruction descriptor: f32 accumulator, tf32 A and B, both
+    static constexpr uint32_t B_BYTES = uint32_t(R) * R * 2;
+    static constexpr uint32_t TILE_BYTES = 8192 * 8;
+    static constexpr size_t SMEM = 2 * size_t(B_BYTES) + 2 * size_t(TILE_BYTES) + 128;
+    // kind::f16 instruction descriptor: f32 accumulator, f16 A and B, both
     // K-major, N = R, M = 128.
-    static constexpr uint32_t IDESC =
-        (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(R >> 3) << 17) | (uint32_t(128 >> 4) << 24);
+    static constexpr uint32_t IDESC = (1u << 4) | (uint32_t(R >> 3) << 17) | (uint32_t(128 >> 4) << 24);
     static_assert(R >= 32 && R <= 256 && (R % 16) == 0, "MMA N out of range");
     static_assert(NCOLS == 512, "tensor memory holds 512 columns");
 };
@@ -104,18 +124,59 @@ __device__ __forceinline__ bool tc_wait_bounded(uint32_t bar, uint32_t parity) {
     }
 }
 
-// Nearest tf32 value (ties away from zero), low 13 bits cleared.
-__device__ __forceinline__ float tf32_hi(float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return __uint_as_float(r & 0xffffe000u);
+// Byte offset of fp16 element (n, k) of a B operand with R rows (N) in the
+// K-major no-swizzle layout: per K-step of 16 a block of R * 32 bytes; inside
+// it core matrix (n / 8, (k % 16) / 8) at 256 * (n / 8) + 128 * ((k % 16) / 8).
+__device__ __forceinline__ uint32_t b_off(int n, int k, int R) {
+    return uint32_t((k >> 4) * (R * 32) + (n >> 3) * 256 + ((k >> 3) & 1) * 128 + (n & 7) * 16 + (k & 7) * 2);
 }
 
-// Byte offset of element (n, k) of a B operand with R rows (N) in the K-major
-// no-swizzle layout: per K-step of 8 a block of R * 32 bytes; inside it core
-// matrix (n / 8, (k % 8) / 4) at 256 * (n / 8) + 128 * ((k % 8) / 4).
-__device__ __forceinline__ uint32_t b_off(int n, int k, int R) {
-    return uint32_t((k >> 3) * (R * 32) + (n >> 3) * 256 + ((k >> 2) & 1) * 128 + (n & 7) * 16 + (k & 3) * 4);
+// Word (8-byte amplitude) index of tile index u in a staged tile: the 16-byte
+// granule index (bits 1..3) is XORed with a fold of the higher bits, so the 32
+// lanes reading one component of 32 rows hit distinct banks whether the rows
+// differ in low or in high tile bits. Bit 0 is left alone: a 16-byte granule
+// (two amplitudes) stays whole, as cp.async copies it.
+__device__ __forceinline__ uint32_t tile_swz(uint32_t u) {
+    return u ^ ((((u >> 4) ^ (u >> 7) ^ (u >> 10)) & 7u) << 1);
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+__device__ __forceinline__ void data_bar() { asm volatile("bar.sync 5, 256;" ::: "memory"); }
+__device__ __forceinline__ bool data_bar_any(bool v) {
+    uint32_t r;
+    asm volatile("{ .reg .pred p, q; setp.ne.u32 p, %1, 0; bar.red.or.pred q, 5, 256, p; selp.u32 %0, 1, 0, q; }"
+                 : "=r"(r)
+                 : "r"(uint32_t(v))
+                 : "memory");
+    return r != 0;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// 2^e for e in [-126, 127].
+__device__ __forceinline__ float exp2i(int e) { return __uint_as_float(uint32_t(e + 127) << 23); }
+
+// Scale exponent s with max 2^s in [2^14, 2^15) for a non-negative maximum m
+// (clamped to [-100, 100]; zero rows get 100 and stay zero).
+__device__ __forceinline__ int scale_exp(float m) {
+    const int s = 141 - int((__float_as_uint(m) >> 23) & 0xffu);
+    return s < -100 ? -100 : (s > 100 ? 100 : s);
+}
+
+// (a, b) -> packed fp16 pair hi and the packed rounding remainders lo.
+__device__ __forceinline__ void split_f16(float a, float b, uint32_t& hi, uint32_t& lo) {
+    const __half2 h = __floats2half2_rn(a, b);
+    const float2 hf = __half22float2(h);
+    const __half2 l = __floats2half2_rn(a - hf.x, b - hf.y);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
 }
 
 __device__ __forceinline__ uint64_t b_desc(uint32_t addr) {
@@ -128,7 +189,7 @@ __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::
 __device__ __forceinline__ void tc_mma(uint32_t d, uint32_t a, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
     asm volatile(
         "{ .reg .pred p; setp.ne.b32 p, %4, 0; "
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p; }" ::"r"(d),
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p; }" ::"r"(d),
         "r"(a), "l"(bdesc), "r"(idesc), "r"(acc)
         : "memory");
 }
@@ -144,6 +205,12 @@ __device__ __forceinline__ void tmem_st16(uint32_t taddr, const float* v) {
         "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7]), "f"(v[8]), "f"(v[9]),
         "f"(v[10]), "f"(v[11]), "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15])
         : "memory");
+}
+
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t* v) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(taddr), "r"(v[0]),
+                 "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
+                 : "memory");
 }
 
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
@@ -172,22 +239,39 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
     unsigned char* sb = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tc_smem_raw) + 127) & ~uintptr_t(127));
     unsigned char* Bhi = sb;
     unsigned char* Blo = sb + G::B_BYTES;
-    __shared__ __align__(8) uint64_t mma_bar;
+    unsigned char* tiles_smem = sb + 2 * G::B_BYTES;  // two staged tiles of TILE_BYTES
+    __shared__ __align__(8) uint64_t x_full[2];    // data warps -> MMA warp: X of pair p staged (8 arrivals)
+    __shared__ __align__(8) uint64_t mma_done[2];  // MMA warp -> data warps: accumulator of pair p complete
     __shared__ uint32_t tmem_slot;
+    __shared__ uint32_t wmax_bits;
+    __shared__ int row_exp[NB][2][128];  // per block, thread half and row: that half's scale exponent
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int q = warp & 3, h = warp >> 2;
+    const int q = warp & 3, h = (warp >> 2) & 1;
 
-    // B operand: W = [[Mr, Mi], [-Mi, Mr]] in (output, input) memory order, split hi/lo.
+    // B operand: W = [[Mr, Mi], [-Mi, Mr]] in (output, input) memory order, scaled by 2^sw, split hi/lo.
+    if (tid == 0) wmax_bits = 0;
+    __syncthreads();
+    {
+        float m = 0.f;
+        for (int p = tid; p < D * D; p += kTcThreads) {
+            const float2 e = op[p];
+            m = fmaxf(m, fmaxf(fabsf(e.x), fabsf(e.y)));
+        }
+        atomicMax(&wmax_bits, __float_as_uint(m));
+    }
+    __syncthreads();
+    const int sw = scale_exp(__uint_as_float(wmax_bits));
+    const float wscale = exp2i(sw), wunscale = exp2i(-sw);
     for (int p = tid; p < D * D; p += kTcThreads) {
         const int i = p / D, j = p - (p / D) * D;
         const float2 m = op[a.perm_out[i] * D + a.perm_in[j]];
-        const float w[4] = {m.x, -m.y, m.y, m.x};  // (2i,2j) (2i,2j+1) (2i+1,2j) (2i+1,2j+1)
+        const float w[4] = {m.x * wscale, -m.y * wscale, m.y * wscale, m.x * wscale};  // (2i,2j) (2i,2j+1) (2i+1,2j) (2i+1,2j+1)
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
             const uint32_t o = b_off(2 * i + (e >> 1), 2 * j + (e & 1), R);
-            const float hi = tf32_hi(w[e]);
-            *reinterpret_cast<float*>(Bhi + o) = hi;
-            *reinterpret_cast<float*>(Blo + o) = w[e] - hi;
+            const __half hi = __float2half_rn(w[e]);
+            *reinterpret_cast<__half*>(Bhi + o) = hi;
+            *reinterpret_cast<__half*>(Blo + o) = __float2half_rn(w[e] - __half2float(hi));
         }
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -198,145 +282,193 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 32) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem_u32(&mma_bar)) : "memory");
+        for (int p = 0; p < 2; ++p) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 8;" ::"r"(tc_smem_u32(&x_full[p])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem_u32(&mma_done[p])) : "memory");
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_slot;
-    const uint32_t bar = tc_smem_u32(&mma_bar);
-    const uint32_t row = tmem + (uint32_t(32 * q) << 16);  // this warp's lane quarter
-    const uint32_t bhi = tc_smem_u32(Bhi), blo = tc_smem_u32(Blo);
-    // TMEM columns of block bk: Xhi at bk*BC, Xlo at bk*BC + R, accumulators at bk*BC + 2R + buf*R.
+    const uint64_t step = gridDim.x;
+    const uint64_t t0 = blockIdx.x;  // the grid never exceeds the tile count
+    const uint64_t ntiles = (a.tiles - t0 + step - 1) / step;
 
-    auto group_ptr = [&](uint64_t t, int bk) -> float2* {
-        const uint64_t b = t / a.tiles_per_state, tt = t - b * a.tiles_per_state;
-        const uint64_t g = (tt * NB + uint64_t(bk)) * 128 + uint64_t(32 * q + lane);
-        return sv + int64_t(b) * a.sv_stride + insert_zeros(g, a.sorted, K) + uint64_t(h) * a.hstride;
-    };
-    using Buf = float2[NB][H];
-    auto load = [&](uint64_t t, Buf& v) {
-#pragma unroll
-        for (int bk = 0; bk < NB; ++bk) {
-            const float2* p = group_ptr(t, bk);
-            if (a.vec2) {
-#pragma unroll
-                for (int m = 0; m < H / 2; ++m) {
-                    const float4 x = *reinterpret_cast<const float4*>(p + a.off[2 * m]);
-                    v[bk][2 * m] = make_float2(x.x, x.y);
-                    v[bk][2 * m + 1] = make_float2(x.z, x.w);
+    if (warp == 8) {
+        // ---- MMA warp: one thread issues, in tile order, on alternating buffer pairs.
+        if (lane == 0) {
+            const uint32_t bhi = tc_smem_u32(Bhi), blo = tc_smem_u32(Blo);
+            for (uint64_t k = 0; k < ntiles; ++k) {
+                const int pb = int(k & 1);
+                if (!tc_wait_bounded(tc_smem_u32(&x_full[pb]), uint32_t((k >> 1) & 1))) {
+                    atomicExch(&g_tc_status, 1);
+                    break;
                 }
-            } else {
-#pragma unroll
-                for (int j = 0; j < H; ++j) v[bk][j] = p[a.off[j]];
+                tc_fence_after();
+#pragma unroll 1
+                for (int bk = 0; bk < NB; ++bk) {
+                    const uint32_t d = tmem + uint32_t(bk * BC + 2 * R + pb * R);
+                    const uint32_t xh = tmem + uint32_t(bk * BC + pb * R), xl = xh + R / 2;
+#pragma unroll 1
+                    for (int s = 0; s < R / 16; ++s)
+                        tc_mma(d, xh + uint32_t(8 * s), b_desc(blo + uint32_t(s * R * 32)), G::IDESC, s > 0);
+#pragma unroll 1
+                    for (int s = 0; s < R / 16; ++s)
+                        tc_mma(d, xl + uint32_t(8 * s), b_desc(bhi + uint32_t(s * R * 32)), G::IDESC, 1);
+#pragma unroll 1
+                    for (int s = 0; s < R / 16; ++s)
+                        tc_mma(d, xh + uint32_t(8 * s), b_desc(bhi + uint32_t(s * R * 32)), G::IDESC, 1);
+                }
+                tc_commit(tc_smem_u32(&mma_done[pb]));
             }
         }
-    };
-    auto store_x = [&](const Buf& v) {
+        __syncwarp();
+    } else {
+        // ---- data warps
+        const uint32_t row = tmem + (uint32_t(32 * q) << 16);  // this warp's lane quarter
+        const uint32_t runmask = (1u << a.L) - 1u;
+        // Tile-index and global offsets of this thread's rows (the same in every tile).
+        uint32_t ug[NB];
+        uint64_t gg[NB];
 #pragma unroll
         for (int bk = 0; bk < NB; ++bk) {
+            const uint32_t r = uint32_t(bk * 128 + 32 * q + lane);
+            uint32_t u = 0;
 #pragma unroll
-            for (int c0 = 0; c0 < D; c0 += 16) {
-                float hi[16], lo[16];
-#pragma unroll
-                for (int e = 0; e < 8; ++e) {
-                    const float2 x = v[bk][c0 / 2 + e];
-                    hi[2 * e] = tf32_hi(x.x);
-                    hi[2 * e + 1] = tf32_hi(x.y);
-                    lo[2 * e] = x.x - hi[2 * e];
-                    lo[2 * e + 1] = x.y - hi[2 * e + 1];
-                }
-                tmem_st16(row + uint32_t(bk * BC + h * D + c0), hi);
-                tmem_st16(row + uint32_t(bk * BC + R + h * D + c0), lo);
+            for (int i = 0; i < 13 - K; ++i) u |= ((r >> i) & 1u) << a.pos_g[i];
+            ug[bk] = u | (h ? a.ut_h : 0u);
+            gg[bk] = uint64_t(u & runmask) + a.hoff[u >> a.L] + (h ? a.hstride : 0);
+        }
+        auto tile_base = [&](uint64_t t) -> float2* {
+            const uint64_t b = t / a.tiles_per_state, tt = t - b * a.tiles_per_state;
+            return sv + int64_t(b) * a.sv_stride + insert_zeros(tt, a.tile_bits, 13);
+        };
+        auto issue_load = [&](uint64_t t, int pb) {
+            const float2* base = tile_base(t);
+            const uint32_t dst0 = tc_smem_u32(tiles_smem + pb * G::TILE_BYTES);
+#pragma unroll 4
+            for (int m = 0; m < 4096 / kTcDataThreads; ++m) {
+                const uint32_t u = 2u * uint32_t(tid + m * kTcDataThreads);
+                cp_async16(dst0 + 8u * tile_swz(u), base + (u & runmask) + a.hoff[u >> a.L]);
             }
-        }
-        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-    };
-    auto issue = [&](int buf) {
-        tc_fence_after();
-#pragma unroll 1
-        for (int bk = 0; bk < NB; ++bk) {
-            const uint32_t d = tmem + uint32_t(bk * BC + 2 * R + buf * R);
-            const uint32_t xh = tmem + uint32_t(bk * BC), xl = xh + R;
-#pragma unroll 1
-            for (int s = 0; s < R / 8; ++s)
-                tc_mma(d, xh + uint32_t(8 * s), b_desc(blo + uint32_t(s * R * 32)), G::IDESC, s > 0);
-#pragma unroll 1
-            for (int s = 0; s < R / 8; ++s)
-                tc_mma(d, xl + uint32_t(8 * s), b_desc(bhi + uint32_t(s * R * 32)), G::IDESC, 1);
-#pragma unroll 1
-            for (int s = 0; s < R / 8; ++s)
-                tc_mma(d, xh + uint32_t(8 * s), b_desc(bhi + uint32_t(s * R * 32)), G::IDESC, 1);
-        }
-        tc_commit(bar);
-    };
-    auto drain = [&](uint64_t t, int buf) {
+        };
+        using Scl = float[NB];
+        // Reads this thread's half rows of the tile staged in buffer pb, scales,
+        // splits and stages them into X of pair pb; records 2^-s per block.
+        auto store_x = [&](int pb, Scl& unscale) {
+            const float2* T = reinterpret_cast<const float2*>(tiles_smem + pb * G::TILE_BYTES);
+            float2 v[NB][H];
 #pragma unroll
-        for (int bk = 0; bk < NB; ++bk) {
-            float2* p = group_ptr(t, bk);
-#pragma unroll
-            for (int c0 = 0; c0 < D; c0 += 16) {
-                float r[16];
-                tmem_ld16(row + uint32_t(bk * BC + 2 * R + buf * R + h * D + c0), r);
+            for (int bk = 0; bk < NB; ++bk) {
                 if (a.vec2) {
 #pragma unroll
-                    for (int m = 0; m < 4; ++m)
-                        *reinterpret_cast<float4*>(p + a.off[c0 / 2 + 2 * m]) =
-                            make_float4(r[4 * m], r[4 * m + 1], r[4 * m + 2], r[4 * m + 3]);
+                    for (int m = 0; m < H / 2; ++m) {
+                        const float4 x = *reinterpret_cast<const float4*>(T + tile_swz(ug[bk] | a.ut[2 * m]));
+                        v[bk][2 * m] = make_float2(x.x, x.y);
+                        v[bk][2 * m + 1] = make_float2(x.z, x.w);
+                    }
                 } else {
 #pragma unroll
-                    for (int e = 0; e < 8; ++e) p[a.off[c0 / 2 + e]] = make_float2(r[2 * e], r[2 * e + 1]);
+                    for (int j = 0; j < H; ++j) v[bk][j] = T[tile_swz(ug[bk] | a.ut[j])];
+                }
+                float m = 0.f;
+#pragma unroll
+                for (int j = 0; j < H; ++j) m = fmaxf(m, fmaxf(fabsf(v[bk][j].x), fabsf(v[bk][j].y)));
+                row_exp[bk][h][32 * q + lane] = scale_exp(m);
+            }
+            asm volatile("bar.sync %0, 64;" ::"r"(1 + q) : "memory");  // warps q and q + 4 share these rows
+#pragma unroll
+            for (int bk = 0; bk < NB; ++bk) {
+                const int e0 = row_exp[bk][0][32 * q + lane], e1 = row_exp[bk][1][32 * q + lane];
+                const int se = e0 < e1 ? e0 : e1;
+                const float f = exp2i(se);
+                unscale[bk] = exp2i(-se);
+#pragma unroll
+                for (int c0 = 0; c0 < H; c0 += 8) {
+                    uint32_t hi[8], lo[8];
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) split_f16(v[bk][c0 + e].x * f, v[bk][c0 + e].y * f, hi[e], lo[e]);
+                    const uint32_t col = uint32_t(bk * BC + pb * R + h * H + c0);
+                    tmem_st8(row + col, hi);
+                    tmem_st8(row + col + R / 2, lo);
                 }
             }
-        }
-    };
+            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        };
+        auto drain = [&](uint64_t t, int pb, const Scl& unscale) {
+            float2* base = tile_base(t);
+#pragma unroll
+            for (int bk = 0; bk < NB; ++bk) {
+                float2* p = base + gg[bk];
+                const float u = unscale[bk];
+#pragma unroll
+                for (int c0 = 0; c0 < D; c0 += 16) {
+                    float r[16];
+                    tmem_ld16(row + uint32_t(bk * BC + 2 * R + pb * R + h * D + c0), r);
+#pragma unroll
+                    for (int e = 0; e < 16; ++e) r[e] = (r[e] * wunscale) * u;  // two factors: each stays in range
+                    if (a.vec2) {
+#pragma unroll
+                        for (int m = 0; m < 4; ++m)
+                            *reinterpret_cast<float4*>(p + a.off[c0 / 2 + 2 * m]) =
+                                make_float4(r[4 * m], r[4 * m + 1], r[4 * m + 2], r[4 * m + 3]);
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) p[a.off[c0 / 2 + e]] = make_float2(r[2 * e], r[2 * e + 1]);
+                    }
+                }
+            }
+        };
 
-    // Software pipeline over this CTA's tiles t0, t0 + step, ...: while the
-    // tensor cores work on tile t, the registers receive tile t + 2 step and
-    // the accumulator of tile t - step drains to HBM; tile t + step (loaded one
-    // stage earlier) is staged into TMEM as soon as tile t's MMAs complete.
-    const uint64_t step = gridDim.x;
-    uint64_t t = blockIdx.x;  // the grid never exceeds the tile count
-    Buf vA, vB;
-    load(t, vA);
-    store_x(vA);
-    tc_fence_before();
-    __syncthreads();
-    if (tid == 0) issue(0);
-    if (t + step < a.tiles) load(t + step, vB);
-    uint64_t prev = 0;
-    bool have_prev = false;
-    int buf = 0;
-    uint32_t phase = 0;
-    // On entry: tile t's MMAs run into accumulator `buf`; `nxt` holds (or is
-    // receiving) tile t + step; `cur` is free. Returns false after the last tile.
-    auto stage = [&](Buf& cur, Buf& nxt) -> bool {
-        const uint64_t tn = t + step, tnn = tn + step;
-        if (tnn < a.tiles) load(tnn, cur);
-        if (have_prev) drain(prev, buf ^ 1);
-        const bool ok = tc_wait_bounded(bar, phase);
-        phase ^= 1;
-        if (__syncthreads_or(!ok)) {
-            if (tid == 0) atomicExch(&g_tc_status, 1);
-            return false;
+        // Stage k (tile t0 + k step, pair k % 2): wait for its copy, stage its X
+        // rows and signal the MMA warp, refill its shared-memory buffer with
+        // tile k + 2, then drain tile k - 1 once its MMAs are complete.
+        issue_load(t0, 0);
+        cp_async_commit();
+        if (ntiles > 1) issue_load(t0 + step, 1);
+        cp_async_commit();
+        bool fail = false;
+        Scl sA, sB;
+        auto stage = [&](uint64_t k, Scl& sc, Scl& scp, int pc) -> bool {
+            const int pn = pc ^ 1;
+            cp_async_wait1();                    // this thread's copies of tile k have landed
+            if (data_bar_any(fail)) return false;  // ... and everyone's; a failure seen by any thread stops all
+            store_x(pc, sc);
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(tc_smem_u32(&x_full[pc]));
+            data_bar();                          // every read of buffer pc is done
+            if (k + 2 < ntiles) issue_load(t0 + (k + 2) * step, pc);
+            cp_async_commit();
+            if (k >= 1) {
+                if (!tc_wait_bounded(tc_smem_u32(&mma_done[pn]), uint32_t(((k - 1) >> 1) & 1))) {
+                    fail = true;
+                    if (tid == 0) atomicExch(&g_tc_status, 2);
+                } else {
+                    tc_fence_after();
+                    drain(t0 + (k - 1) * step, pn, scp);
+                }
+            }
+            return true;
+        };
+        bool live = true;
+        for (uint64_t k = 0; live && k < ntiles; k += 2) {
+            live = stage(k, sA, sB, 0);
+            if (live && k + 1 < ntiles) live = stage(k + 1, sB, sA, 1);
         }
-        tc_fence_after();
-        if (tn >= a.tiles) {
-            drain(t, buf);
-            return false;
+        if (live && !fail) {
+            const uint64_t k = ntiles - 1;
+            const int pl = int(k & 1);
+            if (tc_wait_bounded(tc_smem_u32(&mma_done[pl]), uint32_t((k >> 1) & 1))) {
+                tc_fence_after();
+                drain(t0 + k * step, pl, pl ? sB : sA);
+            } else if (tid == 0) {
+                atomicExch(&g_tc_status, 2);
+            }
         }
-        store_x(nxt);  // tile t's MMAs are done: X may be overwritten
-        tc_fence_before();
-        __syncthreads();
-        if (tid == 0) issue(buf ^ 1);
-        prev = t;
-        have_prev = true;
-        t = tn;
-        buf ^= 1;
-        return true;
-    };
-    while (stage(vA, vB) && stage(vB, vA)) {
+        asm volatile("cp.async.wait_all;" ::: "memory");
     }
     tc_fence_before();
     __syncthreads();
@@ -415,7 +547,6 @@ int try_dense_tc(void* sv, const void* op, int nbits, const int* sorted, const i
     if (batch > 1 && op_stride != 0) return QGB_EDECLINE;  // one operator for the whole batch
     TcArgs a{};
     a.k = k;
-    for (int j = 0; j < k; ++j) a.sorted[j] = sorted[j];
     const int D = 1 << k;
     uint64_t scat[1 << QGB_MAX_K];
     for (int j = 0; j < D; ++j) {
@@ -433,8 +564,45 @@ int try_dense_tc(void* sv, const void* op, int nbits, const int* sorted, const i
             if (scat[j] == oo) a.perm_out[j] = c;
         }
     }
+    // cp.async copies 16-byte granules: the state (and every state of a batch) must start 16-byte aligned
+    if ((reinterpret_cast<uintptr_t>(sv) % 16) || (batch > 1 && (sv_stride % 2))) return QGB_EDECLINE;
     a.vec2 = sorted[0] == 0 ? 1 : 0;
-    if (a.vec2 && ((reinterpret_cast<uintptr_t>(sv) % 16) || (batch > 1 && (sv_stride % 2)))) a.vec2 = 0;
+    // tile bits: the targets and the 13 - k lowest other bits
+    {
+        int nt = 0, ng = 0, ti = 0;
+        for (int b = 0; b < nbits && ti < 13; ++b) {
+            bool is_t = false;
+            for (int j = 0; j < k; ++j) is_t |= sorted[j] == b;
+            if (is_t) {
+                a.tile_bits[ti++] = b;
+                ++nt;
+            } else if (ng < 13 - k) {
+                a.pos_g[ng++] = ti;
+                a.tile_bits[ti++] = b;
+            }
+        }
+        if (ti != 13 || nt != k || ng != 13 - k) return set_error(QGB_EINVAL, "tensor-core tile geometry");
+        a.L = 0;
+        while (a.L < 13 && a.tile_bits[a.L] == a.L) ++a.L;
+        if (a.L < 7) return set_error(QGB_EINVAL, "tensor-core tile run shorter than 128");
+        for (int j = 0; j < (1 << (13 - a.L)); ++j) {
+            uint64_t o = 0;
+            for (int i = 0; i < 13 - a.L; ++i)
+                if ((j >> i) & 1) o |= uint64_t(1) << a.tile_bits[a.L + i];
+            a.hoff[j] = o;
+        }
+        int pos_t[QGB_MAX_K];
+        for (int j = 0; j < k; ++j)
+            for (int i = 0; i < 13; ++i)
+                if (a.tile_bits[i] == sorted[j]) pos_t[j] = i;
+        for (int j = 0; j < D / 2; ++j) {
+            uint32_t u = 0;
+            for (int i = 0; i < k - 1; ++i)
+                if ((j >> i) & 1) u |= 1u << pos_t[i];
+            a.ut[j] = u;
+        }
+        a.ut_h = 1u << pos_t[k - 1];
+    }
     a.tiles_per_state = uint64_t(1) << (nbits - 13);  // 8192 amplitudes per tile
     a.tiles = a.tiles_per_state * uint64_t(batch);
     a.sv_stride = batch > 1 ? sv_stride : 0;

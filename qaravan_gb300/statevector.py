@@ -79,13 +79,18 @@ class StatevectorSim:
         if self.device.type != "cuda":
             raise _lib.QgbError("qaravan_gb300 runs on CUDA devices only")
         self.dtype = dtype
-        # auto: complex64 -> dense 4-qubit fused blocks, one HBM pass each (fastest measured on the
-        # 28-qubit brickwork); complex128 -> 3-qubit blocks grouped into shared-memory tile sweeps
-        # (float64 arithmetic dominates, so fewer passes win)
+        # auto: complex64 -> dense fused blocks, one HBM pass each: 6-qubit blocks on the tensor
+        # cores from 13 qubits up (half the passes of 4-qubit blocks at the same speed per pass,
+        # fastest measured on the 28-qubit brickwork), 4-qubit blocks on the CUDA cores below;
+        # complex128 -> 3-qubit blocks grouped into shared-memory tile sweeps (float64 arithmetic
+        # dominates, so fewer passes win)
         if mode == "auto":
             mode = "fused" if dtype == torch.complex64 else "sweep"
         if fusion_width is None:
-            fusion_width = 4 if dtype == torch.complex64 else 3
+            if dtype == torch.complex64:
+                fusion_width = 6 if circ.num_sites >= 13 and _lib.lib().qgb_get_dense_impl() >= 1 else 4
+            else:
+                fusion_width = 3
         if tile_bits is None:
             tile_bits = 14 if dtype == torch.complex64 else 13
         self.mode, self.fusion_width, self.tile_bits, self.low_bits = mode, fusion_width, tile_bits, low_bits
