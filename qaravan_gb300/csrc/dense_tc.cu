@@ -71,8 +71,9 @@ struct TcArgs {
     int pos_g[13];                       // tile positions of the 13 - k group bits, ascending
     int perm_in[1 << QGB_MAX_K];         // memory-order input component j -> matrix column
     int perm_out[1 << QGB_MAX_K];        // memory-order output component i -> matrix row
-    uint32_t ut[1 << (QGB_MAX_K - 1)];   // tile-index offsets of the low-half components
+    uint32_t uts[1 << (QGB_MAX_K - 1)];  // swizzled tile-index offsets of the low-half components
     uint32_t ut_h;                       // tile-index offset of the upper half (target sorted[k-1])
+    uint64_t g512[16];                   // global offset of tile index 512 m
     uint64_t off[1 << (QGB_MAX_K - 1)];  // global offsets of the low-half components
     uint64_t hstride;                    // global offset of the upper half
     uint64_t hoff[64];                   // global offset of tile bits L..12, indexed by u >> L
@@ -135,8 +136,10 @@ __device__ __forceinline__ uint32_t b_off(int n, int k, int R) {
 // granule index (bits 1..3) is XORed with a fold of the higher bits, so the 32
 // lanes reading one component of 32 rows hit distinct banks whether the rows
 // differ in low or in high tile bits. Bit 0 is left alone: a 16-byte granule
-// (two amplitudes) stays whole, as cp.async copies it.
-__device__ __forceinline__ uint32_t tile_swz(uint32_t u) {
+// (two amplitudes) stays whole, as cp.async copies it. The map is linear over
+// XOR, so swz(a | b) = swz(a) ^ swz(b) for disjoint bit sets: row and
+// component parts are swizzled once and combined with one XOR.
+__host__ __device__ __forceinline__ uint32_t tile_swz(uint32_t u) {
     return u ^ ((((u >> 4) ^ (u >> 7) ^ (u >> 10)) & 7u) << 1);
 }
 
@@ -330,29 +333,31 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
         const uint32_t row = tmem + (uint32_t(32 * q) << 16);  // this warp's lane quarter
         const uint32_t runmask = (1u << a.L) - 1u;
         // Tile-index and global offsets of this thread's rows (the same in every tile).
-        uint32_t ug[NB];
-        uint64_t gg[NB];
+        uint32_t sug[NB];  // swizzled tile index of this thread's rows (and half)
+        uint64_t gg[NB];   // their global offsets
 #pragma unroll
         for (int bk = 0; bk < NB; ++bk) {
             const uint32_t r = uint32_t(bk * 128 + 32 * q + lane);
             uint32_t u = 0;
 #pragma unroll
             for (int i = 0; i < 13 - K; ++i) u |= ((r >> i) & 1u) << a.pos_g[i];
-            ug[bk] = u | (h ? a.ut_h : 0u);
+            sug[bk] = tile_swz(u | (h ? a.ut_h : 0u));
             gg[bk] = uint64_t(u & runmask) + a.hoff[u >> a.L] + (h ? a.hstride : 0);
         }
+        // cp.async granule m of this thread: tile index 2 tid + 512 m
+        const uint32_t ctid = 2u * uint32_t(tid);
+        const uint32_t sctid = tile_swz(ctid);
+        const uint64_t gctid = uint64_t(ctid & runmask) + a.hoff[ctid >> a.L];
         auto tile_base = [&](uint64_t t) -> float2* {
             const uint64_t b = t / a.tiles_per_state, tt = t - b * a.tiles_per_state;
             return sv + int64_t(b) * a.sv_stride + insert_zeros(tt, a.tile_bits, 13);
         };
         auto issue_load = [&](uint64_t t, int pb) {
-            const float2* base = tile_base(t);
+            const float2* base = tile_base(t) + gctid;
             const uint32_t dst0 = tc_smem_u32(tiles_smem + pb * G::TILE_BYTES);
-#pragma unroll 4
-            for (int m = 0; m < 4096 / kTcDataThreads; ++m) {
-                const uint32_t u = 2u * uint32_t(tid + m * kTcDataThreads);
-                cp_async16(dst0 + 8u * tile_swz(u), base + (u & runmask) + a.hoff[u >> a.L]);
-            }
+#pragma unroll
+            for (int m = 0; m < 4096 / kTcDataThreads; ++m)
+                cp_async16(dst0 + 8u * (sctid ^ tile_swz(512u * uint32_t(m))), base + a.g512[m]);
         };
         using Scl = float[NB];
         // Reads this thread's half rows of the tile staged in buffer pb, scales,
@@ -365,13 +370,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
                 if (a.vec2) {
 #pragma unroll
                     for (int m = 0; m < H / 2; ++m) {
-                        const float4 x = *reinterpret_cast<const float4*>(T + tile_swz(ug[bk] | a.ut[2 * m]));
+                        const float4 x = *reinterpret_cast<const float4*>(T + (sug[bk] ^ a.uts[2 * m]));
                         v[bk][2 * m] = make_float2(x.x, x.y);
                         v[bk][2 * m + 1] = make_float2(x.z, x.w);
                     }
                 } else {
 #pragma unroll
-                    for (int j = 0; j < H; ++j) v[bk][j] = T[tile_swz(ug[bk] | a.ut[j])];
+                    for (int j = 0; j < H; ++j) v[bk][j] = T[sug[bk] ^ a.uts[j]];
                 }
                 float m = 0.f;
 #pragma unroll
@@ -599,9 +604,13 @@ int try_dense_tc(void* sv, const void* op, int nbits, const int* sorted, const i
             uint32_t u = 0;
             for (int i = 0; i < k - 1; ++i)
                 if ((j >> i) & 1) u |= 1u << pos_t[i];
-            a.ut[j] = u;
+            a.uts[j] = tile_swz(u);
         }
         a.ut_h = 1u << pos_t[k - 1];
+        for (int m = 0; m < 16; ++m) {
+            const uint32_t u = 512u * uint32_t(m);
+            a.g512[m] = uint64_t(u & ((1u << a.L) - 1u)) + a.hoff[u >> a.L];
+        }
     }
     a.tiles_per_state = uint64_t(1) << (nbits - 13);  // 8192 amplitudes per tile
     a.tiles = a.tiles_per_state * uint64_t(batch);
