@@ -66,6 +66,7 @@ __device__ int g_tc_status = 0;
 struct TcArgs {
     int k;
     int vec2;                            // global bit 0 is a target: components (2m, 2m+1) adjacent
+    int vec4;                            // global bits 0 and 1 are targets: rows are runs of >= 4 components
     int L;                               // tile bits 0..L-1 are global bits 0..L-1 (L >= 7)
     int tile_bits[13];                   // global bit of each tile bit, ascending
     int pos_g[13];                       // tile positions of the 13 - k group bits, ascending
@@ -95,7 +96,8 @@ template <int K> struct TcGeom {
     static constexpr int NCOLS = NB * BCOLS;  // 512: one CTA per SM
     static constexpr uint32_t B_BYTES = uint32_t(R) * R * 2;
     static constexpr uint32_t TILE_BYTES = 8192 * 8;
-    static constexpr size_t SMEM = 2 * size_t(B_BYTES) + 2 * size_t(TILE_BYTES) + 128;
+    static constexpr uint32_t STAGE_BYTES = 8 * 2048;  // per data warp: 32 rows x 8 components of output
+    static constexpr size_t SMEM = 2 * size_t(B_BYTES) + 2 * size_t(TILE_BYTES) + STAGE_BYTES + 128;
     // kind::f16 instruction descriptor: f32 accumulator, f16 A and B, both
     // K-major, N = R, M = 128.
     static constexpr uint32_t IDESC = (1u << 4) | (uint32_t(R >> 3) << 17) | (uint32_t(128 >> 4) << 24);
@@ -243,6 +245,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
     unsigned char* Bhi = sb;
     unsigned char* Blo = sb + G::B_BYTES;
     unsigned char* tiles_smem = sb + 2 * G::B_BYTES;  // two staged tiles of TILE_BYTES
+    unsigned char* stage_smem = tiles_smem + 2 * G::TILE_BYTES;  // output staging, 2 KB per data warp
     __shared__ __align__(8) uint64_t x_full[2];    // data warps -> MMA warp: X of pair p staged (8 arrivals)
     __shared__ __align__(8) uint64_t mma_done[2];  // MMA warp -> data warps: accumulator of pair p complete
     __shared__ uint32_t tmem_slot;
@@ -414,7 +417,28 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
                     tmem_ld16(row + uint32_t(bk * BC + 2 * R + pb * R + h * D + c0), r);
 #pragma unroll
                     for (int e = 0; e < 16; ++e) r[e] = (r[e] * wunscale) * u;  // two factors: each stays in range
-                    if (a.vec2) {
+                    if (a.vec4) {
+                        // Rows are runs of >= 4 contiguous components: pass the 32 rows x 8
+                        // components through this warp's staging area so that 4 lanes write
+                        // one row's 64 contiguous bytes (whole sectors) and 8 rows go per store.
+                        // 16-byte pieces are XOR-swizzled by (row / 2) % 4 against bank conflicts.
+                        float4* st4 = reinterpret_cast<float4*>(stage_smem + warp * 2048);
+#pragma unroll
+                        for (int m = 0; m < 4; ++m)
+                            st4[lane * 4 + (m ^ ((lane >> 1) & 3))] =
+                                make_float4(r[4 * m], r[4 * m + 1], r[4 * m + 2], r[4 * m + 3]);
+                        __syncwarp();
+                        const int pc = lane & 3;
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) {
+                            const int rho = 8 * i + (lane >> 2);
+                            const float4 x = st4[rho * 4 + (pc ^ ((rho >> 1) & 3))];
+                            float2* pr = reinterpret_cast<float2*>(
+                                __shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(p), rho));
+                            *reinterpret_cast<float4*>(pr + a.off[c0 / 2 + 2 * pc]) = x;
+                        }
+                        __syncwarp();
+                    } else if (a.vec2) {
 #pragma unroll
                         for (int m = 0; m < 4; ++m)
                             *reinterpret_cast<float4*>(p + a.off[c0 / 2 + 2 * m]) =
@@ -572,6 +596,7 @@ int try_dense_tc(void* sv, const void* op, int nbits, const int* sorted, const i
     // cp.async copies 16-byte granules: the state (and every state of a batch) must start 16-byte aligned
     if ((reinterpret_cast<uintptr_t>(sv) % 16) || (batch > 1 && (sv_stride % 2))) return QGB_EDECLINE;
     a.vec2 = sorted[0] == 0 ? 1 : 0;
+    a.vec4 = (k >= 2 && sorted[0] == 0 && sorted[1] == 1) ? 1 : 0;
     // tile bits: the targets and the 13 - k lowest other bits
     {
         int nt = 0, ng = 0, ti = 0;
