@@ -201,6 +201,28 @@ void qgb_philox_uniform(uint32_t event, uint32_t traj, uint32_t stream, uint64_t
 
 /* ---- batches of small uneven circuits ------------------------------------ */
 
+/* Layout sizes of the two device tables qgb_fuse_blocks reads:
+ *   block (qgb_fuse_block_bytes() bytes): int64 out (element offset of the
+ *     block's 2^k x 2^k row-major matrix in `out`), int32 k (<= 6), int32
+ *     op_begin, int32 op_end (its entries in the entry table, first applied
+ *     first), int32 pad;
+ *   entry (qgb_fuse_entry_bytes() bytes): int32 k (<= the block's k), int32
+ *     pos[6] (block-matrix bit of each op bit, 0 = most significant, in the
+ *     op's matrix order), int32 pad, int64 mat (complex128 element offset of
+ *     the op's 2^k x 2^k row-major matrix in `op_mats`). */
+size_t qgb_fuse_block_bytes(void);
+size_t qgb_fuse_entry_bytes(void);
+
+/* The matrix products of gate fusion, on the device (no counterpart in the
+ * reference, which applies each gate as its own contraction through
+ * BaseSim.run, core/base_sim.py:30-53): block b = E_m ... E_1, E_i the
+ * embedding of entry i's op matrix into the block's bits, composed in float64
+ * and written to `out` in `dtype`. Tables and op matrices are device memory;
+ * `out_elems` and `op_elems` bound every offset: an entry outside them is
+ * skipped and reported by qgb_check_status (QGB_EINVAL). */
+int qgb_fuse_blocks(void* out, int dtype, int64_t out_elems, const void* blocks, int nblocks,
+                    const void* entries, int nentries, const void* op_mats, int64_t op_elems, void* stream);
+
 /* Layout sizes of the two device tables qgb_batch_small reads:
  *   circuit (qgb_batch_circuit_bytes() bytes): int64 offset (elements into
  *     `states`), int64 out_offset (doubles into `out`), int32 nbits, int32

@@ -51,6 +51,9 @@ SIGNATURES = {
     "qgb_set_sweep_impl": (C.c_int, [_i]),
     "qgb_init_basis": (C.c_int, [_vp, _i, _i, _u64, _i64, _i64, _vp]),
     "qgb_scale": (C.c_int, [_vp, _i, _i, _vp, _i64, _i64, _vp]),
+    "qgb_fuse_block_bytes": (C.c_size_t, []),
+    "qgb_fuse_entry_bytes": (C.c_size_t, []),
+    "qgb_fuse_blocks": (C.c_int, [_vp, _i, _i64, _vp, _i, _vp, _i, _vp, _i64, _vp]),
     "qgb_set_dense_impl": (C.c_int, [_i]),
     "qgb_get_dense_impl": (C.c_int, []),
     "qgb_reduce_scratch_bytes": (C.c_size_t, [_i, _i, _i64]),

@@ -70,7 +70,7 @@ class _Runner:
         kcap = 5 if self.dtype == torch.complex64 else 4
         isz = torch.empty(0, dtype=self.dtype).element_size()
         plan = compile_ops(ops, n, mode=self.sim.mode, width=self.sim.fusion_width, tile_bits=self.sim.tile_bits,
-                           low_bits=self.sim.low_bits, max_sweep_k=kcap, itemsize=isz)
+                           low_bits=self.sim.low_bits, max_sweep_k=kcap, itemsize=isz, device_fusion=True)
         psi = torch.empty(2 ** n, dtype=self.dtype, device=self.device)
         L = _lib.lib()
         _lib.check(L.qgb_init_basis(psi.data_ptr(), self.code, n, 0, 1, 0, _lib.stream_ptr(self.device)), "init")

@@ -106,11 +106,15 @@ class DensityMatrixBatch:
     # ------------------------------------------------------------ large path
     def _prep_large(self, large, max_streams):
         self.large = []
+        tc = self.isz == 8 and _lib.lib().qgb_get_dense_impl() >= 1
         for i, s, ops in large:
             nb = 2 * s.num_sites
-            tile, width = autotune.choose(nb, self.dtype)
-            plan = compile_ops(ops, nb, mode="sweep", width=width, tile_bits=tile,
-                               max_sweep_k=5 if self.isz == 8 else 4, itemsize=self.isz)
+            if tc and nb >= 13:  # 6-qubit fused blocks on the tensor cores, one HBM pass each
+                plan = compile_ops(ops, nb, mode="fused", width=6, itemsize=self.isz, device_fusion=True)
+            else:
+                tile, width = autotune.choose(nb, self.dtype)
+                plan = compile_ops(ops, nb, mode="sweep", width=width, tile_bits=tile,
+                                   max_sweep_k=5 if self.isz == 8 else 4, itemsize=self.isz, device_fusion=True)
             ex = Executor(plan, self.dtype, self.device, mode_normalize="dm")
             state = torch.empty(4 ** s.num_sites, dtype=self.dtype, device=self.device)
             L = _lib.lib()

@@ -11,7 +11,10 @@ the same op sequence into fewer passes over HBM:
    construction shares no bit with it); earlier blocks whose bits are covered
    and that nothing in between touches are then absorbed too, which folds
    single-qubit layers into the neighbouring two-qubit gates. Matrices are
-   composed on the host in complex128.
+   composed on the host in complex128 (``fuse``) or, with
+   ``device_fusion=True``, only the block membership is decided on the host
+   (``fuse_symbolic``, same decisions) and the products run on the GPU
+   (``qgb_fuse_blocks``) from the raw op matrices.
 2. **Sweep planning** (``plan_sweeps``): consecutive blocks are grouped into
    sweeps whose bits fit one shared-memory tile (the low ``L`` flat bits plus up
    to ``H`` chosen high bits). A block is skipped -- and every later block
@@ -58,15 +61,36 @@ class NormalizeStep:
 
 
 @dataclass
+class Recipe:
+    """A fused block to be composed on the device: its bits (matrix order) and
+    the ops applied to it, first applied first, as (op matrix index into
+    ``Plan.op_matrices``, op bits in the op's matrix order)."""
+    bits: list
+    entries: list
+
+
+@dataclass
 class Plan:
     nbits: int
     steps: list = field(default_factory=list)
-    matrices: list = field(default_factory=list)  # complex128 arrays
+    matrices: list = field(default_factory=list)  # complex128 arrays (host-composed), or Recipe objects
     n_gates: int = 0  # original op count
+    op_matrices: list = field(default_factory=list)  # raw op matrices the recipes refer to
 
     def add_matrix(self, m):
-        self.matrices.append(np.ascontiguousarray(m, dtype=np.complex128))
+        if isinstance(m, Recipe):
+            self.matrices.append(m)
+        else:
+            self.matrices.append(np.ascontiguousarray(m, dtype=np.complex128))
         return len(self.matrices) - 1
+
+    @property
+    def device_fused(self):
+        return any(isinstance(m, Recipe) for m in self.matrices)
+
+    def matrix_dim(self, i):
+        m = self.matrices[i]
+        return 2 ** len(m.bits) if isinstance(m, Recipe) else m.shape[0]
 
     @property
     def n_sweeps(self):
@@ -157,6 +181,62 @@ def fuse(ops, width):
     return [b for b in blocks if b is not None]
 
 
+@dataclass
+class SymBlock:
+    bits: list
+    ops: list  # indices into the fused op list, first applied first
+
+    @property
+    def n_ops(self):
+        return len(self.ops)
+
+
+def fuse_symbolic(ops, width):
+    """The decisions of :func:`fuse` without the matrix products: blocks of at
+    most ``width`` bits, each with the indices of its ops in application order
+    (an absorbed earlier block's ops go in front: it is applied first)."""
+    blocks: list = []
+    last: dict = {}
+    for oi, op in enumerate(ops):
+        bits = list(op.bits)
+        if len(bits) > width:
+            raise ValueError(f"op on {len(bits)} bits exceeds fusion width {width}")
+        deps = [last[b] for b in bits if b in last]
+        cand = max(deps) if deps else None
+        if cand is not None and blocks[cand] is not None and len(_union(blocks[cand].bits, bits)) <= width:
+            blk = blocks[cand]
+            u = sorted(_union(blk.bits, bits), reverse=True)
+            blk.ops.append(oi)
+            blk.bits = u
+            for b in bits:
+                last[b] = cand
+            for j in sorted({d for d in deps if d != cand}, reverse=True):
+                bj = blocks[j]
+                if bj is None or not set(bj.bits) <= set(u):
+                    continue
+                if any(blocks[i] is not None and set(blocks[i].bits) & set(bj.bits) for i in range(j + 1, cand)):
+                    continue
+                blk.ops = bj.ops + blk.ops
+                blocks[j] = None
+                for b in bj.bits:
+                    if last.get(b) == j:
+                        last[b] = cand
+            continue
+        blocks.append(SymBlock(sorted(bits, reverse=True) if len(bits) > 1 else list(bits), [oi]))
+        for b in bits:
+            last[b] = len(blocks) - 1
+    return [b for b in blocks if b is not None]
+
+
+def recipe_matrix(recipe, op_matrices):
+    """Host (complex128) composition of a :class:`Recipe` -- what the device
+    computes; used to check the device kernel and the symbolic fusion."""
+    m = np.eye(2 ** len(recipe.bits), dtype=np.complex128)
+    for mi, bits in recipe.entries:
+        m = embed(op_matrices[mi], bits, recipe.bits) @ m
+    return m
+
+
 # --------------------------------------------------------- sweep planning
 
 def plan_sweeps(blocks, nbits, tile_bits, low_bits=None, max_high=QGB_SWEEP_MAX_HIGH):
@@ -207,14 +287,16 @@ def plan_sweeps(blocks, nbits, tile_bits, low_bits=None, max_high=QGB_SWEEP_MAX_
 
 # ------------------------------------------------------------------- plans
 
-def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, max_sweep_k=5, itemsize=8):
+def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, max_sweep_k=5, itemsize=8,
+                device_fusion=False):
     """Compile an op sequence (with ``None`` marking a renormalisation point)
     into a :class:`Plan`.
 
     ``mode``: ``"gate"`` one pass per op; ``"fused"`` one pass per fused block of
     ``width`` bits; ``"sweep"`` fused blocks grouped into shared-memory tile sweeps.
     ``itemsize`` (8 for complex64, 16 for complex128) caps the tile at 128 KiB
-    of shared memory.
+    of shared memory. ``device_fusion``: block matrices are left as
+    :class:`Recipe` objects for the executor to compose on the GPU.
     """
     tile_bits = min(tile_bits, 14 if itemsize <= 8 else 13)
     plan = Plan(nbits=nbits, n_gates=sum(1 for o in ops if o is not None))
@@ -238,7 +320,13 @@ def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, 
                 plan.steps.append(DenseStep(list(o.bits), plan.add_matrix(o.matrix)))
             continue
         w = max(width, max(len(o.bits) for o in seg))
-        blocks = fuse(seg, w)
+        if device_fusion:
+            base = len(plan.op_matrices)
+            plan.op_matrices.extend(np.ascontiguousarray(o.matrix, dtype=np.complex128) for o in seg)
+            blocks = [Block(b.bits, Recipe(list(b.bits), [(base + i, list(seg[i].bits)) for i in b.ops]), b.n_ops)
+                      for b in fuse_symbolic(seg, w)]
+        else:
+            blocks = fuse(seg, w)
         if mode == "fused" or w > max_sweep_k or tile_bits <= 0:
             for b in blocks:
                 plan.steps.append(DenseStep(list(b.bits), plan.add_matrix(b.matrix)))

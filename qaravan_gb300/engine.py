@@ -4,8 +4,11 @@ device-resident vectors through the C ABI.
 All gate matrices of a plan are uploaded once, packed into one device buffer
 in the state's dtype (the reference instead converts and copies every gate
 matrix host-to-device inside ``StatevectorSim.apply_gate``,
-``tensorQ/statevector_sim.py:19-29,50-52``). Every launch goes to the current
-torch stream; nothing synchronises, so a run can be captured in a CUDA graph.
+``tensorQ/statevector_sim.py:19-29,50-52``). A plan compiled with device
+fusion uploads only the raw op matrices and the block tables (one pinned copy)
+and composes the fused blocks on the GPU (``qgb_fuse_blocks``). Every launch
+goes to the current torch stream; nothing synchronises, so a run can be
+captured in a CUDA graph.
 """
 from __future__ import annotations
 
@@ -15,7 +18,10 @@ import numpy as np
 import torch
 
 from . import _lib
-from .compiler import DenseStep, NormalizeStep, Plan, SweepStep
+from .compiler import DenseStep, NormalizeStep, Plan, Recipe, SweepStep
+
+_FUSE_BLOCK = np.dtype([("out", "<i8"), ("k", "<i4"), ("op_begin", "<i4"), ("op_end", "<i4"), ("pad", "<i4")])
+_FUSE_ENTRY = np.dtype([("k", "<i4"), ("pos", "<i4", (6,)), ("pad", "<i4"), ("mat", "<i8")])
 
 
 def real_dtype(dtype):
@@ -42,21 +48,24 @@ class Executor:
         self.code = _lib.dtype_code(dtype)
         self.device = torch.device(device)
         self.normalize_kind = mode_normalize  # "sv": divide by the 2-norm; "dm": by the trace
-        offs, flat = [], []
-        o = 0
-        for m in plan.matrices:
-            offs.append(o)
-            flat.append(m.reshape(-1))
-            o += m.size
+        if plan.device_fused:
+            offs = self._fuse_on_device(plan)
+        else:
+            offs, flat = [], []
+            o = 0
+            for m in plan.matrices:
+                offs.append(o)
+                flat.append(m.reshape(-1))
+                o += m.size
+            host = np.concatenate(flat) if flat else np.zeros(1, np.complex128)
+            pinned = torch.from_numpy(host).to(dtype=dtype)
+            if torch.cuda.is_available():
+                pinned = pinned.pin_memory()
+            self.mats = pinned.to(device=self.device, non_blocking=True)
+            self._pinned = pinned  # alive until the copy is ordered before any use
+            self.h2d_bytes = self.mats.numel() * self.mats.element_size()
         self.mat_offsets = offs
-        host = np.concatenate(flat) if flat else np.zeros(1, np.complex128)
-        pinned = torch.from_numpy(host).to(dtype=dtype)
-        if torch.cuda.is_available():
-            pinned = pinned.pin_memory()
-        self.mats = pinned.to(device=self.device, non_blocking=True)
-        self._pinned = pinned  # alive until the copy is ordered before any use
         self.itemsize = self.mats.element_size()
-        self.h2d_bytes = self.mats.numel() * self.itemsize
         self._steps = []
         for s in plan.steps:
             if isinstance(s, DenseStep):
@@ -81,6 +90,66 @@ class Executor:
         self.scratch = Scratch(self.device)
         self.norm = torch.empty(1, dtype=torch.float64, device=self.device)
         self.launches = 0
+
+    def _fuse_on_device(self, plan):
+        """Uploads the raw op matrices (complex128) and the block/entry tables in
+        one pinned buffer and composes every block matrix on the GPU; returns the
+        element offset of each plan matrix in ``self.mats``."""
+        L = _lib.lib()
+        if L.qgb_fuse_block_bytes() != _FUSE_BLOCK.itemsize or L.qgb_fuse_entry_bytes() != _FUSE_ENTRY.itemsize:
+            raise _lib.QgbError("fusion table layout mismatch with the library")
+        op_mats = list(plan.op_matrices)
+        recipes = []
+        for m in plan.matrices:
+            if isinstance(m, Recipe):
+                recipes.append(m)
+            else:  # a host matrix: a one-entry recipe on its own bit order
+                k = int(np.log2(m.shape[0]))
+                op_mats.append(np.ascontiguousarray(m, dtype=np.complex128))
+                bits = list(range(k - 1, -1, -1))
+                recipes.append(Recipe(bits, [(len(op_mats) - 1, bits)]))
+        op_off, o = [], 0
+        for m in op_mats:
+            op_off.append(o)
+            o += m.size
+        n_op_elems = max(o, 1)
+        blocks = np.zeros(len(recipes), dtype=_FUSE_BLOCK)
+        n_ent = sum(len(r.entries) for r in recipes)
+        ents = np.zeros(max(n_ent, 1), dtype=_FUSE_ENTRY)
+        offs, out, e = [], 0, 0
+        for i, r in enumerate(recipes):
+            k = len(r.bits)
+            offs.append(out)
+            blocks[i] = (out, k, e, e + len(r.entries), 0)
+            pos_of = {b: j for j, b in enumerate(r.bits)}
+            for mi, obits in r.entries:
+                ents["k"][e] = len(obits)
+                ents["pos"][e, :len(obits)] = [pos_of[b] for b in obits]
+                ents["mat"][e] = op_off[mi]
+                e += 1
+            out += 4 ** k
+        opm = np.concatenate([m.reshape(-1) for m in op_mats]) if op_mats else np.zeros(1, np.complex128)
+        sections = [opm.view(np.uint8), blocks.view(np.uint8), ents.view(np.uint8)]
+        starts, nbytes = [], 0
+        for sec in sections:
+            starts.append(nbytes)
+            nbytes += (sec.size + 15) // 16 * 16
+        host = np.zeros(nbytes, dtype=np.uint8)
+        for st0, sec in zip(starts, sections):
+            host[st0:st0 + sec.size] = sec
+        pinned = torch.from_numpy(host)
+        if torch.cuda.is_available():
+            pinned = pinned.pin_memory()
+        dev = pinned.to(device=self.device, non_blocking=True)
+        self._pinned = pinned  # alive until the copy is ordered before any use
+        self._fuse_tables = dev
+        self.h2d_bytes = nbytes
+        self.mats = torch.empty(max(out, 1), dtype=self.dtype, device=self.device)
+        base = dev.data_ptr()
+        _lib.check(L.qgb_fuse_blocks(self.mats.data_ptr(), self.code, self.mats.numel(), base + starts[1],
+                                     len(recipes), base + starts[2], n_ent, base + starts[0], n_op_elems,
+                                     _lib.stream_ptr(self.device)), "fuse_blocks")
+        return offs
 
     def run(self, state: torch.Tensor, batch: int = 1, stride: int = 0, mats: torch.Tensor | None = None,
             mat_stride: int = 0, events: list | None = None):

@@ -123,7 +123,7 @@ class StatevectorSim:
             kcap = 5 if self.dtype == torch.complex64 else 4
             plan = compile_ops(ops, self.num_sites, mode=self.mode, width=self.fusion_width,
                                tile_bits=self.tile_bits, low_bits=self.low_bits, max_sweep_k=kcap,
-                               itemsize=torch.empty(0, dtype=self.dtype).element_size())
+                               itemsize=torch.empty(0, dtype=self.dtype).element_size(), device_fusion=True)
             self._exec = Executor(plan, self.dtype, self.device)
         return self._exec
 

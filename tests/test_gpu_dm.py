@@ -97,9 +97,11 @@ def test_dm_kats(dtype):
 
 
 @pytest.mark.parametrize("dtype", DTYPES)
-def test_dm_noisy_tfi_10q(dtype):
+@pytest.mark.parametrize("mode,width,tile", [("sweep", 4, 12), ("auto", None, 13)])
+def test_dm_noisy_tfi_10q(dtype, mode, width, tile):
     """Per-gate depolarising + amplitude damping on the 10-qubit TFI Trotter
-    circuit, as vec(rho) on 20 bits, against the reference DM run."""
+    circuit, as vec(rho) on 20 bits, against the reference DM run; "auto" is the
+    default path (6-qubit fused blocks on the tensor cores for complex64)."""
     from qaravan_gb300 import DensityMatrixSim
     from qaravan_gb300.circuits import Circuit
     from qaravan_gb300.gates import ID
@@ -116,7 +118,7 @@ def test_dm_noisy_tfi_10q(dtype):
     circ = Circuit([g for g in seq if g.name != "ID"], n=n)
     circ.layers = [[g] for g in seq]
     circ.built = True
-    sim = DensityMatrixSim(circ, dtype=dtype, mode="sweep", fusion_width=4, tile_bits=12)
+    sim = DensityMatrixSim(circ, dtype=dtype, mode=mode, fusion_width=width, tile_bits=tile)
     sim.run()
     zs = sim.pauli_expectations([(1.0, 'i' * q + 'z' + 'i' * (n - q - 1)) for q in range(n)]).cpu().numpy()
     assert np.max(np.abs(zs - z["z"])) < 10 * TOL[dtype]
