@@ -79,6 +79,15 @@ int qgb_check_status(void* stream);
 int qgb_op_action(void* sv, int dtype, int n, const int* indices, int k, const void* op,
                   int64_t op_stride, int64_t batch, int64_t sv_stride, void* stream);
 
+/* qgb_op_action for an op the caller knows to be unitary (fused gate blocks):
+ * the tensor-core path then rescales each group of 2^k amplitudes to its input
+ * norm, which a unitary preserves exactly, removing the systematic shrinkage of
+ * the tensor cores' round-toward-zero fp32 accumulation (about 1e-7 of the
+ * norm per pass). Other paths ignore the hint. No counterpart in the
+ * reference, which applies gates through op_action (:124-140). */
+int qgb_op_action_unitary(void* sv, int dtype, int n, const int* indices, int k, const void* op,
+                          int64_t op_stride, int64_t batch, int64_t sv_stride, void* stream);
+
 /* A fused pass (several gates per read+write of the state), planned by the
  * host compiler from a Circuit's gate list (core/base_sim.py:30-53 loop). */
 int qgb_apply_sweep(void* sv, int dtype, int n, const qgb_sweep* sweep, const void* mats,

@@ -46,6 +46,7 @@ class Op:
 class DenseStep:
     bits: list
     mat: int  # index into the plan's matrix list
+    unitary: bool = False  # the block is unitary (every op in it is): its launch may restore group norms
 
 
 @dataclass
@@ -287,6 +288,21 @@ def plan_sweeps(blocks, nbits, tile_bits, low_bits=None, max_high=QGB_SWEEP_MAX_
 
 # ------------------------------------------------------------------- plans
 
+def unitary_flags(ops, tol=1e-6):
+    """Whether each op's matrix is unitary (max |M^H M - I| < tol), batched by size."""
+    flags = [False] * len(ops)
+    by_dim: dict = {}
+    for i, o in enumerate(ops):
+        m = np.asarray(o.matrix)
+        by_dim.setdefault(m.shape[0], []).append(i)
+    for d, idx in by_dim.items():
+        m = np.stack([np.asarray(ops[i].matrix, dtype=np.complex128) for i in idx])
+        err = np.abs(np.einsum("bji,bjk->bik", m.conj(), m) - np.eye(d)).max(axis=(1, 2))
+        for i, e in zip(idx, err):
+            flags[i] = bool(e < tol)
+    return flags
+
+
 def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, max_sweep_k=5, itemsize=8,
                 device_fusion=False):
     """Compile an op sequence (with ``None`` marking a renormalisation point)
@@ -315,21 +331,26 @@ def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, 
             continue
         if not seg:
             continue
+        uflags = unitary_flags(seg)
         if mode == "gate":
-            for o in seg:
-                plan.steps.append(DenseStep(list(o.bits), plan.add_matrix(o.matrix)))
+            for o, u in zip(seg, uflags):
+                plan.steps.append(DenseStep(list(o.bits), plan.add_matrix(o.matrix), u))
             continue
         w = max(width, max(len(o.bits) for o in seg))
         if device_fusion:
             base = len(plan.op_matrices)
             plan.op_matrices.extend(np.ascontiguousarray(o.matrix, dtype=np.complex128) for o in seg)
+            sym = fuse_symbolic(seg, w)
             blocks = [Block(b.bits, Recipe(list(b.bits), [(base + i, list(seg[i].bits)) for i in b.ops]), b.n_ops)
-                      for b in fuse_symbolic(seg, w)]
+                      for b in sym]
+            bflags = [all(uflags[i] for i in b.ops) for b in sym]
         else:
             blocks = fuse(seg, w)
+            bflags = [bool(np.abs(b.matrix.conj().T @ b.matrix - np.eye(b.matrix.shape[0])).max() < 1e-6)
+                      for b in blocks]
         if mode == "fused" or w > max_sweep_k or tile_bits <= 0:
-            for b in blocks:
-                plan.steps.append(DenseStep(list(b.bits), plan.add_matrix(b.matrix)))
+            for b, u in zip(blocks, bflags):
+                plan.steps.append(DenseStep(list(b.bits), plan.add_matrix(b.matrix), u))
             continue
         for L, high, taken in plan_sweeps(blocks, nbits, tile_bits, low_bits):
             tpos = {b: b for b in range(L)}

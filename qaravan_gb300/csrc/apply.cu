@@ -234,7 +234,8 @@ namespace qgb_host {
 // Applies a dense 2^k x 2^k op whose input bit j is in_bits[j] and output bit
 // j is out_bits[j] (same set of bits) to `batch` vectors of 2^nbits entries.
 int apply_dense_bits(void* sv, int dtype, int nbits, const int* in_bits, const int* out_bits, int k,
-                     const void* op, int64_t op_stride, int64_t batch, int64_t sv_stride, cudaStream_t st) {
+                     const void* op, int64_t op_stride, int64_t batch, int64_t sv_stride, cudaStream_t st,
+                     int unitary = 0) {
     if (!sv || !op) return set_error(QGB_EINVAL, "null state or operator pointer");
     if (dtype != QGB_C64 && dtype != QGB_C128) return set_error(QGB_EINVAL, "dtype %d unknown", dtype);
     if (k < 1 || k > QGB_MAX_K) return set_error(QGB_EINVAL, "gate width k=%d not in [1, %d]", k, QGB_MAX_K);
@@ -274,7 +275,8 @@ int apply_dense_bits(void* sv, int dtype, int nbits, const int* in_bits, const i
     a.sv_stride = sv_stride;
     a.groups = uint64_t(1) << (nbits - k);
     if (dtype == QGB_C64) {
-        const int rc = try_dense_tc(sv, op, nbits, a.sorted, in_bits, out_bits, k, op_stride, batch, sv_stride, st);
+        const int rc =
+            try_dense_tc(sv, op, nbits, a.sorted, in_bits, out_bits, k, op_stride, batch, sv_stride, unitary, st);
         if (rc != QGB_EDECLINE) return rc;
     }
     return dtype == QGB_C64 ? dispatch_dense<float>(sv, op, a, st) : dispatch_dense<double>(sv, op, a, st);
@@ -282,8 +284,10 @@ int apply_dense_bits(void* sv, int dtype, int nbits, const int* in_bits, const i
 
 }  // namespace qgb_host
 
-extern "C" int qgb_op_action(void* sv, int dtype, int n, const int* indices, int k, const void* op,
-                             int64_t op_stride, int64_t batch, int64_t sv_stride, void* stream) {
+namespace {
+
+int op_action(void* sv, int dtype, int n, const int* indices, int k, const void* op, int64_t op_stride,
+              int64_t batch, int64_t sv_stride, void* stream, int unitary) {
     if (n < 1 || n > QGB_MAX_QUBITS) return set_error(QGB_EINVAL, "n=%d not in [1, %d]", n, QGB_MAX_QUBITS);
     if (!indices) return set_error(QGB_EINVAL, "null indices");
     if (k < 1 || k > QGB_MAX_K) return set_error(QGB_EINVAL, "gate width k=%d not in [1, %d]", k, QGB_MAX_K);
@@ -292,7 +296,20 @@ extern "C" int qgb_op_action(void* sv, int dtype, int n, const int* indices, int
         if (indices[j] < 0 || indices[j] >= n) return set_error(QGB_EINVAL, "site %d out of range for n=%d", indices[j], n);
         bits[j] = n - 1 - indices[j];
     }
-    return apply_dense_bits(sv, dtype, n, bits, bits, k, op, op_stride, batch, sv_stride, (cudaStream_t)stream);
+    return apply_dense_bits(sv, dtype, n, bits, bits, k, op, op_stride, batch, sv_stride, (cudaStream_t)stream,
+                            unitary);
+}
+
+}  // namespace
+
+extern "C" int qgb_op_action(void* sv, int dtype, int n, const int* indices, int k, const void* op,
+                             int64_t op_stride, int64_t batch, int64_t sv_stride, void* stream) {
+    return op_action(sv, dtype, n, indices, k, op, op_stride, batch, sv_stride, stream, 0);
+}
+
+extern "C" int qgb_op_action_unitary(void* sv, int dtype, int n, const int* indices, int k, const void* op,
+                                     int64_t op_stride, int64_t batch, int64_t sv_stride, void* stream) {
+    return op_action(sv, dtype, n, indices, k, op, op_stride, batch, sv_stride, stream, 1);
 }
 
 extern "C" int qgb_dm_apply_superop(void* rho, int dtype, int n, const int* indices, int k, const void* superop,

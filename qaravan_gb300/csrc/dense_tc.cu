@@ -161,6 +161,51 @@ __device__ __forceinline__ bool data_bar_any(bool v) {
     return r != 0;
 }
 
+// AND of v over the 64 threads of warps q and q + 4 (named barrier 1 + q).
+__device__ __forceinline__ bool pair_all(int q, bool v) {
+    uint32_t r;
+    asm volatile("{ .reg .pred p, q; setp.ne.u32 p, %1, 0; bar.red.and.pred q, %2, 64, p; selp.u32 %0, 1, 0, q; }"
+                 : "=r"(r)
+                 : "r"(uint32_t(v)), "r"(1 + q)
+                 : "memory");
+    return r != 0;
+}
+
+// Packed pairs of fp32 (one 64-bit register, Blackwell's f32x2 arithmetic).
+__device__ __forceinline__ unsigned long long f2pack(float a, float b) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void f2unpack(unsigned long long v, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long f2fma(unsigned long long a, unsigned long long b, unsigned long long c) {
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+__device__ __forceinline__ unsigned long long f2mul(unsigned long long a, unsigned long long b) {
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+
+// Sum of squares of N floats (N a multiple of 8) with 8 interleaved partial
+// sums (shallower rounding-error growth than one running sum), two per f32x2.
+template <int N> __device__ __forceinline__ float sumsq8(const float* x) {
+    unsigned long long acc[4] = {0ull, 0ull, 0ull, 0ull};
+#pragma unroll
+    for (int i = 0; i < N / 2; ++i) {
+        const unsigned long long v = f2pack(x[2 * i], x[2 * i + 1]);
+        acc[i & 3] = f2fma(v, v, acc[i & 3]);
+    }
+    float s[8];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) f2unpack(acc[j], s[2 * j], s[2 * j + 1]);
+    return ((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7]));
+}
+
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
@@ -235,7 +280,8 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
                  : "memory");
 }
 
-template <int K>
+// UNIT: the op is unitary; each group's norm is restored after the product.
+template <int K, bool UNIT>
 __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restrict__ sv, const float2* __restrict__ op,
                                                                  const __grid_constant__ TcArgs a) {
     using G = TcGeom<K>;
@@ -250,7 +296,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
     __shared__ __align__(8) uint64_t mma_done[2];  // MMA warp -> data warps: accumulator of pair p complete
     __shared__ uint32_t tmem_slot;
     __shared__ uint32_t wmax_bits;
-    __shared__ int row_exp[NB][2][128];  // per block, thread half and row: that half's scale exponent
+    __shared__ int row_exp[NB][2][128];    // per block, thread half and row: that half's scale exponent
+    __shared__ float row_in[NB][2][128];   // ... that half's squared input norm (unitary ops)
+    __shared__ float row_out[NB][2][128];  // ... that half's squared output norm (unitary ops)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int q = warp & 3, h = (warp >> 2) & 1;
 
@@ -364,8 +412,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
         };
         using Scl = float[NB];
         // Reads this thread's half rows of the tile staged in buffer pb, scales,
-        // splits and stages them into X of pair pb; records 2^-s per block.
-        auto store_x = [&](int pb, Scl& unscale) {
+        // splits and stages them into X of pair pb; records 2^-s per block and,
+        // for a unitary op, the row's squared norm.
+        auto store_x = [&](int pb, Scl& unscale, Scl& nin) {
             const float2* T = reinterpret_cast<const float2*>(tiles_smem + pb * G::TILE_BYTES);
             float2 v[NB][H];
 #pragma unroll
@@ -385,19 +434,26 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
 #pragma unroll
                 for (int j = 0; j < H; ++j) m = fmaxf(m, fmaxf(fabsf(v[bk][j].x), fabsf(v[bk][j].y)));
                 row_exp[bk][h][32 * q + lane] = scale_exp(m);
+                if constexpr (UNIT) row_in[bk][h][32 * q + lane] = sumsq8<2 * H>(reinterpret_cast<const float*>(v[bk]));
             }
             asm volatile("bar.sync %0, 64;" ::"r"(1 + q) : "memory");  // warps q and q + 4 share these rows
 #pragma unroll
             for (int bk = 0; bk < NB; ++bk) {
+                if constexpr (UNIT) nin[bk] = row_in[bk][0][32 * q + lane] + row_in[bk][1][32 * q + lane];
                 const int e0 = row_exp[bk][0][32 * q + lane], e1 = row_exp[bk][1][32 * q + lane];
                 const int se = e0 < e1 ? e0 : e1;
                 const float f = exp2i(se);
+                const unsigned long long f2 = f2pack(f, f);
                 unscale[bk] = exp2i(-se);
 #pragma unroll
                 for (int c0 = 0; c0 < H; c0 += 8) {
                     uint32_t hi[8], lo[8];
 #pragma unroll
-                    for (int e = 0; e < 8; ++e) split_f16(v[bk][c0 + e].x * f, v[bk][c0 + e].y * f, hi[e], lo[e]);
+                    for (int e = 0; e < 8; ++e) {
+                        float xs, ys;
+                        f2unpack(f2mul(f2pack(v[bk][c0 + e].x, v[bk][c0 + e].y), f2), xs, ys);
+                        split_f16(xs, ys, hi[e], lo[e]);
+                    }
                     const uint32_t col = uint32_t(bk * BC + pb * R + h * H + c0);
                     tmem_st8(row + col, hi);
                     tmem_st8(row + col + R / 2, lo);
@@ -405,47 +461,104 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
             }
             asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
         };
-        auto drain = [&](uint64_t t, int pb, const Scl& unscale) {
+        // Stores one 16-column chunk (8 components) of this thread's result row.
+        auto put16 = [&](float2* p, int c0, const float* r) {
+            if (a.vec4) {
+                // Rows are runs of >= 4 contiguous components: pass the 32 rows x 8
+                // components through this warp's staging area so that 4 lanes write
+                // one row's 64 contiguous bytes (whole sectors) and 8 rows go per store.
+                // 16-byte pieces are XOR-swizzled by (row / 2) % 4 against bank conflicts.
+                float4* st4 = reinterpret_cast<float4*>(stage_smem + warp * 2048);
+#pragma unroll
+                for (int m = 0; m < 4; ++m)
+                    st4[lane * 4 + (m ^ ((lane >> 1) & 3))] = make_float4(r[4 * m], r[4 * m + 1], r[4 * m + 2], r[4 * m + 3]);
+                __syncwarp();
+                const int pc = lane & 3;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int rho = 8 * i + (lane >> 2);
+                    const float4 x = st4[rho * 4 + (pc ^ ((rho >> 1) & 3))];
+                    float2* pr = reinterpret_cast<float2*>(
+                        __shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(p), rho));
+                    *reinterpret_cast<float4*>(pr + a.off[c0 / 2 + 2 * pc]) = x;
+                }
+                __syncwarp();
+            } else if (a.vec2) {
+#pragma unroll
+                for (int m = 0; m < 4; ++m)
+                    *reinterpret_cast<float4*>(p + a.off[c0 / 2 + 2 * m]) =
+                        make_float4(r[4 * m], r[4 * m + 1], r[4 * m + 2], r[4 * m + 3]);
+            } else {
+#pragma unroll
+                for (int e = 0; e < 8; ++e) p[a.off[c0 / 2 + e]] = make_float2(r[2 * e], r[2 * e + 1]);
+            }
+        };
+        auto drain = [&](uint64_t t, int pb, const Scl& unscale, const Scl& nin) {
             float2* base = tile_base(t);
+            if constexpr (UNIT) {
+                // The op preserves each group's norm: rescale every row to its input norm,
+                // which removes the tensor cores' round-toward-zero shrinkage. All blocks'
+                // rows are loaded first (NB * D = 64 floats in every case) so that one pair
+                // barrier exchanges every block's half-row norms.
+                float y[NB][D];
 #pragma unroll
-            for (int bk = 0; bk < NB; ++bk) {
-                float2* p = base + gg[bk];
-                const float u = unscale[bk];
+                for (int bk = 0; bk < NB; ++bk) {
+                    const uint32_t acc = row + uint32_t(bk * BC + 2 * R + pb * R + h * D);
 #pragma unroll
-                for (int c0 = 0; c0 < D; c0 += 16) {
-                    float r[16];
-                    tmem_ld16(row + uint32_t(bk * BC + 2 * R + pb * R + h * D + c0), r);
+                    for (int c0 = 0; c0 < D; c0 += 16) tmem_ld16(acc + uint32_t(c0), y[bk] + c0);
+                    row_out[bk][h][32 * q + lane] = sumsq8<D>(y[bk]);  // in accumulator units
+                }
+                asm volatile("bar.sync %0, 64;" ::"r"(1 + q) : "memory");
 #pragma unroll
-                    for (int e = 0; e < 16; ++e) r[e] = (r[e] * wunscale) * u;  // two factors: each stays in range
-                    if (a.vec4) {
-                        // Rows are runs of >= 4 contiguous components: pass the 32 rows x 8
-                        // components through this warp's staging area so that 4 lanes write
-                        // one row's 64 contiguous bytes (whole sectors) and 8 rows go per store.
-                        // 16-byte pieces are XOR-swizzled by (row / 2) % 4 against bank conflicts.
-                        float4* st4 = reinterpret_cast<float4*>(stage_smem + warp * 2048);
+                for (int bk = 0; bk < NB; ++bk) {
+                    const float u = unscale[bk];
+                    // the accumulator is 2^(s + sw) times the result: one multiply by su when
+                    // that power of two is a normal float, else the two factors in turn
+                    const float su = u * wunscale;
+                    const bool one = su >= 1.17549435e-38f && su <= 1.0e38f;
+                    const float nraw = row_out[bk][0][32 * q + lane] + row_out[bk][1][32 * q + lane];
+                    // g = sqrt(nin / nout) - 1 to first order (|g| ~ 1e-7, the next term ~ g^2);
+                    // y = acc su (1 + g) = fma(acc, su g, acc su): the factor 1 + g itself is
+                    // within an ulp of 1, where fp32 cannot resolve it
+                    const float nout = one ? (nraw * su) * su : 0.f;
+                    const float g = nout > 0.f ? (nin[bk] - nout) / (2.f * nout) : 0.f;
+                    if (one) {
+                        const float cg = su * g;
+                        const unsigned long long cg2 = f2pack(cg, cg), su2 = f2pack(su, su);
 #pragma unroll
-                        for (int m = 0; m < 4; ++m)
-                            st4[lane * 4 + (m ^ ((lane >> 1) & 3))] =
-                                make_float4(r[4 * m], r[4 * m + 1], r[4 * m + 2], r[4 * m + 3]);
-                        __syncwarp();
-                        const int pc = lane & 3;
-#pragma unroll
-                        for (int i = 0; i < 4; ++i) {
-                            const int rho = 8 * i + (lane >> 2);
-                            const float4 x = st4[rho * 4 + (pc ^ ((rho >> 1) & 3))];
-                            float2* pr = reinterpret_cast<float2*>(
-                                __shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(p), rho));
-                            *reinterpret_cast<float4*>(pr + a.off[c0 / 2 + 2 * pc]) = x;
+                        for (int e = 0; e < D; e += 2) {
+                            const unsigned long long v = f2pack(y[bk][e], y[bk][e + 1]);
+                            f2unpack(f2fma(v, cg2, f2mul(v, su2)), y[bk][e], y[bk][e + 1]);
                         }
-                        __syncwarp();
-                    } else if (a.vec2) {
-#pragma unroll
-                        for (int m = 0; m < 4; ++m)
-                            *reinterpret_cast<float4*>(p + a.off[c0 / 2 + 2 * m]) =
-                                make_float4(r[4 * m], r[4 * m + 1], r[4 * m + 2], r[4 * m + 3]);
                     } else {
 #pragma unroll
-                        for (int e = 0; e < 8; ++e) p[a.off[c0 / 2 + e]] = make_float2(r[2 * e], r[2 * e + 1]);
+                        for (int e = 0; e < D; ++e) y[bk][e] = (y[bk][e] * wunscale) * u;
+                    }
+                    float2* p = base + gg[bk];
+#pragma unroll
+                    for (int c0 = 0; c0 < D; c0 += 16) put16(p, c0, y[bk] + c0);
+                }
+            } else {
+#pragma unroll
+                for (int bk = 0; bk < NB; ++bk) {
+                    float2* p = base + gg[bk];
+                    const float u = unscale[bk];
+                    const uint32_t acc = row + uint32_t(bk * BC + 2 * R + pb * R + h * D);
+                    const float su = u * wunscale;
+                    const bool one = su >= 1.17549435e-38f && su <= 1.0e38f;
+#pragma unroll
+                    for (int c0 = 0; c0 < D; c0 += 16) {
+                        float r[16];
+                        tmem_ld16(acc + uint32_t(c0), r);
+                        if (one) {
+                            const unsigned long long su2 = f2pack(su, su);
+#pragma unroll
+                            for (int e = 0; e < 16; e += 2) f2unpack(f2mul(f2pack(r[e], r[e + 1]), su2), r[e], r[e + 1]);
+                        } else {
+#pragma unroll
+                            for (int e = 0; e < 16; ++e) r[e] = (r[e] * wunscale) * u;
+                        }
+                        put16(p, c0, r);
                     }
                 }
             }
@@ -459,12 +572,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
         if (ntiles > 1) issue_load(t0 + step, 1);
         cp_async_commit();
         bool fail = false;
-        Scl sA, sB;
-        auto stage = [&](uint64_t k, Scl& sc, Scl& scp, int pc) -> bool {
+        Scl sA, sB, nA, nB;
+        auto stage = [&](uint64_t k, Scl& sc, Scl& scp, Scl& nc, Scl& ncp, int pc) -> bool {
             const int pn = pc ^ 1;
             cp_async_wait1();                    // this thread's copies of tile k have landed
             if (data_bar_any(fail)) return false;  // ... and everyone's; a failure seen by any thread stops all
-            store_x(pc, sc);
+            store_x(pc, sc, nc);
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(tc_smem_u32(&x_full[pc]));
@@ -472,27 +585,29 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
             if (k + 2 < ntiles) issue_load(t0 + (k + 2) * step, pc);
             cp_async_commit();
             if (k >= 1) {
-                if (!tc_wait_bounded(tc_smem_u32(&mma_done[pn]), uint32_t(((k - 1) >> 1) & 1))) {
+                // both warps sharing these rows take the same branch (the drain has a pair barrier)
+                const bool ok = pair_all(q, tc_wait_bounded(tc_smem_u32(&mma_done[pn]), uint32_t(((k - 1) >> 1) & 1)));
+                if (!ok) {
                     fail = true;
                     if (tid == 0) atomicExch(&g_tc_status, 2);
                 } else {
                     tc_fence_after();
-                    drain(t0 + (k - 1) * step, pn, scp);
+                    drain(t0 + (k - 1) * step, pn, scp, ncp);
                 }
             }
             return true;
         };
         bool live = true;
         for (uint64_t k = 0; live && k < ntiles; k += 2) {
-            live = stage(k, sA, sB, 0);
-            if (live && k + 1 < ntiles) live = stage(k + 1, sB, sA, 1);
+            live = stage(k, sA, sB, nA, nB, 0);
+            if (live && k + 1 < ntiles) live = stage(k + 1, sB, sA, nB, nA, 1);
         }
         if (live && !fail) {
             const uint64_t k = ntiles - 1;
             const int pl = int(k & 1);
-            if (tc_wait_bounded(tc_smem_u32(&mma_done[pl]), uint32_t((k >> 1) & 1))) {
+            if (pair_all(q, tc_wait_bounded(tc_smem_u32(&mma_done[pl]), uint32_t((k >> 1) & 1)))) {
                 tc_fence_after();
-                drain(t0 + k * step, pl, pl ? sB : sA);
+                drain(t0 + k * step, pl, pl ? sB : sA, pl ? nB : nA);
             } else if (tid == 0) {
                 atomicExch(&g_tc_status, 2);
             }
@@ -525,23 +640,24 @@ int dense_impl() {
     return g_dense_impl;
 }
 
-template <int K>
+template <int K, bool UNIT>
 int launch_tc(float2* sv, const float2* op, const TcArgs& a, cudaStream_t st) {
     using G = TcGeom<K>;
     static int per_sm = 0;
     if (per_sm == 0) {
-        if (cudaFuncSetAttribute(dense_tc_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(G::SMEM)) !=
-            cudaSuccess)
+        if (cudaFuncSetAttribute(dense_tc_kernel<K, UNIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 int(G::SMEM)) != cudaSuccess)
             return qgb_host::check_launch("dense_tc attribute");
         int occ = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dense_tc_kernel<K>, kTcThreads, G::SMEM) != cudaSuccess)
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dense_tc_kernel<K, UNIT>, kTcThreads, G::SMEM) !=
+            cudaSuccess)
             return qgb_host::check_launch("dense_tc occupancy");
         per_sm = occ < 1 ? occ : 1;  // each CTA holds all 512 TMEM columns
         if (per_sm < 1) return qgb_host::set_error(QGB_ECUDA, "dense_tc kernel does not fit on an SM");
     }
     const uint64_t cap = uint64_t(qgb_host::sm_count()) * uint64_t(per_sm);
     const unsigned grid = unsigned(a.tiles < cap ? a.tiles : cap);
-    dense_tc_kernel<K><<<grid, kTcThreads, G::SMEM, st>>>(sv, op, a);
+    dense_tc_kernel<K, UNIT><<<grid, kTcThreads, G::SMEM, st>>>(sv, op, a);
     return qgb_host::check_launch("dense_tc kernel");
 }
 
@@ -569,7 +685,7 @@ int set_dense_impl(int mode) {
 // nothing) when the op is not one it takes, so that the caller runs the
 // CUDA-core kernel instead.
 int try_dense_tc(void* sv, const void* op, int nbits, const int* sorted, const int* in_bits, const int* out_bits,
-                 int k, int64_t op_stride, int64_t batch, int64_t sv_stride, cudaStream_t st) {
+                 int k, int64_t op_stride, int64_t batch, int64_t sv_stride, int unitary, cudaStream_t st) {
     const int mode = dense_impl();
     if (mode == 0 || k < 4 || k > 6 || (k == 4 && mode < 2)) return QGB_EDECLINE;
     if (nbits < 13) return QGB_EDECLINE;              // fewer than one 8192-amplitude tile
@@ -643,9 +759,9 @@ int try_dense_tc(void* sv, const void* op, int nbits, const int* sorted, const i
     float2* s = static_cast<float2*>(sv);
     const float2* m = static_cast<const float2*>(op);
     switch (k) {
-        case 4: return launch_tc<4>(s, m, a, st);
-        case 5: return launch_tc<5>(s, m, a, st);
-        default: return launch_tc<6>(s, m, a, st);
+        case 4: return unitary ? launch_tc<4, true>(s, m, a, st) : launch_tc<4, false>(s, m, a, st);
+        case 5: return unitary ? launch_tc<5, true>(s, m, a, st) : launch_tc<5, false>(s, m, a, st);
+        default: return unitary ? launch_tc<6, true>(s, m, a, st) : launch_tc<6, false>(s, m, a, st);
     }
 }
 

@@ -13,12 +13,26 @@ captured in a CUDA graph.
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 import torch
 
 from . import _lib
 from .compiler import DenseStep, NormalizeStep, Plan, Recipe, SweepStep
+
+# Unitary fused blocks go through qgb_op_action_unitary, whose tensor-core path
+# restores each amplitude group's norm (removing the round-toward-zero shrinkage
+# of tensor-core accumulation, ~1e-7 of the norm per pass) at ~10 % of the
+# kernel's speed; QGB_NORM_RESTORE=0 or set_norm_restore(False) skips it.
+_NORM_RESTORE = os.environ.get("QGB_NORM_RESTORE", "1") != "0"
+
+
+def set_norm_restore(flag: bool):
+    """Process-wide: restore group norms on unitary tensor-core blocks (default True)."""
+    global _NORM_RESTORE
+    _NORM_RESTORE = bool(flag)
+
 
 _FUSE_BLOCK = np.dtype([("out", "<i8"), ("k", "<i4"), ("op_begin", "<i4"), ("op_end", "<i4"), ("pad", "<i4")])
 _FUSE_ENTRY = np.dtype([("k", "<i4"), ("pos", "<i4", (6,)), ("pad", "<i4"), ("mat", "<i8")])
@@ -71,7 +85,7 @@ class Executor:
             if isinstance(s, DenseStep):
                 nb = plan.nbits
                 sites = [nb - 1 - b for b in s.bits]
-                self._steps.append(("dense", _lib.int_array(sites), len(sites), offs[s.mat]))
+                self._steps.append(("dense", _lib.int_array(sites), len(sites), offs[s.mat], s.unitary))
             elif isinstance(s, SweepStep):
                 sw = _lib.Sweep()
                 sw.low_bits = s.low_bits
@@ -171,13 +185,11 @@ class Executor:
                 e0 = torch.cuda.Event(enable_timing=True)
                 e0.record()
             if s[0] == "dense":
-                _, sites, k, off = s
-                if mat_stride:
-                    _lib.check(L.qgb_op_action(ptr, self.code, nb, sites, k, mptr + off * self.itemsize,
-                                               mat_stride, batch, stride, st), "op_action")
-                else:
-                    _lib.check(L.qgb_op_action(ptr, self.code, nb, sites, k, mptr + off * self.itemsize, 0,
-                                               batch, stride, st), "op_action")
+                _, sites, k, off, unitary = s
+                # per-vector matrices (mat_stride) need not be unitary: only the plan's own are flagged
+                fn = L.qgb_op_action_unitary if (unitary and _NORM_RESTORE and mats is self.mats) else L.qgb_op_action
+                _lib.check(fn(ptr, self.code, nb, sites, k, mptr + off * self.itemsize, mat_stride if mat_stride else 0,
+                              batch, stride, st), "op_action")
                 launches += 1
             elif s[0] == "sweep":
                 _lib.check(L.qgb_apply_sweep(ptr, self.code, nb, C.byref(s[1]), mptr, mat_stride, batch, stride, st),
