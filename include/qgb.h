@@ -147,6 +147,34 @@ int qgb_pauli_expectation(const void* sv, int dtype, int n, const char* paulis, 
 int qgb_pauli_expectation_noalloc(const void* sv, int dtype, int n, const char* paulis, const double* coeff,
                                   int nterms, double* out, void* stream);
 
+/* Outcome probabilities of measuring `m` sites (measure_sv,
+ * tensorQ/statevector_sim.py:185-193, whose probabilities are the diagonal of
+ * rdm_from_sv, :182-183): probs[b] = sum over the other sites of |psi|^2, with
+ * sites[0] the most significant bit of b (the reference orders the sites
+ * ascending: pass them sorted for its outcome strings). float64, device,
+ * 2^m entries, m <= 30, bitwise reproducible. Scratch:
+ * qgb_probs_scratch_bytes(n, m) bytes (0 when m is within 5 of n). */
+size_t qgb_probs_scratch_bytes(int n, int m);
+int qgb_outcome_probs(const void* sv, int dtype, int n, const int* sites, int m, double* probs, void* scratch,
+                      size_t scratch_bytes, void* stream);
+
+/* Draws `shots` outcomes (int64 indices into probs, device) from the 2^m
+ * probabilities (m <= 28, need not be normalised): float64 prefix sums and a
+ * binary search per shot on a Philox4x32-10 uniform, counter (shot, 0, 1) under
+ * key `seed` -- the same seed gives the same shots. Replaces the
+ * numpy.random.choice call of measure_sv (:189-193). Scratch:
+ * qgb_sample_scratch_bytes(m). */
+size_t qgb_sample_scratch_bytes(int m);
+int qgb_sample_outcomes(const double* probs, int m, int64_t shots, uint64_t seed, int64_t* out, void* scratch,
+                        size_t scratch_bytes, void* stream);
+
+/* Post-measurement state (measure_and_collapse_sv, :195-215): out (2^(n-m)
+ * entries, the unmeasured sites in their order) = psi restricted to the
+ * measured bits `outcome` (sites[0] its most significant bit), divided by
+ * sqrt(probs[outcome]) read on the device. */
+int qgb_collapse(const void* sv, int dtype, int n, const int* sites, int m, uint64_t outcome, const double* probs,
+                 void* out, void* stream);
+
 /* <a_b|b_b> = sum conj(a) b for every state b: out[2b], out[2b+1] = real,
  * imaginary part (float64). With b = (x)_q O_q a it gives
  * StatevectorSim.local_expectation / one_local_expectation (:63-73, :81-94). */
