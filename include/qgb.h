@@ -147,6 +147,14 @@ int qgb_pauli_expectation(const void* sv, int dtype, int n, const char* paulis, 
 int qgb_pauli_expectation_noalloc(const void* sv, int dtype, int n, const char* paulis, const double* coeff,
                                   int nterms, double* out, void* stream);
 
+/* Applies one Pauli string per state in place (the sampled noise layers of
+ * MonteCarloSim, tensorQ/monte_carlo_sim.py:14-28, which the reference turns
+ * into X/Y/Z gates): state b gets i^ny[b] X^xmask[b] Z^zmask[b], flat-bit
+ * masks (site q = bit n-1-q, a Y site in both masks). Masks and counts are
+ * device arrays of `batch` entries. */
+int qgb_pauli_layer(void* sv, int dtype, int n, const uint64_t* xmask, const uint64_t* zmask, const int* ny,
+                    int64_t batch, int64_t sv_stride, void* stream);
+
 /* Outcome probabilities of measuring `m` sites (measure_sv,
  * tensorQ/statevector_sim.py:185-193, whose probabilities are the diagonal of
  * rdm_from_sv, :182-183): probs[b] = sum over the other sites of |psi|^2, with

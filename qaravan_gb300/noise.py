@@ -86,6 +86,14 @@ class PauliNoise(Noise):
     def get_kraus(self, *args, **kwargs):
         return [np.emath.sqrt(p) * _embed_dense(s) for p, s in zip(self.probs, self.strings)]
 
+    def pinv(self):
+        """The inverse channel as a (quasi-probability) Pauli channel: fidelities
+        inverted and mapped back through the full symplectic matrix
+        (``core/noise.py:131-135``)."""
+        inv_fid = 1 / np.diag(self.ptm())
+        inv_probs = np.linalg.inv(self.symp_matrix(full=True)) @ inv_fid
+        return PauliNoise(pauli_strings(self.num_sites), inv_probs)
+
     def compose(self, other):
         acc = {}
         for s1, p1 in zip(self.strings, self.probs):
@@ -123,6 +131,26 @@ class PauliLindbladNoise(Noise):
 
     def get_kraus(self, *args, **kwargs):
         raise NotImplementedError("PauliLindbladNoise is defined by its superoperator")
+
+    def sample_string(self, rng=None):
+        """Each generator fires independently with its rate; the fired strings
+        multiply (phases dropped) (``core/noise.py:194-200``)."""
+        rng = np.random.default_rng() if rng is None else rng
+        flags = [rng.random() < r for r in self.rates]
+        out = 'i' * self.num_sites
+        for s, f in zip(self.strings, flags):
+            if f:
+                out, _ = pauli_multiply(out, s)
+        return out
+
+    def sample(self, rng=None):
+        return pauli_string_to_gates(self.sample_string(rng))
+
+    def inv_sample(self, rng=None):
+        """A layer of the inverse channel and its quasi-probability prefactor
+        gamma * (-1)^(layer non-empty) (``core/noise.py:206-210``)."""
+        layer = self.sample(rng)
+        return layer, self.gamma * (-1) ** (len(layer) != 0)
 
 
 def depolarizing(p):
