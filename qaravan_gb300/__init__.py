@@ -1,8 +1,10 @@
 """qaravan_gb300 -- GB300 (sm_103a) engine for qaravan's tensorQ gate-application path.
 
 Drop-in for the reference's torch backend: ``StatevectorSim``,
-``DensityMatrixSim``, ``TrajectorySim`` (noisy trajectories), the adjoint
-gradient, and the reference's circuit / gate / noise objects (which work
+``DensityMatrixSim``, ``MonteCarloSim`` / ``trotter_mc_sim`` (sampled Pauli
+noise), ``TrajectorySim`` (depolarising + amplitude-damping trajectories),
+measurement and sampling, the adjoint gradient, and the reference's circuit /
+gate / noise objects (which work
 unchanged when the reference package itself is installed). All arithmetic
 runs in the hand-written CUDA kernels of ``libqgb.so`` (C ABI in
 ``include/qgb.h``); there is no CPU path.
@@ -13,7 +15,8 @@ from .density_matrix import DensityMatrixSim
 from .gates import (CNOT, CZ, H, ID, RX, RY, RZ, RXX, RYY, RZZ, SDG, SWAP, SX, U, X, Y, Z, Gate, Reset,
                     iSWAP, kak_unitary)
 from .hamiltonians import TFI
-from .noise import AmplitudeDamping, PauliNoise, QubitNoise, amplitude_damping, depolarizing
+from .montecarlo import MonteCarloSim, trotter_mc_sim
+from .noise import AmplitudeDamping, PauliLindbladNoise, PauliNoise, QubitNoise, amplitude_damping, depolarizing
 from .statevector import StatevectorSim
 
 __version__ = "0.1.0"
