@@ -44,6 +44,8 @@
 //     block); warp w+4h reads, scales, splits and stages components
 //     [h*D/2, (h+1)*D/2) of its groups, and later drains the same half of the
 //     result rows straight to HBM;
+//   * unitary ops (UNIT): each group row is rescaled to its input norm after the
+//     product, in two phases around the pipeline's CTA-wide barriers;
 //   * the MMA warp waits on an mbarrier that the 8 data warps arrive at once a
 //     tile's X rows are staged, issues the 3 * (2D/16) MMAs per block
 //     (M = 128, N = 2D, K = 16) and commits them to a second mbarrier, which the
@@ -157,16 +159,6 @@ __device__ __forceinline__ bool data_bar_any(bool v) {
     asm volatile("{ .reg .pred p, q; setp.ne.u32 p, %1, 0; bar.red.or.pred q, 5, 256, p; selp.u32 %0, 1, 0, q; }"
                  : "=r"(r)
                  : "r"(uint32_t(v))
-                 : "memory");
-    return r != 0;
-}
-
-// AND of v over the 64 threads of warps q and q + 4 (named barrier 1 + q).
-__device__ __forceinline__ bool pair_all(int q, bool v) {
-    uint32_t r;
-    asm volatile("{ .reg .pred p, q; setp.ne.u32 p, %1, 0; bar.red.and.pred q, %2, 64, p; selp.u32 %0, 1, 0, q; }"
-                 : "=r"(r)
-                 : "r"(uint32_t(v)), "r"(1 + q)
                  : "memory");
     return r != 0;
 }
@@ -298,7 +290,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
     __shared__ uint32_t wmax_bits;
     __shared__ int row_exp[NB][2][128];    // per block, thread half and row: that half's scale exponent
     __shared__ float row_in[NB][2][128];   // ... that half's squared input norm (unitary ops)
-    __shared__ float row_out[NB][2][128];  // ... that half's squared output norm (unitary ops)
+    __shared__ float row_out[2][NB][2][128];  // per buffer pair: that half's squared output norm (unitary ops)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int q = warp & 3, h = (warp >> 2) & 1;
 
@@ -493,73 +485,82 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
                 for (int e = 0; e < 8; ++e) p[a.off[c0 / 2 + e]] = make_float2(r[2 * e], r[2 * e + 1]);
             }
         };
-        auto drain = [&](uint64_t t, int pb, const Scl& unscale, const Scl& nin) {
+        // Non-unitary ops: the accumulator streams to HBM chunk by chunk.
+        auto drain = [&](uint64_t t, int pb, const Scl& unscale) {
             float2* base = tile_base(t);
-            if constexpr (UNIT) {
-                // The op preserves each group's norm: rescale every row to its input norm,
-                // which removes the tensor cores' round-toward-zero shrinkage. All blocks'
-                // rows are loaded first (NB * D = 64 floats in every case) so that one pair
-                // barrier exchanges every block's half-row norms.
-                float y[NB][D];
 #pragma unroll
-                for (int bk = 0; bk < NB; ++bk) {
-                    const uint32_t acc = row + uint32_t(bk * BC + 2 * R + pb * R + h * D);
+            for (int bk = 0; bk < NB; ++bk) {
+                float2* p = base + gg[bk];
+                const float u = unscale[bk];
+                const uint32_t acc = row + uint32_t(bk * BC + 2 * R + pb * R + h * D);
+                // the accumulator is 2^(s + sw) times the result: one multiply by su when that
+                // power of two is a normal float, else the two factors in turn
+                const float su = u * wunscale;
+                const bool one = su >= 1.17549435e-38f && su <= 1.0e38f;
 #pragma unroll
-                    for (int c0 = 0; c0 < D; c0 += 16) tmem_ld16(acc + uint32_t(c0), y[bk] + c0);
-                    row_out[bk][h][32 * q + lane] = sumsq8<D>(y[bk]);  // in accumulator units
-                }
-                asm volatile("bar.sync %0, 64;" ::"r"(1 + q) : "memory");
-#pragma unroll
-                for (int bk = 0; bk < NB; ++bk) {
-                    const float u = unscale[bk];
-                    // the accumulator is 2^(s + sw) times the result: one multiply by su when
-                    // that power of two is a normal float, else the two factors in turn
-                    const float su = u * wunscale;
-                    const bool one = su >= 1.17549435e-38f && su <= 1.0e38f;
-                    const float nraw = row_out[bk][0][32 * q + lane] + row_out[bk][1][32 * q + lane];
-                    // g = sqrt(nin / nout) - 1 to first order (|g| ~ 1e-7, the next term ~ g^2);
-                    // y = acc su (1 + g) = fma(acc, su g, acc su): the factor 1 + g itself is
-                    // within an ulp of 1, where fp32 cannot resolve it
-                    const float nout = one ? (nraw * su) * su : 0.f;
-                    const float g = nout > 0.f ? (nin[bk] - nout) / (2.f * nout) : 0.f;
+                for (int c0 = 0; c0 < D; c0 += 16) {
+                    float r[16];
+                    tmem_ld16(acc + uint32_t(c0), r);
                     if (one) {
-                        const float cg = su * g;
-                        const unsigned long long cg2 = f2pack(cg, cg), su2 = f2pack(su, su);
+                        const unsigned long long su2 = f2pack(su, su);
 #pragma unroll
-                        for (int e = 0; e < D; e += 2) {
-                            const unsigned long long v = f2pack(y[bk][e], y[bk][e + 1]);
-                            f2unpack(f2fma(v, cg2, f2mul(v, su2)), y[bk][e], y[bk][e + 1]);
+                        for (int e = 0; e < 16; e += 2) f2unpack(f2mul(f2pack(r[e], r[e + 1]), su2), r[e], r[e + 1]);
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < 16; ++e) r[e] = (r[e] * wunscale) * u;
+                    }
+                    put16(p, c0, r);
+                }
+            }
+        };
+        // Unitary ops, in two phases so that the two warps sharing a row meet at a
+        // barrier the pipeline has anyway: (A) once the tile's MMAs are complete,
+        // publish each half-row's squared norm (accumulator units); (B) after the
+        // next CTA-wide barrier, reload the accumulator and store every row rescaled
+        // to its input norm -- which removes the tensor cores' round-toward-zero
+        // shrinkage. The accumulator stays valid until the MMAs of the tile after
+        // next, which wait for phase B.
+        auto drain_norms = [&](int pb) {
+#pragma unroll
+            for (int bk = 0; bk < NB; ++bk) {
+                const uint32_t acc = row + uint32_t(bk * BC + 2 * R + pb * R + h * D);
+                float y[D];
+#pragma unroll
+                for (int c0 = 0; c0 < D; c0 += 16) tmem_ld16(acc + uint32_t(c0), y + c0);
+                row_out[pb][bk][h][32 * q + lane] = sumsq8<D>(y);
+            }
+        };
+        auto drain_rescaled = [&](uint64_t t, int pb, const Scl& unscale, const Scl& nin) {
+            float2* base = tile_base(t);
+#pragma unroll
+            for (int bk = 0; bk < NB; ++bk) {
+                float2* p = base + gg[bk];
+                const float u = unscale[bk];
+                const uint32_t acc = row + uint32_t(bk * BC + 2 * R + pb * R + h * D);
+                const float su = u * wunscale;
+                const bool one = su >= 1.17549435e-38f && su <= 1.0e38f;
+                const float nraw = row_out[pb][bk][0][32 * q + lane] + row_out[pb][bk][1][32 * q + lane];
+                // g = sqrt(nin / nout) - 1 to first order (|g| ~ 1e-7, the next term ~ g^2);
+                // y = acc su (1 + g) = fma(acc, su g, acc su): the factor 1 + g itself is
+                // within an ulp of 1, where fp32 cannot resolve it
+                const float nout = one ? (nraw * su) * su : 0.f;
+                const float g = nout > 0.f ? (nin[bk] - nout) / (2.f * nout) : 0.f;
+                const unsigned long long cg2 = f2pack(su * g, su * g), su2 = f2pack(su, su);
+#pragma unroll
+                for (int c0 = 0; c0 < D; c0 += 16) {
+                    float r[16];
+                    tmem_ld16(acc + uint32_t(c0), r);
+                    if (one) {
+#pragma unroll
+                        for (int e = 0; e < 16; e += 2) {
+                            const unsigned long long v = f2pack(r[e], r[e + 1]);
+                            f2unpack(f2fma(v, cg2, f2mul(v, su2)), r[e], r[e + 1]);
                         }
                     } else {
 #pragma unroll
-                        for (int e = 0; e < D; ++e) y[bk][e] = (y[bk][e] * wunscale) * u;
+                        for (int e = 0; e < 16; ++e) r[e] = (r[e] * wunscale) * u;
                     }
-                    float2* p = base + gg[bk];
-#pragma unroll
-                    for (int c0 = 0; c0 < D; c0 += 16) put16(p, c0, y[bk] + c0);
-                }
-            } else {
-#pragma unroll
-                for (int bk = 0; bk < NB; ++bk) {
-                    float2* p = base + gg[bk];
-                    const float u = unscale[bk];
-                    const uint32_t acc = row + uint32_t(bk * BC + 2 * R + pb * R + h * D);
-                    const float su = u * wunscale;
-                    const bool one = su >= 1.17549435e-38f && su <= 1.0e38f;
-#pragma unroll
-                    for (int c0 = 0; c0 < D; c0 += 16) {
-                        float r[16];
-                        tmem_ld16(acc + uint32_t(c0), r);
-                        if (one) {
-                            const unsigned long long su2 = f2pack(su, su);
-#pragma unroll
-                            for (int e = 0; e < 16; e += 2) f2unpack(f2mul(f2pack(r[e], r[e + 1]), su2), r[e], r[e + 1]);
-                        } else {
-#pragma unroll
-                            for (int e = 0; e < 16; ++e) r[e] = (r[e] * wunscale) * u;
-                        }
-                        put16(p, c0, r);
-                    }
+                    put16(p, c0, r);
                 }
             }
         };
@@ -577,6 +578,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
             const int pn = pc ^ 1;
             cp_async_wait1();                    // this thread's copies of tile k have landed
             if (data_bar_any(fail)) return false;  // ... and everyone's; a failure seen by any thread stops all
+            if constexpr (UNIT) {
+                // tile k - 2 (pair pc): its norms were published before this barrier; its
+                // accumulator and scales are overwritten only after this point
+                if (k >= 2) {
+                    tc_fence_after();
+                    drain_rescaled(t0 + (k - 2) * step, pc, sc, nc);
+                }
+            }
             store_x(pc, sc, nc);
             tc_fence_before();
             __syncwarp();
@@ -585,14 +594,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
             if (k + 2 < ntiles) issue_load(t0 + (k + 2) * step, pc);
             cp_async_commit();
             if (k >= 1) {
-                // both warps sharing these rows take the same branch (the drain has a pair barrier)
-                const bool ok = pair_all(q, tc_wait_bounded(tc_smem_u32(&mma_done[pn]), uint32_t(((k - 1) >> 1) & 1)));
-                if (!ok) {
+                if (!tc_wait_bounded(tc_smem_u32(&mma_done[pn]), uint32_t(((k - 1) >> 1) & 1))) {
                     fail = true;
                     if (tid == 0) atomicExch(&g_tc_status, 2);
                 } else {
                     tc_fence_after();
-                    drain(t0 + (k - 1) * step, pn, scp, ncp);
+                    if constexpr (UNIT)
+                        drain_norms(pn);
+                    else
+                        drain(t0 + (k - 1) * step, pn, scp);
                 }
             }
             return true;
@@ -602,14 +612,35 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
             live = stage(k, sA, sB, nA, nB, 0);
             if (live && k + 1 < ntiles) live = stage(k + 1, sB, sA, nB, nA, 1);
         }
-        if (live && !fail) {
+        if (live) {
             const uint64_t k = ntiles - 1;
             const int pl = int(k & 1);
-            if (pair_all(q, tc_wait_bounded(tc_smem_u32(&mma_done[pl]), uint32_t((k >> 1) & 1)))) {
-                tc_fence_after();
-                drain(t0 + k * step, pl, pl ? sB : sA, pl ? nB : nA);
-            } else if (tid == 0) {
-                atomicExch(&g_tc_status, 2);
+            if constexpr (UNIT) {
+                // tile k - 1's phase B, then tile k's phases A and B
+                if (!data_bar_any(fail)) {
+                    if (k >= 1) {
+                        tc_fence_after();
+                        drain_rescaled(t0 + (k - 1) * step, pl ^ 1, pl ? sA : sB, pl ? nA : nB);
+                    }
+                    if (tc_wait_bounded(tc_smem_u32(&mma_done[pl]), uint32_t((k >> 1) & 1))) {
+                        tc_fence_after();
+                        drain_norms(pl);
+                    } else {
+                        fail = true;
+                        if (tid == 0) atomicExch(&g_tc_status, 2);
+                    }
+                    if (!data_bar_any(fail)) {
+                        tc_fence_after();
+                        drain_rescaled(t0 + k * step, pl, pl ? sB : sA, pl ? nB : nA);
+                    }
+                }
+            } else if (!fail) {
+                if (tc_wait_bounded(tc_smem_u32(&mma_done[pl]), uint32_t((k >> 1) & 1))) {
+                    tc_fence_after();
+                    drain(t0 + k * step, pl, pl ? sB : sA);
+                } else if (tid == 0) {
+                    atomicExch(&g_tc_status, 2);
+                }
             }
         }
         asm volatile("cp.async.wait_all;" ::: "memory");
