@@ -15,6 +15,7 @@ from .density_matrix import DensityMatrixSim
 from .gates import (CNOT, CZ, H, ID, RX, RY, RZ, RXX, RYY, RZZ, SDG, SWAP, SX, U, X, Y, Z, Gate, Reset,
                     iSWAP, kak_unitary)
 from .hamiltonians import TFI
+from .environments import RunContext, environment_state_prep, environment_update, sv_environment
 from .montecarlo import MonteCarloSim, trotter_mc_sim
 from .noise import AmplitudeDamping, PauliLindbladNoise, PauliNoise, QubitNoise, amplitude_damping, depolarizing
 from .statevector import StatevectorSim
