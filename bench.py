@@ -317,6 +317,64 @@ def section_adjoint(n=24, layers=40, base_layers=4):
     return out
 
 
+def section_adjoint_batch(n=20, layers=40, sets=64, single_sample=8):
+    """Energies and angle gradients of 64 parameter sets of the 20-qubit
+    hardware-efficient ansatz (TFI energy, complex64) in one batched sweep, vs the
+    single-set adjoint run set by set and vs torch autograd through the
+    reference's torch path (one set, full depth), same GPU."""
+    import torch
+    from qaravan_gb300 import StatevectorSim, workloads
+    from qaravan_gb300.adjoint import BatchedAnsatz, adjoint_energy
+    from qaravan_gb300.hamiltonians import TFI
+    terms = TFI(n, 1, 1).pauli_sum()
+    ba = BatchedAnsatz.hea(n, layers, dtype=torch.complex64)
+    pset = np.stack([workloads.hea_params(n, layers, 100 + s) for s in range(sets)])
+    flat = torch.tensor(pset.reshape(sets, -1), dtype=torch.float64, device="cuda")
+    ba.energy_and_grad(flat, terms)  # warm-up
+    torch.cuda.synchronize()
+    torch.cuda.reset_peak_memory_stats()
+    base = torch.cuda.memory_allocated()
+    t0 = time.perf_counter()
+    E, grad = ba.energy_and_grad(flat, terms)
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    peak = torch.cuda.max_memory_allocated() - base
+    E, grad = E.cpu().numpy(), grad.cpu().numpy()
+
+    def single(s):
+        th = torch.tensor(pset[s], dtype=torch.float64, requires_grad=True)
+        e = adjoint_energy(StatevectorSim(workloads.hea_circuit(n, layers, th), dtype=torch.complex64), terms)
+        e.backward()
+        return float(e.item()), th.grad.numpy().reshape(-1).copy()
+
+    single(0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ref = [single(s) for s in range(single_sample)]
+    torch.cuda.synchronize()
+    t_single = (time.perf_counter() - t0) / single_sample
+    gdiff = max(float(np.abs(grad[s] - g).max() / max(np.abs(g).max(), 1e-30)) for s, (_, g) in enumerate(ref))
+    ediff = max(abs(E[s] - e) for s, (e, _) in enumerate(ref))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e_ref, th = _torch_reference_energy(n, layers, pset[0], terms, "cuda")
+    e_ref.backward()
+    torch.cuda.synchronize()
+    t_auto = time.perf_counter() - t0
+    g_auto = th.grad.numpy().reshape(-1)
+    return {"qubits": n, "layers": layers, "parameter_sets": sets, "params_per_set": 2 * n * layers,
+            "gates_per_set": len(ba.gates), "dtype": "c64",
+            "batched_s": round(t_batch, 4), "gradients_per_s": round(sets / t_batch, 2),
+            "peak_state_multiples_per_set": round(peak / (sets * 2 ** n * 8), 2),
+            "single_set_adjoint_s": round(t_single, 4),
+            "speedup_vs_single_set_adjoint": round(t_single * sets / t_batch, 2),
+            "torch_autograd_one_set_s": round(t_auto, 4),
+            "speedup_vs_torch_autograd": round(t_auto * sets / t_batch, 2),
+            "max_rel_grad_diff_vs_single_set": gdiff, "max_energy_diff_vs_single_set": float(ediff),
+            "max_rel_grad_diff_vs_autograd_set0": float(np.abs(grad[0] - g_auto).max() / np.abs(g_auto).max()),
+            "energy_diff_vs_autograd_set0": abs(float(E[0]) - float(e_ref.item()))}
+
+
 def section_trajectories(n=20, ntraj=1024, steps=40):
     """1024 noisy TFI Trotter trajectories (depolarising 1e-3 + amplitude damping 5e-4
     after every gate), one CUDA graph; mean <Z_i>, <Z_i Z_i+1>."""
@@ -490,9 +548,10 @@ def gpu_arm(args):
     del state, ex, sim
     torch.cuda.empty_cache()
     sections = {}
-    wanted = args.sections.split(",") if args.sections != "all" else ["variants", "adjoint", "trajectories",
-                                                                       "dm_batch"]
+    wanted = args.sections.split(",") if args.sections != "all" else ["variants", "adjoint", "adjoint_batch",
+                                                                       "trajectories", "dm_batch"]
     for name, fn in [("variants", lambda: section_variants(n, gates)), ("adjoint", section_adjoint),
+                     ("adjoint_batch", section_adjoint_batch),
                      ("trajectories", section_trajectories), ("dm_batch", section_dm_batch)]:
         if name in wanted:
             try:
@@ -575,7 +634,7 @@ def main():
     p.add_argument("--cpu-budget", type=float, default=12.0)
     p.add_argument("--ref-gates", type=int, default=2)
     p.add_argument("--sections", default="all",
-                   help="comma list of variants,adjoint,trajectories,dm_batch; 'none' for the headline only")
+                   help="comma list of variants,adjoint,adjoint_batch,trajectories,dm_batch; 'none' for the headline only")
     args = p.parse_args()
     if args.impl == "reference":
         reference_arm(args)

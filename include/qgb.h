@@ -216,6 +216,33 @@ int qgb_partial_overlap(const void* a, const void* b, int dtype, int n, const in
 int qgb_adjoint_step(void* phi, void* lam, int dtype, int n, const int* indices, int k, const void* op,
                      double* grad_out, void* scratch, size_t scratch_bytes, void* stream);
 
+/* qgb_adjoint_step for `batch` states (at sv_stride elements; phi and lam
+ * batches disjoint), state b with its own gate matrix at op + b * op_stride
+ * elements; grad_out (if not NULL) gets each state's 2 * 4^k doubles back to
+ * back. One launch for every parameter set of a batched gradient. */
+int qgb_adjoint_step_batched(void* phi, void* lam, int dtype, int n, const int* indices, int k, const void* op,
+                             int64_t op_stride, int64_t batch, int64_t sv_stride, double* grad_out, void* scratch,
+                             size_t scratch_bytes, void* stream);
+
+/* Parametrised gate matrices M(theta) = expm(-i theta P) = cos(theta) I -
+ * i sin(theta) P (core/param_gates.py:21-80, no factor 1/2) for `nsets`
+ * parameter sets in one launch: gate g of set s (kinds[g]: 1 RX, 2 RY, 3 RZ,
+ * 4 RXX, 5 RYY, 6 RZZ; other kinds are left to the caller) with angle
+ * params[s * nparams + pidx[g]] (float64), written row-major in `dtype` at
+ * out + s * set_stride + g * gate_stride elements. All arrays in device memory.
+ * Replaces the per-gate host construction and host-to-device copy of the
+ * reference (tensorQ/statevector_sim.py:19-29). */
+int qgb_param_matrices(const int* kinds, const int* pidx, int ngates, const double* params, int nparams,
+                       int64_t nsets, void* out, int dtype, int64_t gate_stride, int64_t set_stride, void* stream);
+
+/* Chain rule to the angles: grad_out[s * nparams + j] = sum over the gates g
+ * of parameter j (CSR csr_ptr / csr_gate) of Re sum_rc conj(G[r,c])
+ * dM/dtheta[r,c], G the gate's matrix gradient (torch's convention, complex
+ * float64) for set s at gmat + g * gate_block + s * d * d double2 (d = 2 or 4:
+ * the batched adjoint step's output layout). Device arrays. */
+int qgb_param_grads(const int* kinds, const int* csr_ptr, const int* csr_gate, int nparams, const double* params,
+                    int64_t nsets, const double* gmat, int64_t gate_block, double* grad_out, void* stream);
+
 /* ---- noisy trajectories -------------------------------------------------- */
 
 /* Blocks per trajectory used by qgb_traj_step (sizes its `partials`: at least

@@ -277,6 +277,8 @@ struct AdjointArgs {
     int sorted[2];
     uint32_t off[4];
     int want_grad;
+    int64_t sv_stride;  // batch: state b at phi + b * sv_stride (and lam)
+    int64_t op_stride;  // batch: its gate matrix at U + b * op_stride
 };
 
 template <typename T, int K>
@@ -286,6 +288,10 @@ __global__ void __launch_bounds__(kRedThreads) adjoint_kernel(cplx<T>* __restric
                                                               double* __restrict__ partials) {
     constexpr int D = 1 << K;
     using C = cplx<T>;
+    const int64_t bidx = blockIdx.y;  // state of the batch
+    phi += bidx * a.sv_stride;
+    lam += bidx * a.sv_stride;
+    U += bidx * a.op_stride;
     C ud[D * D];  // U^dagger
 #pragma unroll
     for (int r = 0; r < D; ++r)
@@ -334,7 +340,8 @@ __global__ void __launch_bounds__(kRedThreads) adjoint_kernel(cplx<T>* __restric
             lam[base + a.off[r]] = ln[r];
         }
     }
-    if (a.want_grad) block_reduce_store<2 * D * D>(acc, partials + blockIdx.x, gridDim.x);
+    // partials[(b * slots + slot) * nblk + blk], the layout finish() sums
+    if (a.want_grad) block_reduce_store<2 * D * D>(acc, partials + bidx * (2 * D * D) * gridDim.x + blockIdx.x, gridDim.x);
 }
 
 // out = sum_t coeff[t] P_t sv
@@ -634,19 +641,28 @@ extern "C" int qgb_pauli_apply(const void* sv, void* out, int dtype, int n, cons
     return check_launch("pauli apply");
 }
 
-extern "C" int qgb_adjoint_step(void* phi, void* lam, int dtype, int n, const int* indices, int k, const void* op,
-                                double* grad_out, void* scratch, size_t scratch_bytes, void* stream) {
-    int rc = check_common(phi, dtype, n, 1, 0);
+extern "C" int qgb_adjoint_step_batched(void* phi, void* lam, int dtype, int n, const int* indices, int k,
+                                        const void* op, int64_t op_stride, int64_t batch, int64_t sv_stride,
+                                        double* grad_out, void* scratch, size_t scratch_bytes, void* stream) {
+    int rc = check_common(phi, dtype, n, batch, sv_stride);
     if (rc) return rc;
     if (!lam || !op || !indices) return set_error(QGB_EINVAL, "null pointer");
     if (lam == phi) return set_error(QGB_EINVAL, "the two vectors must be distinct");
     if (k < 1 || k > 2 || k > n) return set_error(QGB_EINVAL, "adjoint steps support gates on 1 or 2 sites (k=%d)", k);
+    if (op_stride < 0) return set_error(QGB_EINVAL, "negative operator stride");
+    const int64_t span = (batch - 1) * (sv_stride > 0 ? sv_stride : 0) + (int64_t(1) << n);
+    const char* pb = static_cast<const char*>(phi);
+    const char* lb = static_cast<const char*>(lam);
+    const int64_t esz = dtype == QGB_C64 ? 8 : 16;
+    if (pb < lb + span * esz && lb < pb + span * esz) return set_error(QGB_EINVAL, "the two batches overlap");
     const int slots = 2 << (2 * k);
-    if (grad_out && (!scratch || scratch_bytes < red_scratch(n, slots, 1)))
+    if (grad_out && (!scratch || scratch_bytes < red_scratch(n, slots, batch)))
         return set_error(QGB_ESCRATCH, "scratch too small");
     AdjointArgs a{};
     a.n = n;
     a.want_grad = grad_out != nullptr;
+    a.sv_stride = batch > 1 ? sv_stride : 0;
+    a.op_stride = batch > 1 ? op_stride : 0;
     int pos[2];
     for (int j = 0; j < k; ++j) {
         if (indices[j] < 0 || indices[j] >= n) return set_error(QGB_EINVAL, "site out of range");
@@ -659,7 +675,7 @@ extern "C" int qgb_adjoint_step(void* phi, void* lam, int dtype, int n, const in
     }
     for (int r = 0; r < (1 << k); ++r) a.off[r] = uint32_t(matrix_offset(r, pos, k));
     cudaStream_t st = (cudaStream_t)stream;
-    const unsigned grid = unsigned(red_blocks(n));
+    const dim3 grid(unsigned(red_blocks(n)), unsigned(batch));
     double* part = (double*)scratch;
     if (dtype == QGB_C64) {
         if (k == 1) adjoint_kernel<float, 1><<<grid, kRedThreads, 0, st>>>((float2*)phi, (float2*)lam, (const float2*)op, a, part);
@@ -670,7 +686,13 @@ extern "C" int qgb_adjoint_step(void* phi, void* lam, int dtype, int n, const in
     }
     if ((rc = check_launch("adjoint step"))) return rc;
     if (!grad_out) return QGB_OK;
-    return finish(part, red_blocks(n), slots, 1, nullptr, grad_out, st);
+    return finish(part, red_blocks(n), slots, batch, nullptr, grad_out, st);
+}
+
+extern "C" int qgb_adjoint_step(void* phi, void* lam, int dtype, int n, const int* indices, int k, const void* op,
+                                double* grad_out, void* scratch, size_t scratch_bytes, void* stream) {
+    return qgb_adjoint_step_batched(phi, lam, dtype, n, indices, k, op, 0, 1, 0, grad_out, scratch, scratch_bytes,
+                                    stream);
 }
 
 // ---------------------------------------------------------------------------
