@@ -355,6 +355,8 @@ def section_adjoint_batch(n=20, layers=40, sets=64, single_sample=8):
     t_single = (time.perf_counter() - t0) / single_sample
     gdiff = max(float(np.abs(grad[s] - g).max() / max(np.abs(g).max(), 1e-30)) for s, (_, g) in enumerate(ref))
     ediff = max(abs(E[s] - e) for s, (e, _) in enumerate(ref))
+    e_w, _ = _torch_reference_energy(n, 1, pset[0][:1], terms, "cuda")  # warm-up of the torch path
+    e_w.backward()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     e_ref, th = _torch_reference_energy(n, layers, pset[0], terms, "cuda")
@@ -362,6 +364,12 @@ def section_adjoint_batch(n=20, layers=40, sets=64, single_sample=8):
     torch.cuda.synchronize()
     t_auto = time.perf_counter() - t0
     g_auto = th.grad.numpy().reshape(-1)
+    # error of the complex64 batch against the same sweep in complex128 (first 4 sets)
+    b128 = BatchedAnsatz.hea(n, layers, dtype=torch.complex128)
+    E128, g128 = b128.energy_and_grad(flat[:4], terms)
+    E128, g128 = E128.cpu().numpy(), g128.cpu().numpy()
+    err64 = max(float(np.abs(grad[s] - g128[s]).max() / np.abs(g128[s]).max()) for s in range(4))
+    err64_single = max(float(np.abs(ref[s][1] - g128[s]).max() / np.abs(g128[s]).max()) for s in range(4))
     return {"qubits": n, "layers": layers, "parameter_sets": sets, "params_per_set": 2 * n * layers,
             "gates_per_set": len(ba.gates), "dtype": "c64",
             "batched_s": round(t_batch, 4), "gradients_per_s": round(sets / t_batch, 2),
@@ -371,6 +379,8 @@ def section_adjoint_batch(n=20, layers=40, sets=64, single_sample=8):
             "torch_autograd_one_set_s": round(t_auto, 4),
             "speedup_vs_torch_autograd": round(t_auto * sets / t_batch, 2),
             "max_rel_grad_diff_vs_single_set": gdiff, "max_energy_diff_vs_single_set": float(ediff),
+            "max_rel_grad_err_vs_c128": err64, "max_energy_err_vs_c128": float(np.abs(E[:4] - E128).max()),
+            "single_set_max_rel_grad_err_vs_c128": err64_single,
             "max_rel_grad_diff_vs_autograd_set0": float(np.abs(grad[0] - g_auto).max() / np.abs(g_auto).max()),
             "energy_diff_vs_autograd_set0": abs(float(E[0]) - float(e_ref.item()))}
 

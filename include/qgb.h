@@ -224,6 +224,18 @@ int qgb_adjoint_step_batched(void* phi, void* lam, int dtype, int n, const int* 
                              int64_t op_stride, int64_t batch, int64_t sv_stride, double* grad_out, void* scratch,
                              size_t scratch_bytes, void* stream);
 
+/* The reverse step for a rotation U = expm(-i theta P) (P a Pauli product on
+ * the k sites, P^2 = I; `generator` = P as 4^k complex128 pairs, row-major in
+ * the order of `indices`, exactly one nonzero per row, else QGB_EINVAL):
+ * uncomputes phi and lam like qgb_adjoint_step_batched and writes
+ * grad_out[b] = Im <lam_b| P |phi_b>, both taken at the gate's
+ * output. For a real loss with co-state lam, dL/dtheta = 2 * grad_out[b]: the
+ * angle derivative of core/param_gates.py:51-103 without the 2 * 4^k
+ * matrix-gradient slots. */
+int qgb_adjoint_step_rotation(void* phi, void* lam, int dtype, int n, const int* indices, int k, const void* op,
+                              int64_t op_stride, const double* generator, int64_t batch, int64_t sv_stride,
+                              double* grad_out, void* scratch, size_t scratch_bytes, void* stream);
+
 /* Parametrised gate matrices M(theta) = expm(-i theta P) = cos(theta) I -
  * i sin(theta) P (core/param_gates.py:21-80, no factor 1/2) for `nsets`
  * parameter sets in one launch: gate g of set s (kinds[g]: 1 RX, 2 RY, 3 RZ,
@@ -235,13 +247,14 @@ int qgb_adjoint_step_batched(void* phi, void* lam, int dtype, int n, const int* 
 int qgb_param_matrices(const int* kinds, const int* pidx, int ngates, const double* params, int nparams,
                        int64_t nsets, void* out, int dtype, int64_t gate_stride, int64_t set_stride, void* stream);
 
-/* Chain rule to the angles: grad_out[s * nparams + j] = sum over the gates g
- * of parameter j (CSR csr_ptr / csr_gate) of Re sum_rc conj(G[r,c])
- * dM/dtheta[r,c], G the gate's matrix gradient (torch's convention, complex
- * float64) for set s at gmat + g * gate_block + s * d * d double2 (d = 2 or 4:
- * the batched adjoint step's output layout). Device arrays. */
-int qgb_param_grads(const int* kinds, const int* csr_ptr, const int* csr_gate, int nparams, const double* params,
-                    int64_t nsets, const double* gmat, int64_t gate_block, double* grad_out, void* stream);
+/* Angle gradients from per-gate derivatives: grad_out[s * nparams + j] =
+ * scale * sum over the gates g of parameter j (CSR csr_ptr / csr_gate, in that
+ * order) of gate_values[g * nsets + s], e.g. the outputs of
+ * qgb_adjoint_step_rotation (scale 2 * dL/dE). Device arrays. Replaces the
+ * autograd walk from each gate matrix back to its angle (torch.linalg.matrix_exp
+ * backward, core/param_gates.py:51-103). */
+int qgb_param_grads(const int* csr_ptr, const int* csr_gate, int nparams, int64_t nsets, const double* gate_values,
+                    double scale, double* grad_out, void* stream);
 
 /* ---- noisy trajectories -------------------------------------------------- */
 

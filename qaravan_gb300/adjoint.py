@@ -78,7 +78,11 @@ class _Runner:
         return psi
 
     def reverse(self, psi, lam, mats, need):
-        """Reverse sweep from (psi, lam); returns per-gate sum_rest lam[r] conj(phi[c]) (complex128) or None."""
+        """Reverse sweep from (psi, lam). ``need[i]``: falsy (no gradient), True
+        (the matrix block sum_rest lam[r] conj(phi[c])) or, for a rotation
+        exp(-i theta P), P as a ctypes double array (re, im pairs): the scalar
+        Im <lam|P|phi> at the gate's output. Returns per gate the complex128
+        block, the float, or None."""
         L = _lib.lib()
         n = self.n
         st = _lib.stream_ptr(self.device)
@@ -96,20 +100,29 @@ class _Runner:
         scr = self.scratch.get(nbytes)
         base, gbase = dev.data_ptr(), grads_dev.data_ptr()
         for i in range(len(self.gates) - 1, -1, -1):
-            g = self.gates[i]
-            out = gbase + i * 32 * 8 if need[i] else None
-            _lib.check(L.qgb_adjoint_step(phi.data_ptr(), lam.data_ptr(), self.code, n, self._sites[i],
-                                          len(g.indices), base + int(offs[i]) * isz, out, scr.data_ptr(), nbytes, st),
-                       "adjoint_step")
+            k = len(self.gates[i].indices)
+            op = base + int(offs[i]) * isz
+            want = need[i]
+            if want is not None and want is not False and want is not True:
+                _lib.check(L.qgb_adjoint_step_rotation(phi.data_ptr(), lam.data_ptr(), self.code, n, self._sites[i], k,
+                                                       op, 0, want, 1, 0, gbase + i * 32 * 8, scr.data_ptr(), nbytes,
+                                                       st), "adjoint_step_rotation")
+            else:
+                out = gbase + i * 32 * 8 if want else None
+                _lib.check(L.qgb_adjoint_step(phi.data_ptr(), lam.data_ptr(), self.code, n, self._sites[i], k, op, out,
+                                              scr.data_ptr(), nbytes, st), "adjoint_step")
         host = grads_dev.cpu().numpy()
         out = []
         for i, g in enumerate(self.gates):
-            if not need[i]:
+            want = need[i]
+            if want is None or want is False:
                 out.append(None)
-                continue
-            d = 2 ** len(g.indices)
-            v = host[i, :2 * d * d]
-            out.append((v[0::2] + 1j * v[1::2]).reshape(d, d))
+            elif want is True:
+                d = 2 ** len(g.indices)
+                v = host[i, :2 * d * d]
+                out.append((v[0::2] + 1j * v[1::2]).reshape(d, d))
+            else:
+                out.append(float(host[i, 0]))
         return out
 
 
@@ -117,39 +130,109 @@ def _grad_like(m, arr):
     return torch.from_numpy(arr).to(device=m.device, dtype=m.dtype if m.is_complex() else torch.complex128)
 
 
+# Rotations exp(-i theta P) with P a Pauli or a Pauli pair (core/param_gates.py:51-103):
+# kind -> P as a dense matrix (rows = the gate's index order).
+_KIND = {"RX": 1, "RY": 2, "RZ": 3, "RXX": 4, "RYY": 5, "RZZ": 6}
+_PX = np.array([[0, 1], [1, 0]], dtype=np.complex128)
+_PY = np.array([[0, -1j], [1j, 0]], dtype=np.complex128)
+_PZ = np.array([[1, 0], [0, -1]], dtype=np.complex128)
+_GEN = {1: _PX, 2: _PY, 3: _PZ, 4: np.kron(_PX, _PX), 5: np.kron(_PY, _PY), 6: np.kron(_PZ, _PZ)}
+_GEN_C = {k: _lib.double_array(np.stack([m.real, m.imag], axis=-1).reshape(-1)) for k, m in _GEN.items()}
+
+
+def _rotation_angle(g):
+    """The torch angle of a rotation gate whose matrix is still the one built
+    from it, else None."""
+    kind = _KIND.get(getattr(g, "name", None))
+    angles = getattr(g, "angles", None)
+    if kind is None or not isinstance(angles, tuple) or len(angles) != 1:
+        return None
+    a = angles[0]
+    if not (torch.is_tensor(a) and a.numel() == 1 and getattr(g, "built_from_angles", lambda: False)()):
+        return None
+    return a
+
+
+class _Inputs:
+    """How the gates enter autograd. A rotation gate exp(-i theta P) built from
+    a torch angle contributes its angle (all such angles stacked into one
+    float64 vector): dL/dtheta = Re sum conj(G) dM/dtheta (G = dL/dM) equals
+    2 Im <lam|P|phi> at the gate's output (M commutes with P), which the
+    rotation form of the reverse step reduces directly, so autograd never walks
+    back through ``matrix_exp``. Every other gate contributes its matrix."""
+
+    def __init__(self, gates):
+        self.mats = _matrices(gates)
+        self.rot, angles = [], []
+        for i, g in enumerate(gates):
+            a = _rotation_angle(g)
+            if a is not None:
+                self.rot.append(i)
+                angles.append(a.reshape(()).to(torch.float64))
+        rs = set(self.rot)
+        self.other = [i for i in range(len(gates)) if i not in rs]
+        self.angles = torch.stack([a.cpu() for a in angles]) if angles else torch.zeros(0, dtype=torch.float64)
+        self.kinds = np.array([_KIND[gates[i].name] for i in self.rot], dtype=np.int64)
+
+    def args(self):
+        return (self.angles, *[self.mats[i] for i in self.other])
+
+    def need(self, needs_input_grad, first):
+        """Per gate, what the reverse sweep computes (``_Runner.reverse``), from
+        the Function's ``needs_input_grad`` (angles at ``first``, other matrices
+        after): a rotation's generator, True for a matrix block, or False."""
+        need = [False] * len(self.mats)
+        if needs_input_grad[first]:
+            for i, k in zip(self.rot, self.kinds):
+                need[i] = _GEN_C[int(k)]
+        for j, i in enumerate(self.other):
+            need[i] = bool(needs_input_grad[first + 1 + j])
+        return need
+
+    def grads(self, blocks, scale, needs_input_grad, first):
+        """Gradients for ``args()`` from the sweep's outputs times ``scale`` (the
+        factor that turns a block into dL/dM): a rotation's Im <lam|P|phi> times
+        ``scale`` is Re sum conj(dL/dM) dM/dtheta, its angle's gradient."""
+        g_ang = None
+        if needs_input_grad[first] and self.rot:
+            out = np.array([scale * blocks[i] for i in self.rot], dtype=np.float64)
+            g_ang = torch.from_numpy(out).to(self.angles.device)
+        rest = [None if blocks[i] is None else _grad_like(self.mats[i], scale * blocks[i]) for i in self.other]
+        return (g_ang, *rest)
+
+
 class _StateFn(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, runner, *mats):
-        psi = runner.forward_state(mats)
-        ctx.runner = runner
-        ctx.mats = mats
+    def forward(ctx, runner, inputs, *args):
+        psi = runner.forward_state(inputs.mats)
+        ctx.runner, ctx.inputs = runner, inputs
         ctx.save_for_backward(psi)
         return psi
 
     @staticmethod
     def backward(ctx, g_psi):
         (psi,) = ctx.saved_tensors
-        runner, mats = ctx.runner, ctx.mats
-        need = [ctx.needs_input_grad[1 + i] for i in range(len(mats))]
+        runner, inputs = ctx.runner, ctx.inputs
+        need = inputs.need(ctx.needs_input_grad, 2)
         lam = g_psi.detach().to(runner.dtype).contiguous().clone()
-        blocks = runner.reverse(psi, lam, mats, need)
-        return (None, *[None if b is None else _grad_like(m, b) for m, b in zip(mats, blocks)])
+        blocks = runner.reverse(psi, lam, inputs.mats, need)
+        return (None, None, *inputs.grads(blocks, 1.0, ctx.needs_input_grad, 2))
 
 
 class _EnergyFn(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, runner, terms, *mats):
+    def forward(ctx, runner, terms, inputs, *args):
         from .statevector import pauli_expectations
-        psi = runner.forward_state(mats)
+        psi = runner.forward_state(inputs.mats)
         e = pauli_expectations(psi, runner.n, terms).sum()
-        ctx.runner, ctx.terms, ctx.mats = runner, terms, mats
+        ctx.runner, ctx.terms, ctx.inputs = runner, terms, inputs
         ctx.save_for_backward(psi)
         return e
 
     @staticmethod
     def backward(ctx, g_e):
         (psi,) = ctx.saved_tensors
-        runner, terms, mats = ctx.runner, ctx.terms, ctx.mats
+        runner, terms, inputs = ctx.runner, ctx.terms, ctx.inputs
         L = _lib.lib()
         n = runner.n
         lam = torch.empty_like(psi)
@@ -157,10 +240,9 @@ class _EnergyFn(torch.autograd.Function):
         coeff = _lib.double_array([c for c, _ in terms])
         _lib.check(L.qgb_pauli_apply(psi.data_ptr(), lam.data_ptr(), runner.code, n, strings, coeff, len(terms), 1, 0,
                                      _lib.stream_ptr(runner.device)), "pauli_apply")
-        need = [ctx.needs_input_grad[2 + i] for i in range(len(mats))]
-        blocks = runner.reverse(psi, lam, mats, need)
-        scale = 2.0 * float(g_e)
-        return (None, None, *[None if b is None else _grad_like(m, scale * b) for m, b in zip(mats, blocks)])
+        need = inputs.need(ctx.needs_input_grad, 3)
+        blocks = runner.reverse(psi, lam, inputs.mats, need)
+        return (None, None, None, *inputs.grads(blocks, 2.0 * float(g_e), ctx.needs_input_grad, 3))
 
 
 def _matrices(gates):
@@ -170,20 +252,20 @@ def _matrices(gates):
 
 def run_with_adjoint(sim):
     """Differentiable ``StatevectorSim.run``: the returned state carries an
-    adjoint backward to every gate matrix that requires grad."""
+    adjoint backward to every gate matrix (or rotation angle) that requires grad."""
     gates = _gate_list(sim)
-    return _StateFn.apply(_Runner(sim, gates), *_matrices(gates))
+    inputs = _Inputs(gates)
+    return _StateFn.apply(_Runner(sim, gates), inputs, *inputs.args())
 
 
 def adjoint_energy(sim, terms):
     """Differentiable ``sum_t c_t <psi|P_t|psi>`` (float64) of ``sim``'s circuit."""
     gates = _gate_list(sim)
-    return _EnergyFn.apply(_Runner(sim, gates), list(terms), *_matrices(gates))
+    inputs = _Inputs(gates)
+    return _EnergyFn.apply(_Runner(sim, gates), list(terms), inputs, *inputs.args())
 
 
 # ------------------------------------------------------------ parameter-set batches
-
-_KIND = {"RX": 1, "RY": 2, "RZ": 3, "RXX": 4, "RYY": 5, "RZZ": 6}
 
 
 class BatchedAnsatz:
@@ -197,8 +279,10 @@ class BatchedAnsatz:
     the parameter tensor (``qgb_param_matrices``: ``expm(-i theta P)`` as in
     ``core/param_gates.py``); the forward pass applies each gate to all sets in
     one launch with per-set matrices; the reverse sweep (``lam = H psi``, then
-    ``qgb_adjoint_step_batched`` per gate) carries all sets together and leaves
-    each gate's matrix gradient, which ``qgb_param_grads`` maps to the angles.
+    one step per gate over all sets: ``qgb_adjoint_step_rotation`` for a
+    rotation, which also reduces its angle derivative 2 Im <lam|P|phi>, and
+    ``qgb_adjoint_step_batched`` for a fixed gate) carries all sets together;
+    ``qgb_param_grads`` sums the derivatives of the gates of each parameter.
     Memory: three states per set."""
 
     def __init__(self, n, gates, nparams=None, dtype=torch.complex64, device="cuda"):
@@ -235,6 +319,7 @@ class BatchedAnsatz:
         self._csr_gate = torch.from_numpy(flat).to(self.device)
         self._sites = [_lib.int_array(idx) for _, idx, _ in self.gates]
         self._need = [k != 0 for k in kinds]
+        self._gens = [_GEN_C[k] if k else None for k in kinds]
         self.scratch = Scratch(self.device)
 
     @classmethod
@@ -291,19 +376,23 @@ class BatchedAnsatz:
         _lib.check(L.qgb_pauli_apply(psi.data_ptr(), lam.data_ptr(), self.code, n, strings, coeff, len(terms), P, N, st),
                    "pauli_apply")
         phi = psi  # uncomputed in place
-        gblock = 32 * P  # doubles per gate: each set's 2 * d^2 back to back
-        gmat = torch.zeros(len(self.gates) * gblock, dtype=torch.float64, device=self.device)
+        gvals = torch.zeros(len(self.gates) * P, dtype=torch.float64, device=self.device)  # [gate][set]
         nbytes = L.qgb_reduce_scratch_bytes(n, 32, P)
         scr = self.scratch.get(nbytes)
         for g in range(len(self.gates) - 1, -1, -1):
             idx = self.gates[g][1]
-            out = gmat.data_ptr() + g * gblock * 8 if self._need[g] else None
-            _lib.check(L.qgb_adjoint_step_batched(phi.data_ptr(), lam.data_ptr(), self.code, n, self._sites[g], len(idx),
-                                                  base + g * 16 * isz, set_stride, P, N, out, scr.data_ptr(), nbytes,
-                                                  st), "adjoint_step_batched")
+            op = base + g * 16 * isz
+            if self._need[g]:
+                _lib.check(L.qgb_adjoint_step_rotation(phi.data_ptr(), lam.data_ptr(), self.code, n, self._sites[g],
+                                                       len(idx), op, set_stride, self._gens[g], P, N,
+                                                       gvals.data_ptr() + g * P * 8, scr.data_ptr(), nbytes, st),
+                           "adjoint_step_rotation")
+            else:
+                _lib.check(L.qgb_adjoint_step_batched(phi.data_ptr(), lam.data_ptr(), self.code, n, self._sites[g],
+                                                      len(idx), op, set_stride, P, N, None, scr.data_ptr(), nbytes,
+                                                      st), "adjoint_step_batched")
         grad = torch.empty(P, self.nparams, dtype=torch.float64, device=self.device)
-        gmat *= 2.0  # torch's convention: dE/dM = 2 sum lam conj(phi) for E = <psi|H|psi>
-        _lib.check(L.qgb_param_grads(self._kinds.data_ptr(), self._csr_ptr.data_ptr(), self._csr_gate.data_ptr(),
-                                     self.nparams, params.data_ptr(), P, gmat.data_ptr(), gblock // 2, grad.data_ptr(),
-                                     st), "param_grads")
+        # dE/dtheta = 2 Im <lam|P|phi> per gate (lam = H psi), summed over the gates of each parameter
+        _lib.check(L.qgb_param_grads(self._csr_ptr.data_ptr(), self._csr_gate.data_ptr(), self.nparams, P,
+                                     gvals.data_ptr(), 2.0, grad.data_ptr(), st), "param_grads")
         return E, grad

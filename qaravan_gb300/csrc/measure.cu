@@ -10,8 +10,9 @@
 //    list order, first site = most significant outcome bit), r the rest.
 //    A warp sums one (bin, chunk of r) pair with lane-strided reads and a
 //    fixed shuffle tree; a second kernel adds the chunks of each bin in
-//    order. Float64 throughout, bitwise reproducible. When r has fewer than
-//    32 values one thread sums a bin.
+//    order. Float64 sums (complex64 states: float32 sums of 16 squares
+//    folded into float64, the Acc rule), bitwise reproducible. When r has
+//    fewer than 32 values one thread sums a bin.
 //  * sample_outcomes: inclusive prefix sums of p in float64 (blocks of 4096,
 //    the block totals scanned by one CTA, then offsets added), and per shot a
 //    53-bit Philox uniform u scaled by the total and a binary search for the
@@ -54,12 +55,14 @@ __global__ void __launch_bounds__(kMeasThreads) probs_warp_kernel(const cplx<T>*
     if (w >= bins * a.chunks) return;  // whole warps leave together
     const uint64_t b = w % bins, c = w / bins;
     const uint64_t ob = place_outcome(b, a);
-    double acc = 0.0;
+    Acc<T, 1> part_sum;
     for (uint64_t r = c * a.chunk + lane; r < (c + 1) * a.chunk; r += 32) {
         const cplx<T> v = sv[insert_zeros(r, a.sorted, a.m) | ob];
-        acc = fma(double(v.x), double(v.x), acc);
-        acc = fma(double(v.y), double(v.y), acc);
+        part_sum.add(0, v.x * v.x + v.y * v.y);
+        part_sum.step();
     }
+    part_sum.flush();
+    double acc = part_sum.d[0];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) part[c * bins + b] = acc;
@@ -71,13 +74,14 @@ __global__ void __launch_bounds__(kMeasThreads) probs_thread_kernel(const cplx<T
     const uint64_t b = uint64_t(blockIdx.x) * kMeasThreads + threadIdx.x;
     if (b >= (uint64_t(1) << a.m)) return;
     const uint64_t ob = place_outcome(b, a);
-    double acc = 0.0;
+    Acc<T, 1> acc;
     for (uint64_t r = 0; r < a.rest; ++r) {
         const cplx<T> v = sv[insert_zeros(r, a.sorted, a.m) | ob];
-        acc = fma(double(v.x), double(v.x), acc);
-        acc = fma(double(v.y), double(v.y), acc);
+        acc.add(0, v.x * v.x + v.y * v.y);
+        acc.step();
     }
-    probs[b] = acc;
+    acc.flush();
+    probs[b] = acc.d[0];
 }
 
 __global__ void __launch_bounds__(kMeasThreads) probs_finish_kernel(const double* __restrict__ part, double* __restrict__ probs,

@@ -7,10 +7,11 @@
 // (tensorQ/statevector_sim.py:19-29). Since P^2 = I,
 //     M(theta)    =  cos(theta) I - i sin(theta) P,
 //     dM/dtheta   = -sin(theta) I - i cos(theta) P,
-// so one thread per (parameter set, gate) writes M from the set's angle, and
-// one thread per (set, parameter) sums Re tr(G^H dM/dtheta) over the gates that
-// use the parameter (G the gate's matrix gradient in torch's convention,
-// 2 dL/d conj(M)), in the fixed order of a host-built CSR list.
+// so one thread per (parameter set, gate) writes M from the set's angle. The
+// angle derivative of each gate comes from the rotation form of the adjoint
+// step (2 Im <lam|P|phi>, equal to Re tr(G^H dM/dtheta) for the matrix
+// gradient G); one thread per (set, parameter) then sums it over the gates
+// that use the parameter, in the fixed order of a host-built CSR list.
 // Kinds: 1 RX, 2 RY, 3 RZ (one site); 4 RXX, 5 RYY, 6 RZZ (two sites).
 #include "qgb_common.cuh"
 
@@ -58,39 +59,20 @@ __global__ void param_matrices_kernel(const int* __restrict__ kinds, const int* 
     }
 }
 
-// grad_out[s * nparams + j] = sum over gates g using parameter j (CSR: gates
-// csr_gate[csr_ptr[j] .. csr_ptr[j+1])) of Re sum_rc conj(G_g[r,c]) dM_g/dtheta[r,c].
-// G of gate g for set s at gmat + g * gate_block + s * d^2 (the batched adjoint
-// step's per-gate output: each set's d x d block back to back).
-__global__ void param_grads_kernel(const int* __restrict__ kinds, const int* __restrict__ csr_ptr,
-                                   const int* __restrict__ csr_gate, int nparams, const double* __restrict__ params,
-                                   int64_t nsets, const double2* __restrict__ gmat, int64_t gate_block,
+// grad_out[s * nparams + j] = scale * sum over the gates g of parameter j
+// (CSR: csr_gate[csr_ptr[j] .. csr_ptr[j+1]), in that order) of
+// gate_values[g * nsets + s] -- per-gate angle derivatives, e.g. the rotation
+// form of the adjoint step, Im <lam|P|phi>, for which scale = 2.
+__global__ void param_grads_kernel(const int* __restrict__ csr_ptr, const int* __restrict__ csr_gate, int nparams,
+                                   int64_t nsets, const double* __restrict__ gate_values, double scale,
                                    double* __restrict__ grad_out) {
     const int64_t item = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (item >= nsets * nparams) return;
     const int64_t s = item / nparams;
     const int j = int(item - s * nparams);
-    double sn, cs;
-    sincos(params[s * nparams + j], &sn, &cs);
     double acc = 0.0;
-    for (int e = csr_ptr[j]; e < csr_ptr[j + 1]; ++e) {
-        const int g = csr_gate[e];
-        const int kind = kinds[g];
-        if (kind < 1 || kind > 6) continue;
-        const int d = kind_dim(kind);
-        const double2* G = gmat + int64_t(g) * gate_block + s * d * d;
-        for (int r = 0; r < d; ++r) {
-            double2 ph;
-            const int c = pauli_perm(kind, r, ph);
-            // dM[r,c] = -i cos(theta) ph (+ -sin(theta) on the diagonal)
-            double dre = cs * ph.y, dim = -cs * ph.x;
-            if (c == r) dre -= sn;
-            const double2 gv = G[r * d + c];
-            acc += gv.x * dre + gv.y * dim;  // Re(conj(g) dm)
-            if (c != r) acc += G[r * d + r].x * (-sn);
-        }
-    }
-    grad_out[s * nparams + j] = acc;
+    for (int e = csr_ptr[j]; e < csr_ptr[j + 1]; ++e) acc += gate_values[int64_t(csr_gate[e]) * nsets + s];
+    grad_out[s * nparams + j] = scale * acc;
 }
 
 }  // namespace qgb
@@ -119,15 +101,13 @@ extern "C" int qgb_param_matrices(const int* kinds, const int* pidx, int ngates,
     return check_launch("param matrices");
 }
 
-extern "C" int qgb_param_grads(const int* kinds, const int* csr_ptr, const int* csr_gate, int nparams,
-                               const double* params, int64_t nsets, const double* gmat, int64_t gate_block,
-                               double* grad_out, void* stream) {
-    if (!kinds || !csr_ptr || !csr_gate || !params || !gmat || !grad_out) return set_error(QGB_EINVAL, "null pointer");
+extern "C" int qgb_param_grads(const int* csr_ptr, const int* csr_gate, int nparams, int64_t nsets,
+                               const double* gate_values, double scale, double* grad_out, void* stream) {
+    if (!csr_ptr || !csr_gate || !gate_values || !grad_out) return set_error(QGB_EINVAL, "null pointer");
     if (nparams < 1 || nsets < 1) return set_error(QGB_EINVAL, "empty parameter batch");
-    if (gate_block < 16 * nsets) return set_error(QGB_EINVAL, "gradient block smaller than 16 * nsets");
     const int64_t items = nsets * nparams;
     const unsigned g = unsigned((items + 255) / 256);
-    param_grads_kernel<<<g, 256, 0, (cudaStream_t)stream>>>(kinds, csr_ptr, csr_gate, nparams, params, nsets,
-                                                            (const double2*)gmat, gate_block, grad_out);
+    param_grads_kernel<<<g, 256, 0, (cudaStream_t)stream>>>(csr_ptr, csr_gate, nparams, nsets, gate_values, scale,
+                                                            grad_out);
     return check_launch("param grads");
 }

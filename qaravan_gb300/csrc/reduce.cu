@@ -4,10 +4,11 @@
 // tensorQ/statevector_sim.py:217-234; local/one_local_expectation :63-94;
 // partial_overlap :155-180; DensityMatrixSim expectations and trace,
 // tensorQ/density_matrix_sim.py:49-89). Each reduction reads the state once
-// per group of terms, keeps per-thread float64 sums, reduces a block in a
-// fixed shuffle order, writes one partial per block into caller-provided
-// scratch, and a second kernel sums the partials in a fixed order, so the
-// result is bitwise reproducible run to run.
+// per group of terms, keeps per-thread float64 sums (complex64 states: float32
+// chunk sums folded into float64, see Acc), reduces a block in a fixed
+// shuffle order, writes one partial per block into caller-provided scratch,
+// and a second kernel sums the partials in a fixed order, so the result is
+// bitwise reproducible run to run.
 #include <cstring>
 #include <vector>
 
@@ -58,7 +59,8 @@ struct PauliGroup {
 };
 
 // Re( i^ny * z )
-__device__ __forceinline__ double re_iny(double re, double im, int ny) {
+template <typename R>
+__device__ __forceinline__ R re_iny(R re, R im, int ny) {
     switch (ny & 3) {
         case 0: return re;
         case 1: return -im;
@@ -76,18 +78,17 @@ __global__ void __launch_bounds__(kRedThreads) pauli_group_kernel(const cplx<T>*
     const int64_t b = blockIdx.y;
     const cplx<T>* s = sv + b * sv_stride;
     const int nblk = gridDim.x;
-    double acc[NT];
-#pragma unroll
-    for (int j = 0; j < NT; ++j) acc[j] = 0.0;
+    Acc<T, NT> acc;
     const uint64_t stride = uint64_t(nblk) * blockDim.x;
     if (g.xmask == 0) {
         const uint64_t len = uint64_t(1) << n;
         for (uint64_t x = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; x < len; x += stride) {
             const cplx<T> a = s[x];
-            const double p = double(a.x) * double(a.x) + double(a.y) * double(a.y);
+            const T p = a.x * a.x + a.y * a.y;
 #pragma unroll
             for (int j = 0; j < NT; ++j)
-                if (j < g.nterms) acc[j] += (__popcll(x & g.zmask[j]) & 1) ? -p : p;
+                if (j < g.nterms) acc.add(j, (__popcll(x & g.zmask[j]) & 1) ? -p : p);
+            acc.step();
         }
     } else {
         // visit each pair {x, x ^ xmask} once: x has a zero at the top bit of xmask
@@ -98,21 +99,23 @@ __global__ void __launch_bounds__(kRedThreads) pauli_group_kernel(const cplx<T>*
             const uint64_t y = x ^ g.xmask;
             const cplx<T> a = s[x], c = s[y];
             // v = conj(psi[y]) psi[x] contributes at x; conj(v) contributes at y
-            const double vr = double(c.x) * a.x + double(c.y) * a.y;
-            const double vi = double(c.x) * a.y - double(c.y) * a.x;
+            const T vr = c.x * a.x + c.y * a.y;
+            const T vi = c.x * a.y - c.y * a.x;
 #pragma unroll
             for (int j = 0; j < NT; ++j)
                 if (j < g.nterms) {
-                    const double tx = re_iny(vr, vi, g.ny[j]);
-                    const double ty = re_iny(vr, -vi, g.ny[j]);
-                    acc[j] += ((__popcll(x & g.zmask[j]) & 1) ? -tx : tx) + ((__popcll(y & g.zmask[j]) & 1) ? -ty : ty);
+                    const T tx = re_iny<T>(vr, vi, g.ny[j]);
+                    const T ty = re_iny<T>(vr, -vi, g.ny[j]);
+                    acc.add(j, ((__popcll(x & g.zmask[j]) & 1) ? -tx : tx) + ((__popcll(y & g.zmask[j]) & 1) ? -ty : ty));
                 }
+            acc.step();
         }
     }
+    acc.flush();
 #pragma unroll
-    for (int j = 0; j < NT; ++j) acc[j] *= g.coeff[j < g.nterms ? j : 0];
+    for (int j = 0; j < NT; ++j) acc.d[j] *= g.coeff[j < g.nterms ? j : 0];
     double* dst = partials + (int64_t(b) * nslots + g.slot0) * nblk + blockIdx.x;
-    block_reduce_store<NT>(acc, dst, nblk, g.nterms);
+    block_reduce_store<NT>(acc.d, dst, nblk, g.nterms);
 }
 
 // out[b * nslots + t] = coeff[t] * sum_blk partials[(b * nslots + t) * nblk + blk]
@@ -135,12 +138,14 @@ __global__ void __launch_bounds__(kRedThreads) norm2_kernel(const cplx<T>* __res
                                                             double* __restrict__ partials) {
     const cplx<T>* s = sv + int64_t(blockIdx.y) * sv_stride;
     const uint64_t len = uint64_t(1) << n, stride = uint64_t(gridDim.x) * blockDim.x;
-    double acc[1] = {0.0};
+    Acc<T, 1> acc;
     for (uint64_t x = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; x < len; x += stride) {
         const cplx<T> a = s[x];
-        acc[0] += double(a.x) * a.x + double(a.y) * a.y;
+        acc.add(0, a.x * a.x + a.y * a.y);
+        acc.step();
     }
-    block_reduce_store<1>(acc, partials + int64_t(blockIdx.y) * gridDim.x + blockIdx.x, gridDim.x);
+    acc.flush();
+    block_reduce_store<1>(acc.d, partials + int64_t(blockIdx.y) * gridDim.x + blockIdx.x, gridDim.x);
 }
 
 // <a|b> = sum conj(a) b (slots 0, 1 = real, imaginary).
@@ -151,13 +156,15 @@ __global__ void __launch_bounds__(kRedThreads) inner_kernel(const cplx<T>* __res
     const cplx<T>* x = a + b * stride_ab;
     const cplx<T>* y = bv + b * stride_ab;
     const uint64_t len = uint64_t(1) << n, stride = uint64_t(gridDim.x) * blockDim.x;
-    double acc[2] = {0.0, 0.0};
+    Acc<T, 2> acc;
     for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < len; i += stride) {
         const cplx<T> u = x[i], v = y[i];
-        acc[0] += double(u.x) * v.x + double(u.y) * v.y;
-        acc[1] += double(u.x) * v.y - double(u.y) * v.x;
+        acc.add(0, u.x * v.x + u.y * v.y);
+        acc.add(1, u.x * v.y - u.y * v.x);
+        acc.step();
     }
-    block_reduce_store<2>(acc, partials + (b * 2) * gridDim.x + blockIdx.x, gridDim.x);
+    acc.flush();
+    block_reduce_store<2>(acc.d, partials + (b * 2) * gridDim.x + blockIdx.x, gridDim.x);
 }
 
 // Partial overlap on k <= 2 sites: slots 2*(r*D+c) (+1) = re/im of sum a[r,rest] conj(b[c,rest]).
@@ -176,9 +183,7 @@ __global__ void __launch_bounds__(kRedThreads) overlap_kernel(const cplx<T>* __r
     const cplx<T>* x = a + b * stride_ab;
     const cplx<T>* y = bv + b * stride_ab;
     const uint64_t groups = uint64_t(1) << (o.n - K), stride = uint64_t(gridDim.x) * blockDim.x;
-    double acc[2 * D * D];
-#pragma unroll
-    for (int j = 0; j < 2 * D * D; ++j) acc[j] = 0.0;
+    Acc<T, 2 * D * D> acc;
     for (uint64_t g = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; g < groups; g += stride) {
         uint64_t base = g;
 #pragma unroll
@@ -194,11 +199,13 @@ __global__ void __launch_bounds__(kRedThreads) overlap_kernel(const cplx<T>* __r
 #pragma unroll
             for (int c = 0; c < D; ++c) {
                 // u[r] * conj(v[c])
-                acc[2 * (r * D + c)] += double(u[r].x) * v[c].x + double(u[r].y) * v[c].y;
-                acc[2 * (r * D + c) + 1] += double(u[r].y) * v[c].x - double(u[r].x) * v[c].y;
+                acc.add(2 * (r * D + c), u[r].x * v[c].x + u[r].y * v[c].y);
+                acc.add(2 * (r * D + c) + 1, u[r].y * v[c].x - u[r].x * v[c].y);
             }
+        acc.step();
     }
-    block_reduce_store<2 * D * D>(acc, partials + (b * 2 * D * D) * gridDim.x + blockIdx.x, gridDim.x);
+    acc.flush();
+    block_reduce_store<2 * D * D>(acc.d, partials + (b * 2 * D * D) * gridDim.x + blockIdx.x, gridDim.x);
 }
 
 // DM: Tr(rho P) for one Pauli group: sum_x rho[x, x ^ xmask] i^ny (-1)^{pop(x & zmask)}.
@@ -209,21 +216,21 @@ __global__ void __launch_bounds__(kRedThreads) dm_pauli_kernel(const cplx<T>* __
     const int64_t b = blockIdx.y;
     const cplx<T>* r = rho + b * stride;
     const uint64_t dim = uint64_t(1) << n, step = uint64_t(gridDim.x) * blockDim.x;
-    double acc[NT];
-#pragma unroll
-    for (int j = 0; j < NT; ++j) acc[j] = 0.0;
+    Acc<T, NT> acc;
     for (uint64_t x = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; x < dim; x += step) {
         const cplx<T> v = r[(x << n) | (x ^ g.xmask)];
 #pragma unroll
         for (int j = 0; j < NT; ++j)
             if (j < g.nterms) {
-                const double t = re_iny(double(v.x), double(v.y), g.ny[j]);
-                acc[j] += (__popcll(x & g.zmask[j]) & 1) ? -t : t;
+                const T t = re_iny<T>(v.x, v.y, g.ny[j]);
+                acc.add(j, (__popcll(x & g.zmask[j]) & 1) ? -t : t);
             }
+        acc.step();
     }
+    acc.flush();
 #pragma unroll
-    for (int j = 0; j < NT; ++j) acc[j] *= g.coeff[j < g.nterms ? j : 0];
-    block_reduce_store<NT>(acc, partials + (int64_t(b) * nslots + g.slot0) * gridDim.x + blockIdx.x, gridDim.x,
+    for (int j = 0; j < NT; ++j) acc.d[j] *= g.coeff[j < g.nterms ? j : 0];
+    block_reduce_store<NT>(acc.d, partials + (int64_t(b) * nslots + g.slot0) * gridDim.x + blockIdx.x, gridDim.x,
                            g.nterms);
 }
 
@@ -241,21 +248,23 @@ __global__ void __launch_bounds__(kRedThreads) dm_product_kernel(const cplx<T>* 
     const cplx<T>* r = rho + int64_t(blockIdx.y) * stride;
     const uint64_t len = uint64_t(1) << (2 * n), step = uint64_t(gridDim.x) * blockDim.x;
     const uint64_t lo = (uint64_t(1) << n) - 1;
-    double acc[1] = {0.0};
+    Acc<T, 1> acc;
     for (uint64_t v = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; v < len; v += step) {
         const uint64_t y = v >> n, x = v & lo;  // entry rho[y, x]
-        double wr = 1.0, wi = 0.0;
+        T wr = T(1), wi = T(0);
         for (int q = 0; q < n; ++q) {
             const int xa = int((x >> (n - 1 - q)) & 1), yb = int((y >> (n - 1 - q)) & 1);
             const double2 c = p.o[q][2 * xa + yb];
-            const double tr = wr * c.x - wi * c.y;
-            wi = wr * c.y + wi * c.x;
+            const T tr = wr * T(c.x) - wi * T(c.y);
+            wi = wr * T(c.y) + wi * T(c.x);
             wr = tr;
         }
         const cplx<T> e = r[v];
-        acc[0] += wr * double(e.x) - wi * double(e.y);
+        acc.add(0, wr * e.x - wi * e.y);
+        acc.step();
     }
-    block_reduce_store<1>(acc, partials + int64_t(blockIdx.y) * gridDim.x + blockIdx.x, gridDim.x);
+    acc.flush();
+    block_reduce_store<1>(acc.d, partials + int64_t(blockIdx.y) * gridDim.x + blockIdx.x, gridDim.x);
 }
 
 template <typename T>
@@ -263,30 +272,50 @@ __global__ void __launch_bounds__(kRedThreads) dm_trace_kernel(const cplx<T>* __
                                                                double* __restrict__ partials) {
     const cplx<T>* r = rho + int64_t(blockIdx.y) * stride;
     const uint64_t dim = uint64_t(1) << n, step = uint64_t(gridDim.x) * blockDim.x;
-    double acc[1] = {0.0};
-    for (uint64_t x = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; x < dim; x += step)
-        acc[0] += double(r[(x << n) | x].x);
-    block_reduce_store<1>(acc, partials + int64_t(blockIdx.y) * gridDim.x + blockIdx.x, gridDim.x);
+    Acc<T, 1> acc;
+    for (uint64_t x = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; x < dim; x += step) {
+        acc.add(0, r[(x << n) | x].x);
+        acc.step();
+    }
+    acc.flush();
+    block_reduce_store<1>(acc.d, partials + int64_t(blockIdx.y) * gridDim.x + blockIdx.x, gridDim.x);
 }
 
 // Adjoint reverse step for one gate U on K <= 2 sites, one pass over two vectors:
-//   phi <- U^dagger phi,  grad[r][c] += lam[r] * conj(phi_new[c]),  lam <- U^dagger lam
-// (slots 2*(r*D+c) (+1) = re/im; the host scales by 2, torch's convention).
+//   phi <- U^dagger phi,  lam <- U^dagger lam, and, by GradMode,
+//   kGradNone:     nothing else;
+//   kGradMatrix:   grad[r][c] += lam[r] * conj(phi_new[c]) (slots 2*(r*D+c) (+1) =
+//                  re/im; the host scales by 2, torch's convention);
+//   kGradRotation: for U = exp(-i theta P) (P^2 = I): one slot,
+//                  Im sum_r conj(lam[r]) (P phi)[r] with phi, lam taken at the
+//                  gate's output (before the uncompute). Since U commutes with P,
+//                  Re sum_rc conj(G[r,c]) dU/dtheta[r,c] = 2 Im <lam|P|phi> for
+//                  G = 2 sum lam[r] conj(phi_new[c]): the angle's gradient
+//                  without the 2 D^2 matrix-gradient slots.
+enum GradMode { kGradNone = 0, kGradMatrix = 1, kGradRotation = 2 };
+
 struct AdjointArgs {
     int n;
     int sorted[2];
     uint32_t off[4];
-    int want_grad;
     int64_t sv_stride;  // batch: state b at phi + b * sv_stride (and lam)
     int64_t op_stride;  // batch: its gate matrix at U + b * op_stride
+    int gcol[4];        // kGradRotation: P[r][gcol[r]] = gval[r], the only nonzero of row r
+    double2 gval[4];
 };
 
-template <typename T, int K>
+template <int K, int MODE>
+__host__ __device__ constexpr int adjoint_slots() {
+    return MODE == kGradMatrix ? (2 << (2 * K)) : 1;
+}
+
+template <typename T, int K, int MODE>
 __global__ void __launch_bounds__(kRedThreads) adjoint_kernel(cplx<T>* __restrict__ phi, cplx<T>* __restrict__ lam,
                                                               const cplx<T>* __restrict__ U,
                                                               const __grid_constant__ AdjointArgs a,
                                                               double* __restrict__ partials) {
     constexpr int D = 1 << K;
+    constexpr int NS = adjoint_slots<K, MODE>();
     using C = cplx<T>;
     const int64_t bidx = blockIdx.y;  // state of the batch
     phi += bidx * a.sv_stride;
@@ -301,9 +330,14 @@ __global__ void __launch_bounds__(kRedThreads) adjoint_kernel(cplx<T>* __restric
             ud[r * D + c] = mk<T>(u.x, -u.y);
         }
     const uint64_t groups = uint64_t(1) << (a.n - K), stride = uint64_t(gridDim.x) * blockDim.x;
-    double acc[2 * D * D];
+    C gv[D];  // kGradRotation: the nonzero of each row of P, in the state's precision
+    int gc[D];
 #pragma unroll
-    for (int j = 0; j < 2 * D * D; ++j) acc[j] = 0.0;
+    for (int r = 0; r < D; ++r) {
+        gv[r] = mk<T>(T(a.gval[r].x), T(a.gval[r].y));
+        gc[r] = a.gcol[r];
+    }
+    Acc<T, NS> acc;
     for (uint64_t g = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; g < groups; g += stride) {
         uint64_t base = g;
 #pragma unroll
@@ -325,14 +359,29 @@ __global__ void __launch_bounds__(kRedThreads) adjoint_kernel(cplx<T>* __restric
             pn[r] = x;
             ln[r] = y;
         }
-        if (a.want_grad) {
+        if constexpr (MODE == kGradMatrix) {
 #pragma unroll
             for (int r = 0; r < D; ++r)
 #pragma unroll
                 for (int c = 0; c < D; ++c) {
-                    acc[2 * (r * D + c)] += double(l[r].x) * pn[c].x + double(l[r].y) * pn[c].y;
-                    acc[2 * (r * D + c) + 1] += double(l[r].y) * pn[c].x - double(l[r].x) * pn[c].y;
+                    acc.add(2 * (r * D + c), l[r].x * pn[c].x + l[r].y * pn[c].y);
+                    acc.add(2 * (r * D + c) + 1, l[r].y * pn[c].x - l[r].x * pn[c].y);
                 }
+            acc.step();
+        } else if constexpr (MODE == kGradRotation) {
+            T s = T(0);
+#pragma unroll
+            for (int r = 0; r < D; ++r) {
+                C pc = p[0];  // p[gc[r]] by selects (no dynamic register indexing)
+#pragma unroll
+                for (int c = 1; c < D; ++c)
+                    if (gc[r] == c) pc = p[c];
+                C w = mk<T>(0, 0);
+                cfma(w, gv[r], pc);
+                s += l[r].x * w.y - l[r].y * w.x;  // Im(conj(l) w)
+            }
+            acc.add(0, s);
+            acc.step();
         }
 #pragma unroll
         for (int r = 0; r < D; ++r) {
@@ -341,7 +390,10 @@ __global__ void __launch_bounds__(kRedThreads) adjoint_kernel(cplx<T>* __restric
         }
     }
     // partials[(b * slots + slot) * nblk + blk], the layout finish() sums
-    if (a.want_grad) block_reduce_store<2 * D * D>(acc, partials + bidx * (2 * D * D) * gridDim.x + blockIdx.x, gridDim.x);
+    if constexpr (MODE != kGradNone) {
+        acc.flush();
+        block_reduce_store<NS>(acc.d, partials + bidx * NS * gridDim.x + blockIdx.x, gridDim.x);
+    }
 }
 
 // out = sum_t coeff[t] P_t sv
@@ -359,24 +411,25 @@ __global__ void __launch_bounds__(256) pauli_apply_kernel(const cplx<T>* __restr
     const cplx<T>* s = sv + b * stride;
     cplx<T>* o = out + b * stride;
     const uint64_t len = uint64_t(1) << a.n, step = uint64_t(gridDim.x) * blockDim.x;
+    // computed in the state's own precision (the sum is rounded to it anyway)
     for (uint64_t y = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; y < len; y += step) {
-        double ar = 0, ai = 0;
+        T ar = T(0), ai = T(0);
         for (int t = 0; t < a.nterms; ++t) {
             const uint64_t x = y ^ a.xmask[t];
             const cplx<T> v = s[x];
             // P|x> = i^ny (-1)^{pop(x & z)} |x ^ xmask> ; contribution to out[y]
-            double cr = double(v.x), ci = double(v.y);
+            T cr = v.x, ci = v.y;
             switch (a.ny[t] & 3) {
-                case 1: { double t2 = cr; cr = -ci; ci = t2; } break;
+                case 1: { T t2 = cr; cr = -ci; ci = t2; } break;
                 case 2: cr = -cr; ci = -ci; break;
-                case 3: { double t2 = cr; cr = ci; ci = -t2; } break;
+                case 3: { T t2 = cr; cr = ci; ci = -t2; } break;
                 default: break;
             }
-            const double f = ((__popcll(x & a.zmask[t]) & 1) ? -a.coeff[t] : a.coeff[t]);
+            const T f = T((__popcll(x & a.zmask[t]) & 1) ? -a.coeff[t] : a.coeff[t]);
             ar += f * cr;
             ai += f * ci;
         }
-        o[y] = mk<T>(T(ar), T(ai));
+        o[y] = mk<T>(ar, ai);
     }
 }
 
@@ -641,9 +694,24 @@ extern "C" int qgb_pauli_apply(const void* sv, void* out, int dtype, int n, cons
     return check_launch("pauli apply");
 }
 
-extern "C" int qgb_adjoint_step_batched(void* phi, void* lam, int dtype, int n, const int* indices, int k,
-                                        const void* op, int64_t op_stride, int64_t batch, int64_t sv_stride,
-                                        double* grad_out, void* scratch, size_t scratch_bytes, void* stream) {
+namespace {
+
+template <int MODE>
+void launch_adjoint(void* phi, void* lam, int dtype, int k, const void* op, const AdjointArgs& a, dim3 grid,
+                    double* part, cudaStream_t st) {
+    if (dtype == QGB_C64) {
+        if (k == 1) adjoint_kernel<float, 1, MODE><<<grid, kRedThreads, 0, st>>>((float2*)phi, (float2*)lam, (const float2*)op, a, part);
+        else adjoint_kernel<float, 2, MODE><<<grid, kRedThreads, 0, st>>>((float2*)phi, (float2*)lam, (const float2*)op, a, part);
+    } else {
+        if (k == 1) adjoint_kernel<double, 1, MODE><<<grid, kRedThreads, 0, st>>>((double2*)phi, (double2*)lam, (const double2*)op, a, part);
+        else adjoint_kernel<double, 2, MODE><<<grid, kRedThreads, 0, st>>>((double2*)phi, (double2*)lam, (const double2*)op, a, part);
+    }
+}
+
+// Shared checks and launch of the three adjoint-step forms.
+int adjoint_impl(void* phi, void* lam, int dtype, int n, const int* indices, int k, const void* op, int64_t op_stride,
+                 int64_t batch, int64_t sv_stride, const double* generator, double* grad_out, void* scratch,
+                 size_t scratch_bytes, cudaStream_t st) {
     int rc = check_common(phi, dtype, n, batch, sv_stride);
     if (rc) return rc;
     if (!lam || !op || !indices) return set_error(QGB_EINVAL, "null pointer");
@@ -655,12 +723,12 @@ extern "C" int qgb_adjoint_step_batched(void* phi, void* lam, int dtype, int n, 
     const char* lb = static_cast<const char*>(lam);
     const int64_t esz = dtype == QGB_C64 ? 8 : 16;
     if (pb < lb + span * esz && lb < pb + span * esz) return set_error(QGB_EINVAL, "the two batches overlap");
-    const int slots = 2 << (2 * k);
-    if (grad_out && (!scratch || scratch_bytes < red_scratch(n, slots, batch)))
+    const int mode = !grad_out ? kGradNone : (generator ? kGradRotation : kGradMatrix);
+    const int slots = mode == kGradMatrix ? 2 << (2 * k) : 1;
+    if (mode != kGradNone && (!scratch || scratch_bytes < red_scratch(n, slots, batch)))
         return set_error(QGB_ESCRATCH, "scratch too small");
     AdjointArgs a{};
     a.n = n;
-    a.want_grad = grad_out != nullptr;
     a.sv_stride = batch > 1 ? sv_stride : 0;
     a.op_stride = batch > 1 ? op_stride : 0;
     int pos[2];
@@ -674,19 +742,47 @@ extern "C" int qgb_adjoint_step_batched(void* phi, void* lam, int dtype, int n, 
         if (a.sorted[0] > a.sorted[1]) { const int t = a.sorted[0]; a.sorted[0] = a.sorted[1]; a.sorted[1] = t; }
     }
     for (int r = 0; r < (1 << k); ++r) a.off[r] = uint32_t(matrix_offset(r, pos, k));
-    cudaStream_t st = (cudaStream_t)stream;
+    if (generator) {  // a Pauli product: exactly one nonzero per row
+        const int d = 1 << k;
+        for (int r = 0; r < d; ++r) {
+            int nz = 0;
+            for (int c = 0; c < d; ++c) {
+                const double re = generator[2 * (r * d + c)], im = generator[2 * (r * d + c) + 1];
+                if (re != 0.0 || im != 0.0) {
+                    ++nz;
+                    a.gcol[r] = c;
+                    a.gval[r] = make_double2(re, im);
+                }
+            }
+            if (nz != 1) return set_error(QGB_EINVAL, "generator row %d has %d nonzeros (a Pauli product has one)", r, nz);
+        }
+    }
     const dim3 grid(unsigned(red_blocks(n)), unsigned(batch));
     double* part = (double*)scratch;
-    if (dtype == QGB_C64) {
-        if (k == 1) adjoint_kernel<float, 1><<<grid, kRedThreads, 0, st>>>((float2*)phi, (float2*)lam, (const float2*)op, a, part);
-        else adjoint_kernel<float, 2><<<grid, kRedThreads, 0, st>>>((float2*)phi, (float2*)lam, (const float2*)op, a, part);
-    } else {
-        if (k == 1) adjoint_kernel<double, 1><<<grid, kRedThreads, 0, st>>>((double2*)phi, (double2*)lam, (const double2*)op, a, part);
-        else adjoint_kernel<double, 2><<<grid, kRedThreads, 0, st>>>((double2*)phi, (double2*)lam, (const double2*)op, a, part);
-    }
+    if (mode == kGradNone) launch_adjoint<kGradNone>(phi, lam, dtype, k, op, a, grid, part, st);
+    else if (mode == kGradMatrix) launch_adjoint<kGradMatrix>(phi, lam, dtype, k, op, a, grid, part, st);
+    else launch_adjoint<kGradRotation>(phi, lam, dtype, k, op, a, grid, part, st);
     if ((rc = check_launch("adjoint step"))) return rc;
-    if (!grad_out) return QGB_OK;
+    if (mode == kGradNone) return QGB_OK;
     return finish(part, red_blocks(n), slots, batch, nullptr, grad_out, st);
+}
+
+}  // namespace
+
+extern "C" int qgb_adjoint_step_batched(void* phi, void* lam, int dtype, int n, const int* indices, int k,
+                                        const void* op, int64_t op_stride, int64_t batch, int64_t sv_stride,
+                                        double* grad_out, void* scratch, size_t scratch_bytes, void* stream) {
+    return adjoint_impl(phi, lam, dtype, n, indices, k, op, op_stride, batch, sv_stride, nullptr, grad_out, scratch,
+                        scratch_bytes, (cudaStream_t)stream);
+}
+
+extern "C" int qgb_adjoint_step_rotation(void* phi, void* lam, int dtype, int n, const int* indices, int k,
+                                         const void* op, int64_t op_stride, const double* generator, int64_t batch,
+                                         int64_t sv_stride, double* grad_out, void* scratch, size_t scratch_bytes,
+                                         void* stream) {
+    if (!generator || !grad_out) return set_error(QGB_EINVAL, "null generator or output");
+    return adjoint_impl(phi, lam, dtype, n, indices, k, op, op_stride, batch, sv_stride, generator, grad_out, scratch,
+                        scratch_bytes, (cudaStream_t)stream);
 }
 
 extern "C" int qgb_adjoint_step(void* phi, void* lam, int dtype, int n, const int* indices, int k, const void* op,

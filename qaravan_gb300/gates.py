@@ -224,6 +224,7 @@ class ParamGate(Gate):
         else:
             self.angles = args
             self.matrix = self.construct_matrix()
+            self._angle_matrix = self.matrix  # identity marks "matrix still the one built from the angles"
 
     def __str__(self):
         return f"{self.name} gate on site(s) {self.indices} with angle(s) {self.angles}"
@@ -237,7 +238,19 @@ class ParamGate(Gate):
     def solve_angles(self):
         return "unsolved"
 
+    def built_from_angles(self):
+        """True while ``matrix`` is the one constructed from ``angles`` (not
+        replaced by ``update_matrix`` / ``Circuit.update_gate``)."""
+        return self.matrix is not None and self.matrix is getattr(self, "_angle_matrix", None)
+
     def shallow_copy(self):
+        # The reference rebuilds the gate from its angles (core/param_gates.py:48-49).
+        # While the matrix is still the one built from those angles the rebuild
+        # would recompute the same values, so the copy shares it instead.
+        if self.built_from_angles():
+            g = copy.copy(self)
+            g.indices = list(self.indices)
+            return g
         return type(self)(self.indices, *self.angles)
 
     def _expm(self, gen_np, gen_t):

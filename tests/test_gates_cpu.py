@@ -1,0 +1,45 @@
+"""Gate-object behaviour that decides numbers: rotation matrices against the
+closed form expm(-i t P) = cos t I - i sin t P, and Circuit.copy() semantics of
+parametrised gates (a copy is rebuilt from the angles, so a matrix replaced by
+update_gate does not survive the copy; an untouched matrix is shared)."""
+import numpy as np
+import torch
+
+from qaravan_gb300.circuits import Circuit
+from qaravan_gb300.gates import RX, RXX, RY, RYY, RZ, RZZ
+
+PX = np.array([[0, 1], [1, 0]], dtype=complex)
+PY = np.array([[0, -1j], [1j, 0]])
+PZ = np.diag([1.0, -1.0]).astype(complex)
+GEN = {RX: PX, RY: PY, RZ: PZ, RXX: np.kron(PX, PX), RYY: np.kron(PY, PY), RZZ: np.kron(PZ, PZ)}
+
+
+def test_rotation_matrices_closed_form():
+    for cls, P in GEN.items():
+        idx = [0] if P.shape[0] == 2 else [0, 1]
+        for t in (0.3, -1.7, 2.9):
+            want = np.cos(t) * np.eye(P.shape[0]) - 1j * np.sin(t) * P
+            assert np.max(np.abs(np.asarray(cls(idx, t).matrix) - want)) < 1e-14
+            tm = cls(idx, torch.tensor(t, dtype=torch.float64)).matrix
+            assert np.max(np.abs(tm.detach().numpy() - want)) < 1e-9  # torch.linalg.matrix_exp accuracy
+
+
+def test_copy_shares_angle_built_matrix_and_keeps_autograd():
+    th = torch.tensor([0.4, -0.9], dtype=torch.float64, requires_grad=True)
+    c = Circuit([RY([0], th[0]), RZZ([0, 1], th[1])], n=2)
+    c2 = c.copy()
+    for g, h in zip(c.gate_list, c2.gate_list):
+        assert h.matrix is g.matrix and h.built_from_angles()
+        assert h.indices == g.indices and h.indices is not g.indices
+    c2.gate_list[0].matrix.real.sum().backward()
+    assert th.grad is not None and th.grad[0] != 0
+
+
+def test_copy_rebuilds_a_replaced_matrix_from_angles():
+    c = Circuit([RX([0], 0.7), RY([1], 0.2)], n=2)
+    new = np.eye(2, dtype=complex) * 1j
+    c.update_gate(0, new)
+    assert not c.gate_list[0].built_from_angles()
+    c2 = c.copy()
+    assert np.max(np.abs(np.asarray(c2.gate_list[0].matrix) - np.asarray(RX([0], 0.7).matrix))) < 1e-15
+    assert c2.gate_list[0].built_from_angles()

@@ -124,3 +124,79 @@ def test_adjoint_memory_is_state_sized():
     state = 2 ** n * 8
     assert peak < 5 * state, peak / state
     assert np.all(np.isfinite(th.grad.numpy()))
+
+
+def _oracle_loss_grad(gates, n, terms, leaves):
+    """sum_t c_t <psi|P_t|psi> through the oracle's torch op_action with torch
+    autograd (matrix_exp included), and the gradients of ``leaves``."""
+    st = torch.zeros([2] * n, dtype=torch.complex128)
+    st.view(-1)[0] = 1
+    for layer in ref.construct_layers(gates):
+        for gate in layer:
+            m = gate.matrix if torch.is_tensor(gate.matrix) else torch.tensor(np.asarray(gate.matrix), dtype=torch.complex128)
+            st = ref.op_action_torch(m, gate.indices, st)
+    pauli = {"x": [[0, 1], [1, 0]], "y": [[0, -1j], [1j, 0]], "z": [[1, 0], [0, -1]]}
+    e = 0
+    for c, s in terms:
+        v = st
+        for q, ch in enumerate(s):
+            if ch != "i":
+                v = ref.op_action_torch(torch.tensor(pauli[ch], dtype=torch.complex128), [q], v)
+        e = e + c * torch.vdot(st.reshape(-1), v.reshape(-1)).real
+    e.backward()
+    return float(e), [l.grad.numpy().copy() for l in leaves]
+
+
+def _mixed_circuit(th, free):
+    """Rotations on angles of ``th`` (one angle used twice) and a dense gate whose
+    matrix ``free`` is itself a leaf."""
+    from qaravan_gb300.circuits import Circuit
+    from qaravan_gb300.gates import CNOT, Gate, RX, RXX, RY, RYY, RZ, RZZ
+    n = 5
+    gates = [RX([0], th[0]), RY([1], th[1]), RZ([2], th[2]), RXX([0, 1], th[3]), RYY([2, 3], th[4]),
+             RZZ([3, 4], th[5]), Gate("free", [1, 2], free), CNOT([2, 1], n), RX([4], th[0]), RY([3], th[6])]
+    return Circuit(gates, n=n), n
+
+
+@pytest.mark.parametrize("when", ["before_sim", "inside_sim"])
+def test_rotation_angles_mixed_with_matrix_leaves_and_replaced_gates(when):
+    """Angles and matrix leaves get the oracle's autograd gradients. A rotation
+    whose matrix is replaced (update_gate) before the simulator is built comes
+    back from the angles, as the reference's simulator copies the circuit
+    (core/base_sim.py:11, core/param_gates.py:48-49); one replaced in the
+    simulator's own built circuit keeps the new matrix and its angle gets no
+    gradient from it."""
+    from qaravan_gb300 import StatevectorSim
+    from qaravan_gb300.adjoint import adjoint_energy
+    from qaravan_gb300.hamiltonians import TFI
+    rng = np.random.default_rng(3)
+    p = rng.uniform(-2, 2, size=7)
+    q, _ = np.linalg.qr(rng.normal(size=(4, 4)) + 1j * rng.normal(size=(4, 4)))
+    rep = np.linalg.qr(rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2)))[0]
+    terms = TFI(5, 1, 0.7).pauli_sum()
+    th = torch.tensor(p, requires_grad=True)
+    fr = torch.tensor(q, requires_grad=True)
+    c, n = _mixed_circuit(th, fr)
+    last = len(c.gate_list) - 1
+    if when == "before_sim":
+        c.update_gate(last, rep)
+        sim = StatevectorSim(c, dtype=torch.complex128)
+    else:
+        sim = StatevectorSim(c, dtype=torch.complex128)
+        sim.circ.construct_layers()
+        sim.circ.update_gate(last, rep)
+    e = adjoint_energy(sim, terms)
+    e.backward()
+    th2 = torch.tensor(p, requires_grad=True)
+    fr2 = torch.tensor(q, requires_grad=True)
+    c2, _ = _mixed_circuit(th2, fr2)
+    if when == "inside_sim":
+        c2.update_gate(last, rep)
+    e2, (g_th, g_fr) = _oracle_loss_grad(c2.gate_list, n, terms, [th2, fr2])
+    assert abs(float(e) - e2) < 1e-12
+    assert np.max(np.abs(th.grad.numpy() - g_th)) < 1e-9  # matrix_exp's own derivative error is ~1e-10
+    if when == "inside_sim":
+        assert g_th[6] == 0 and th.grad[6] == 0
+    else:
+        assert abs(g_th[6]) > 1e-3
+    assert np.max(np.abs(fr.grad.numpy() - g_fr)) < 1e-10

@@ -73,3 +73,39 @@ def test_batched_gradient_matches_parameter_shift():
     e, _ = ba.energy_and_grad(shifts, terms)
     e = e.cpu().numpy()
     assert np.max(np.abs(grad.cpu().numpy()[0] - (e[:P] - e[P:]))) < 1e-10
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.complex64, 2e-5), (torch.complex128, 1e-10)])
+def test_all_rotation_kinds_and_shared_parameters(dtype, tol):
+    """RX..RZZ, a fixed gate and a parameter used by two gates: batched gradients
+    against the parameter-shift rule, evaluated by shifting one gate's angle at a
+    time (a shared parameter's derivative is the sum over its gates)."""
+    from qaravan_gb300.adjoint import BatchedAnsatz
+    from qaravan_gb300.gates import CNOT
+    n = 6
+    cx = CNOT([2, 1], n)
+    gates = [("RX", [0], 0), ("RY", [1], 1), ("RZ", [2], 2), ("RXX", [0, 1], 3), ("RYY", [2, 3], 4),
+             ("RZZ", [3, 5], 5), ("fixed", list(cx.indices), np.asarray(cx.matrix)), ("RX", [4], 0),
+             ("RYY", [5, 1], 3), ("RY", [3], 6)]
+    terms = _tfi_terms(n) + [(0.4, "xyiiiz")]
+    ba = BatchedAnsatz(n, gates, dtype=dtype)
+    rng = np.random.default_rng(12)
+    P = 3
+    x = rng.uniform(-2, 2, size=(P, ba.nparams))
+    _, grad = ba.energy_and_grad(x, terms)
+    grad = grad.cpu().numpy()
+    # per-gate angles: a structure with one private parameter per rotation gate
+    rot = [i for i, g in enumerate(gates) if g[0] != "fixed"]
+    private = [(g[0], g[1], rot.index(i)) if g[0] != "fixed" else g for i, g in enumerate(gates)]
+    bp = BatchedAnsatz(n, private, dtype=torch.complex128)
+    for s in range(P):
+        th = np.array([x[s, gates[i][2]] for i in rot])
+        R = len(rot)
+        sh = np.concatenate([np.tile(th, (R, 1)) + np.pi / 4 * np.eye(R), np.tile(th, (R, 1)) - np.pi / 4 * np.eye(R)])
+        e, _ = bp.energy_and_grad(sh, terms)
+        e = e.cpu().numpy()
+        per_gate = e[:R] - e[R:]
+        want = np.zeros(ba.nparams)
+        for j, i in enumerate(rot):
+            want[gates[i][2]] += per_gate[j]
+        assert np.max(np.abs(grad[s] - want)) / np.max(np.abs(want)) < tol
