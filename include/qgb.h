@@ -63,6 +63,28 @@ typedef struct {
     int64_t op_mat[QGB_SWEEP_MAX_OPS];
 } qgb_sweep;
 
+/* One pass of the adjoint reverse sweep over a batch of (state, co-state)
+ * pairs, with the tile geometry of qgb_sweep. The ops are gates on 1 or 2
+ * sites listed in the order the reverse sweep meets them (the circuit's last
+ * gate first; gates on disjoint sites may be swapped). For op i and pair b:
+ * if op_out[i] >= 0, grad_out[op_out[i] * batch + b] = Im <lam_b| P_i |phi_b>
+ * at the gate's output, P_i the rotation generator given by one nonzero per
+ * row (column op_gen_col[i][r], value op_gen_val[i][r] = (re, im)); then
+ * phi_b and lam_b <- U^dagger, U the 2^k x 2^k matrix at
+ * mats + b * mat_stride + op_mat[i] elements (matrix order as qgb_sweep). */
+typedef struct {
+    int32_t low_bits;
+    int32_t n_high;
+    int32_t high_bits[QGB_SWEEP_MAX_HIGH];
+    int32_t n_ops;
+    int32_t op_k[QGB_SWEEP_MAX_OPS];
+    int32_t op_pos[QGB_SWEEP_MAX_OPS][2];
+    int64_t op_mat[QGB_SWEEP_MAX_OPS];
+    int32_t op_out[QGB_SWEEP_MAX_OPS];
+    int32_t op_gen_col[QGB_SWEEP_MAX_OPS][4];
+    double op_gen_val[QGB_SWEEP_MAX_OPS][4][2];
+} qgb_adjoint_sweep;
+
 int qgb_abi_version(void);
 const char* qgb_last_error(void);
 /* Reads and clears the device status word set by bounded waits; returns
@@ -235,6 +257,18 @@ int qgb_adjoint_step_batched(void* phi, void* lam, int dtype, int n, const int* 
 int qgb_adjoint_step_rotation(void* phi, void* lam, int dtype, int n, const int* indices, int k, const void* op,
                               int64_t op_stride, const double* generator, int64_t batch, int64_t sv_stride,
                               double* grad_out, void* scratch, size_t scratch_bytes, void* stream);
+
+/* Scratch bytes for qgb_adjoint_sweep_step (a function of the problem only). */
+size_t qgb_adjoint_sweep_scratch_bytes(int n, int tile_bits, int n_ops, int64_t batch);
+
+/* The adjoint reverse sweep for many gates per pass (qgb_adjoint_sweep): phi
+ * and lam (batch pairs at sv_stride elements, disjoint, 16-byte aligned) are
+ * read and written once per call instead of once per gate, and the rotation
+ * derivatives of qgb_adjoint_step_rotation come out for every op with
+ * op_out >= 0 (each slot written once, fixed summation order). */
+int qgb_adjoint_sweep_step(void* phi, void* lam, int dtype, int n, const qgb_adjoint_sweep* sweep, const void* mats,
+                           int64_t mat_stride, int64_t batch, int64_t sv_stride, double* grad_out, void* scratch,
+                           size_t scratch_bytes, void* stream);
 
 /* Parametrised gate matrices M(theta) = expm(-i theta P) = cos(theta) I -
  * i sin(theta) P (core/param_gates.py:21-80, no factor 1/2) for `nsets`

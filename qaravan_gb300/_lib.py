@@ -38,6 +38,22 @@ class Sweep(C.Structure):
     ]
 
 
+class AdjointSweep(C.Structure):
+    """Mirror of ``qgb_adjoint_sweep``."""
+    _fields_ = [
+        ("low_bits", C.c_int32),
+        ("n_high", C.c_int32),
+        ("high_bits", C.c_int32 * QGB_SWEEP_MAX_HIGH),
+        ("n_ops", C.c_int32),
+        ("op_k", C.c_int32 * QGB_SWEEP_MAX_OPS),
+        ("op_pos", (C.c_int32 * 2) * QGB_SWEEP_MAX_OPS),
+        ("op_mat", C.c_int64 * QGB_SWEEP_MAX_OPS),
+        ("op_out", C.c_int32 * QGB_SWEEP_MAX_OPS),
+        ("op_gen_col", (C.c_int32 * 4) * QGB_SWEEP_MAX_OPS),
+        ("op_gen_val", ((C.c_double * 2) * 4) * QGB_SWEEP_MAX_OPS),
+    ]
+
+
 _vp, _i, _i64, _u64, _sz, _dp, _cp, _ip = (C.c_void_p, C.c_int, C.c_int64, C.c_uint64, C.c_size_t,
                                            C.POINTER(C.c_double), C.c_char_p, C.POINTER(C.c_int))
 
@@ -56,6 +72,9 @@ SIGNATURES = {
     "qgb_adjoint_step_batched": (C.c_int, [_vp, _vp, _i, _i, _ip, _i, _vp, _i64, _i64, _i64, _vp, _vp, _sz, _vp]),
     "qgb_param_matrices": (C.c_int, [_vp, _vp, _i, _vp, _i, _i64, _vp, _i, _i64, _i64, _vp]),
     "qgb_param_grads": (C.c_int, [_vp, _vp, _i, _i64, _vp, C.c_double, _vp, _vp]),
+    "qgb_adjoint_sweep_scratch_bytes": (C.c_size_t, [_i, _i, _i, _i64]),
+    "qgb_adjoint_sweep_step": (C.c_int, [_vp, _vp, _i, _i, C.POINTER(AdjointSweep), _vp, _i64, _i64, _i64, _vp, _vp,
+                                         _sz, _vp]),
     "qgb_adjoint_step_rotation": (C.c_int, [_vp, _vp, _i, _i, _ip, _i, _vp, _i64, _dp, _i64, _i64, _vp, _vp, _sz, _vp]),
     "qgb_probs_scratch_bytes": (C.c_size_t, [_i, _i]),
     "qgb_outcome_probs": (C.c_int, [_vp, _i, _i, _ip, _i, _vp, _vp, _sz, _vp]),

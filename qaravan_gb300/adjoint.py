@@ -19,6 +19,8 @@ the energy function starts from ``lam = H psi`` and returns
 """
 from __future__ import annotations
 
+import ctypes as C
+
 import numpy as np
 import torch
 
@@ -78,11 +80,13 @@ class _Runner:
         return psi
 
     def reverse(self, psi, lam, mats, need):
-        """Reverse sweep from (psi, lam). ``need[i]``: falsy (no gradient), True
-        (the matrix block sum_rest lam[r] conj(phi[c])) or, for a rotation
-        exp(-i theta P), P as a ctypes double array (re, im pairs): the scalar
-        Im <lam|P|phi> at the gate's output. Returns per gate the complex128
-        block, the float, or None."""
+        """Reverse sweep from (psi, lam). ``need[i]``: False (no gradient), True
+        (the matrix block sum_rest lam[r] conj(phi[c])) or ("rotation", kind)
+        for a rotation exp(-i theta P): the scalar Im <lam|P|phi> at the gate's
+        output. Runs of gates without a matrix block go through tile passes
+        (``qgb_adjoint_sweep_step``, many gates per read of the two states);
+        a matrix block takes its own pass (``qgb_adjoint_step``). Returns per
+        gate the complex128 block, the float, or None."""
         L = _lib.lib()
         n = self.n
         st = _lib.stream_ptr(self.device)
@@ -96,26 +100,36 @@ class _Runner:
         isz = dev.element_size()
         offs = np.cumsum([0] + [m.numel() for m in mats])
         grads_dev = torch.empty(len(self.gates), 32, dtype=torch.float64, device=self.device)
-        nbytes = L.qgb_reduce_scratch_bytes(n, 32, 1)
+        tile = min(_tile_bits(self.dtype), n)
+        nbytes = max(L.qgb_reduce_scratch_bytes(n, 32, 1), L.qgb_adjoint_sweep_scratch_bytes(n, tile, 64, 1))
         scr = self.scratch.get(nbytes)
         base, gbase = dev.data_ptr(), grads_dev.data_ptr()
+        run = []
+
+        def flush():
+            for lo, high, ops in _plan_reverse(run, n, tile):
+                sw = _adjoint_sweep_struct(lo, high, [(bits, int(offs[i]), i * 32 if kind else -1, kind)
+                                                      for (i, kind), bits in ops])
+                _lib.check(L.qgb_adjoint_sweep_step(phi.data_ptr(), lam.data_ptr(), self.code, n, C.byref(sw), base,
+                                                    0, 1, 0, gbase, scr.data_ptr(), nbytes, st), "adjoint_sweep_step")
+            run.clear()
+
         for i in range(len(self.gates) - 1, -1, -1):
             k = len(self.gates[i].indices)
-            op = base + int(offs[i]) * isz
             want = need[i]
-            if want is not None and want is not False and want is not True:
-                _lib.check(L.qgb_adjoint_step_rotation(phi.data_ptr(), lam.data_ptr(), self.code, n, self._sites[i], k,
-                                                       op, 0, want, 1, 0, gbase + i * 32 * 8, scr.data_ptr(), nbytes,
-                                                       st), "adjoint_step_rotation")
+            if want is True:
+                flush()
+                _lib.check(L.qgb_adjoint_step(phi.data_ptr(), lam.data_ptr(), self.code, n, self._sites[i], k,
+                                              base + int(offs[i]) * isz, gbase + i * 32 * 8, scr.data_ptr(), nbytes,
+                                              st), "adjoint_step")
             else:
-                out = gbase + i * 32 * 8 if want else None
-                _lib.check(L.qgb_adjoint_step(phi.data_ptr(), lam.data_ptr(), self.code, n, self._sites[i], k, op, out,
-                                              scr.data_ptr(), nbytes, st), "adjoint_step")
+                run.append(((i, want[1] if want else 0), [n - 1 - q for q in self.gates[i].indices]))
+        flush()
         host = grads_dev.cpu().numpy()
         out = []
         for i, g in enumerate(self.gates):
             want = need[i]
-            if want is None or want is False:
+            if want is False:
                 out.append(None)
             elif want is True:
                 d = 2 ** len(g.indices)
@@ -138,6 +152,71 @@ _PY = np.array([[0, -1j], [1j, 0]], dtype=np.complex128)
 _PZ = np.array([[1, 0], [0, -1]], dtype=np.complex128)
 _GEN = {1: _PX, 2: _PY, 3: _PZ, 4: np.kron(_PX, _PX), 5: np.kron(_PY, _PY), 6: np.kron(_PZ, _PZ)}
 _GEN_C = {k: _lib.double_array(np.stack([m.real, m.imag], axis=-1).reshape(-1)) for k, m in _GEN.items()}
+# per kind: (column, value) of the one nonzero of each generator row
+_GEN_ROWS = {k: [(int(np.flatnonzero(m[r])[0]), complex(m[r, np.flatnonzero(m[r])[0]])) for r in range(m.shape[0])]
+             for k, m in _GEN.items()}
+
+
+def _tile_bits(dtype):
+    """Tile of the adjoint sweeps: state and co-state double-buffered in shared
+    memory (4 x 2^m amplitudes: 128 KiB at m = 12 for complex64, 11 for complex128)."""
+    return 12 if dtype == torch.complex64 else 11
+
+
+def _plan_reverse(items, nbits, tile_bits):
+    """Group the reverse sweep's gates into tile passes. ``items``: (payload, flat
+    bits in matrix order) in the order the sweep meets them. Gates on disjoint
+    bits may change order, which leaves every rotation derivative unchanged
+    (the moved gate commutes with the generator). Returns (L, high, [(payload,
+    bits)]) per pass."""
+    from types import SimpleNamespace
+    from .compiler import plan_sweeps
+    blocks = [SimpleNamespace(bits=list(b), payload=p) for p, b in items]
+    return [(L, high, [(blk.payload, blk.bits) for blk in taken])
+            for L, high, taken in plan_sweeps(blocks, nbits, tile_bits)]
+
+
+def _adjoint_sweep_struct(L, high, ops):
+    """``qgb_adjoint_sweep`` for one pass; ``ops``: (flat bits in matrix order,
+    matrix element offset, output slot or -1, rotation kind when the slot is set)."""
+    sw = _lib.AdjointSweep()
+    sw.low_bits = L
+    sw.n_high = len(high)
+    for i, b in enumerate(high):
+        sw.high_bits[i] = b
+    tpos = {b: b for b in range(L)}
+    tpos.update({b: L + h for h, b in enumerate(high)})
+    sw.n_ops = len(ops)
+    for i, (bits, off, out, kind) in enumerate(ops):
+        sw.op_k[i] = len(bits)
+        for j, b in enumerate(bits):
+            sw.op_pos[i][j] = tpos[b]
+        sw.op_mat[i] = int(off)
+        sw.op_out[i] = int(out)
+        if out >= 0:
+            for r, (c, v) in enumerate(_GEN_ROWS[int(kind)]):
+                sw.op_gen_col[i][r] = c
+                sw.op_gen_val[i][r][0] = v.real
+                sw.op_gen_val[i][r][1] = v.imag
+    return sw
+
+
+def _forward_sweep_struct(L, high, ops):
+    """``qgb_sweep`` for one forward pass; ``ops``: (flat bits in matrix order, matrix element offset)."""
+    sw = _lib.Sweep()
+    sw.low_bits = L
+    sw.n_high = len(high)
+    for i, b in enumerate(high):
+        sw.high_bits[i] = b
+    tpos = {b: b for b in range(L)}
+    tpos.update({b: L + h for h, b in enumerate(high)})
+    sw.n_ops = len(ops)
+    for i, (bits, off) in enumerate(ops):
+        sw.op_k[i] = len(bits)
+        for j, b in enumerate(bits):
+            sw.op_pos[i][j] = tpos[b]
+        sw.op_mat[i] = int(off)
+    return sw
 
 
 def _rotation_angle(g):
@@ -180,11 +259,11 @@ class _Inputs:
     def need(self, needs_input_grad, first):
         """Per gate, what the reverse sweep computes (``_Runner.reverse``), from
         the Function's ``needs_input_grad`` (angles at ``first``, other matrices
-        after): a rotation's generator, True for a matrix block, or False."""
+        after): ("rotation", kind), True for a matrix block, or False."""
         need = [False] * len(self.mats)
         if needs_input_grad[first]:
             for i, k in zip(self.rot, self.kinds):
-                need[i] = _GEN_C[int(k)]
+                need[i] = ("rotation", int(k))
         for j, i in enumerate(self.other):
             need[i] = bool(needs_input_grad[first + 1 + j])
         return need
@@ -283,9 +362,13 @@ class BatchedAnsatz:
     rotation, which also reduces its angle derivative 2 Im <lam|P|phi>, and
     ``qgb_adjoint_step_batched`` for a fixed gate) carries all sets together;
     ``qgb_param_grads`` sums the derivatives of the gates of each parameter.
+    With ``tile_bits`` > 0 (the default) both directions run as tile passes,
+    many gates per read of the states: the forward through ``qgb_apply_sweep``
+    with every set's own matrices, the reverse through
+    ``qgb_adjoint_sweep_step``; ``tile_bits=0`` runs one pass per gate.
     Memory: three states per set."""
 
-    def __init__(self, n, gates, nparams=None, dtype=torch.complex64, device="cuda"):
+    def __init__(self, n, gates, nparams=None, dtype=torch.complex64, device="cuda", tile_bits=None):
         self.n = int(n)
         self.dtype, self.device = dtype, torch.device(device)
         if self.device.type != "cuda":
@@ -320,7 +403,21 @@ class BatchedAnsatz:
         self._sites = [_lib.int_array(idx) for _, idx, _ in self.gates]
         self._need = [k != 0 for k in kinds]
         self._gens = [_GEN_C[k] if k else None for k in kinds]
+        self._kinds_h = kinds
         self.scratch = Scratch(self.device)
+        # tile passes (tile_bits=0: one pass per gate). Forward: the sweep kernel with
+        # every set's own matrices; reverse: the adjoint sweep, derivative slot = gate index.
+        self.tile_bits = _tile_bits(dtype) if tile_bits is None else int(tile_bits)
+        self._fwd, self._rev = [], []
+        if self.tile_bits > 0:
+            bits = [[self.n - 1 - q for q in idx] for _, idx, _ in self.gates]
+            fwd_tile = min(self.tile_bits + 1, self.n)  # one state only: twice the tile of the reverse pass
+            for lo, high, ops in _plan_reverse([(g, bits[g]) for g in range(len(bits))], self.n, fwd_tile):
+                self._fwd.append(_forward_sweep_struct(lo, high, [(b, g * 16) for g, b in ops]))
+            tile = min(self.tile_bits, self.n)
+            for lo, high, ops in _plan_reverse([(g, bits[g]) for g in reversed(range(len(bits)))], self.n, tile):
+                self._rev.append(_adjoint_sweep_struct(lo, high, [(b, g * 16, g if kinds[g] else -1, kinds[g])
+                                                                  for g, b in ops]))
 
     @classmethod
     def hea(cls, n, layers, dtype=torch.complex64, device="cuda"):
@@ -365,9 +462,14 @@ class BatchedAnsatz:
         _lib.check(L.qgb_init_basis(psi.data_ptr(), self.code, n, 0, P, N, st), "init")
         base = mats.data_ptr()
         set_stride = 16 * len(self.gates)
-        for g, (_, idx, _) in enumerate(self.gates):
-            _lib.check(L.qgb_op_action(psi.data_ptr(), self.code, n, self._sites[g], len(idx), base + g * 16 * isz,
-                                       set_stride, P, N, st), "op_action")
+        if self._fwd:
+            for sw in self._fwd:
+                _lib.check(L.qgb_apply_sweep(psi.data_ptr(), self.code, n, C.byref(sw), base, set_stride, P, N, st),
+                           "apply_sweep")
+        else:
+            for g, (_, idx, _) in enumerate(self.gates):
+                _lib.check(L.qgb_op_action(psi.data_ptr(), self.code, n, self._sites[g], len(idx), base + g * 16 * isz,
+                                           set_stride, P, N, st), "op_action")
         terms = list(terms)
         E = pauli_expectations(psi, n, terms, batch=P, stride=N).reshape(P, -1).sum(dim=1)
         lam = torch.empty_like(psi)
@@ -378,8 +480,14 @@ class BatchedAnsatz:
         phi = psi  # uncomputed in place
         gvals = torch.zeros(len(self.gates) * P, dtype=torch.float64, device=self.device)  # [gate][set]
         nbytes = L.qgb_reduce_scratch_bytes(n, 32, P)
+        if self._rev:
+            nbytes = max(nbytes, L.qgb_adjoint_sweep_scratch_bytes(n, min(self.tile_bits, n), 64, P))
         scr = self.scratch.get(nbytes)
-        for g in range(len(self.gates) - 1, -1, -1):
+        for sw in self._rev:
+            _lib.check(L.qgb_adjoint_sweep_step(phi.data_ptr(), lam.data_ptr(), self.code, n, C.byref(sw), base,
+                                                set_stride, P, N, gvals.data_ptr(), scr.data_ptr(), nbytes, st),
+                       "adjoint_sweep_step")
+        for g in (range(len(self.gates) - 1, -1, -1) if not self._rev else ()):
             idx = self.gates[g][1]
             op = base + g * 16 * isz
             if self._need[g]:

@@ -260,7 +260,10 @@ def plan_sweeps(blocks, nbits, tile_bits, low_bits=None, max_high=QGB_SWEEP_MAX_
         high: list = []
         taken, rest = [], []
         blocked: set = set()
-        for blk in remaining:
+        for j, blk in enumerate(remaining):
+            if len(blocked) >= nbits:  # every later block overlaps a skipped one: keep the rest in order
+                rest.extend(remaining[j:])
+                break
             bset = set(blk.bits)
             if bset & blocked or len(taken) >= QGB_SWEEP_MAX_OPS:
                 blocked |= bset
