@@ -292,6 +292,14 @@ def section_adjoint(n=24, layers=40, base_layers=4):
     out["adjoint_grads_per_s"] = round(1.0 / t_full, 3)
     out["adjoint_peak_state_multiples"] = round((torch.cuda.max_memory_allocated() - base) / (2 ** n * 8), 2)
     out["energy"] = e_full
+    # error of the complex64 gradient against the same adjoint gradient in complex128
+    th = torch.tensor(workloads.hea_params(n, layers, 1), dtype=torch.float64, requires_grad=True)
+    e128 = adjoint_energy(StatevectorSim(workloads.hea_circuit(n, layers, th), dtype=torch.complex128), terms)
+    e128.backward()
+    _, _, g64 = adjoint_run(layers)
+    g128 = th.grad.numpy()
+    out["max_rel_grad_err_vs_c128"] = float(np.abs(g64 - g128).max() / np.abs(g128).max())
+    out["energy_err_vs_c128"] = abs(e_full - float(e128.item()))
     # the reference's torch path at a depth that fits, same depth for the adjoint
     t_adj_b, e_adj_b, g_adj_b = adjoint_run(base_layers)
     params = workloads.hea_params(n, base_layers, 1)

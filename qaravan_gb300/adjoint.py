@@ -71,8 +71,16 @@ class _Runner:
         ops = [Op([n - 1 - q for q in g.indices], m) for g, m in zip(self.gates, host)]
         kcap = 5 if self.dtype == torch.complex64 else 4
         isz = torch.empty(0, dtype=self.dtype).element_size()
-        plan = compile_ops(ops, n, mode=self.sim.mode, width=self.sim.fusion_width, tile_bits=self.sim.tile_bits,
-                           low_bits=self.sim.low_bits, max_sweep_k=kcap, itemsize=isz, device_fusion=True)
+        if self.dtype == torch.complex64:
+            # gradients are differences of large, nearly cancelling sums: the forward runs as
+            # float32 CUDA-core tile sweeps of 4-qubit blocks (a few ms) rather than the split-fp16
+            # tensor-core blocks, whose rounding left up to 9e-6 relative gradient error at 20
+            # qubits, 40 layers (3e-6 with the CUDA cores, against complex128)
+            plan = compile_ops(ops, n, mode="sweep", width=4, tile_bits=14, max_sweep_k=kcap, itemsize=isz,
+                               device_fusion=True)
+        else:
+            plan = compile_ops(ops, n, mode=self.sim.mode, width=self.sim.fusion_width, tile_bits=self.sim.tile_bits,
+                               low_bits=self.sim.low_bits, max_sweep_k=kcap, itemsize=isz, device_fusion=True)
         psi = torch.empty(2 ** n, dtype=self.dtype, device=self.device)
         L = _lib.lib()
         _lib.check(L.qgb_init_basis(psi.data_ptr(), self.code, n, 0, 1, 0, _lib.stream_ptr(self.device)), "init")
@@ -159,8 +167,10 @@ _GEN_ROWS = {k: [(int(np.flatnonzero(m[r])[0]), complex(m[r, np.flatnonzero(m[r]
 
 def _tile_bits(dtype):
     """Tile of the adjoint sweeps: state and co-state double-buffered in shared
-    memory (4 x 2^m amplitudes: 128 KiB at m = 12 for complex64, 11 for complex128)."""
-    return 12 if dtype == torch.complex64 else 11
+    memory (4 x 2^m amplitudes: 64 KiB at m = 11 for complex64, three CTAs per
+    SM, the fastest of m = 10-12 measured on 64 sets of 20 qubits; 128 KiB at
+    m = 11 for complex128)."""
+    return 11
 
 
 def _plan_reverse(items, nbits, tile_bits):

@@ -8,7 +8,8 @@
 // gate. Here the host groups consecutive gates of the reverse order whose
 // sites fit one tile (the geometry of the forward sweeps, sweep.cu): a CTA
 // stages the tile of phi and of lam in shared memory (cp.async, double
-// buffered), and for every op, in order,
+// buffered), and for every op, in order (consecutive ops on the same sites in
+// one register pass),
 //   * for a rotation exp(-i theta P) whose derivative is wanted: adds
 //     Im sum conj(lam) (P phi) over the tile's groups (float partial per
 //     thread, a fixed xor-shuffle tree per warp, a float64 accumulator per
@@ -59,17 +60,21 @@ __device__ __forceinline__ void cp_async16_adj(void* smem_dst, const void* gmem_
                  : "memory");
 }
 
-// One op on the staged tiles: derivative (if wanted) at the op's output, then
-// U^dagger on both tiles. threads tid = 0..nthr-1 of the CTA.
-template <typename T, int K>
-__device__ __forceinline__ void adj_tile_op(cplx<T>* __restrict__ pt, cplx<T>* __restrict__ lt, int m,
-                                            const AdjSweepArgs& a, int op, const cplx<T>* __restrict__ U,
-                                            double* __restrict__ red_row, int tid, int nthr) {
+constexpr int kAdjMaxRun = 4;  // consecutive ops on the same sites handled in one register pass
+
+// A run of R consecutive ops on the same K sites (R <= kAdjMaxRun): per group
+// of partner amplitudes, one load and one store of the staged tiles; for each
+// op of the run in order, the derivative (if wanted) at the op's output, then
+// U^dagger on both. threads tid = 0..nthr-1 of the CTA.
+template <typename T, int K, int R>
+__device__ __forceinline__ void adj_tile_run(cplx<T>* __restrict__ pt, cplx<T>* __restrict__ lt, int m,
+                                             const AdjSweepArgs& a, int op0, const cplx<T>* __restrict__ ush,
+                                             double* __restrict__ red, int tid, int nthr) {
     constexpr int D = 1 << K;
     using C = cplx<T>;
     int pos[K], srt[K];
 #pragma unroll
-    for (int j = 0; j < K; ++j) pos[j] = srt[j] = a.op_pos[op][j];
+    for (int j = 0; j < K; ++j) pos[j] = srt[j] = a.op_pos[op0][j];
     if constexpr (K == 2) {
         if (srt[0] > srt[1]) {
             const int t = srt[0];
@@ -85,23 +90,24 @@ __device__ __forceinline__ void adj_tile_op(cplx<T>* __restrict__ pt, cplx<T>* _
         for (int j = 0; j < K; ++j) o |= uint32_t((r >> (K - 1 - j)) & 1) << pos[j];
         soff[r] = swz<T>(o);
     }
-    C ud[D * D];
+    C ud[R][D * D];
+    bool want[R];
+    C gv[R][D];
+    int gc[R][D];
 #pragma unroll
-    for (int r = 0; r < D; ++r)
+    for (int q = 0; q < R; ++q) {
 #pragma unroll
-        for (int c = 0; c < D; ++c) {
-            const C u = __ldg(&U[c * D + r]);
-            ud[r * D + c] = mk<T>(u.x, -u.y);
+        for (int e = 0; e < D * D; ++e) ud[q][e] = ush[(op0 + q) * 16 + e];  // U^dagger, staged per state
+        want[q] = a.op_out[op0 + q] >= 0;
+#pragma unroll
+        for (int r = 0; r < D; ++r) {
+            gv[q][r] = mk<T>(T(a.gval[op0 + q][r].x), T(a.gval[op0 + q][r].y));
+            gc[q][r] = a.gcol[op0 + q][r];
         }
-    const bool want = a.op_out[op] >= 0;
-    C gv[D];
-    int gc[D];
-#pragma unroll
-    for (int r = 0; r < D; ++r) {
-        gv[r] = mk<T>(T(a.gval[op][r].x), T(a.gval[op][r].y));
-        gc[r] = a.gcol[op][r];
     }
-    T s = T(0);
+    T s[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) s[q] = T(0);
     const uint32_t groups = 1u << (m - K);
     for (uint32_t g = tid; g < groups; g += nthr) {
         uint32_t base = g;
@@ -114,35 +120,76 @@ __device__ __forceinline__ void adj_tile_op(cplx<T>* __restrict__ pt, cplx<T>* _
             p[c] = pt[sb ^ soff[c]];
             l[c] = lt[sb ^ soff[c]];
         }
-        if (want) {
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+            if (want[q]) {
+#pragma unroll
+                for (int r = 0; r < D; ++r) {
+                    C pc = p[0];  // p[gc[r]] by selects (no dynamic register indexing)
+#pragma unroll
+                    for (int c = 1; c < D; ++c)
+                        if (gc[q][r] == c) pc = p[c];
+                    C w = mk<T>(0, 0);
+                    cfma(w, gv[q][r], pc);
+                    s[q] += l[r].x * w.y - l[r].y * w.x;  // Im(conj(l) w)
+                }
+            }
+            C pn[D], ln[D];
 #pragma unroll
             for (int r = 0; r < D; ++r) {
-                C pc = p[0];  // p[gc[r]] by selects (no dynamic register indexing)
+                C x = mk<T>(0, 0), y = mk<T>(0, 0);
 #pragma unroll
-                for (int c = 1; c < D; ++c)
-                    if (gc[r] == c) pc = p[c];
-                C w = mk<T>(0, 0);
-                cfma(w, gv[r], pc);
-                s += l[r].x * w.y - l[r].y * w.x;  // Im(conj(l) w)
+                for (int c = 0; c < D; ++c) {
+                    cfma(x, ud[q][r * D + c], p[c]);
+                    cfma(y, ud[q][r * D + c], l[c]);
+                }
+                pn[r] = x;
+                ln[r] = y;
+            }
+#pragma unroll
+            for (int r = 0; r < D; ++r) {
+                p[r] = pn[r];
+                l[r] = ln[r];
             }
         }
 #pragma unroll
         for (int r = 0; r < D; ++r) {
-            C x = mk<T>(0, 0), y = mk<T>(0, 0);
-#pragma unroll
-            for (int c = 0; c < D; ++c) {
-                cfma(x, ud[r * D + c], p[c]);
-                cfma(y, ud[r * D + c], l[c]);
-            }
-            pt[sb ^ soff[r]] = x;
-            lt[sb ^ soff[r]] = y;
+            pt[sb ^ soff[r]] = p[r];
+            lt[sb ^ soff[r]] = l[r];
         }
     }
-    if (want) {  // uniform over the CTA: every lane reaches the shuffles
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if ((tid & 31) == 0) red_row[tid >> 5] += double(s);
+    for (int q = 0; q < R; ++q) {
+        if (want[q]) {  // uniform over the CTA: every lane reaches the shuffles
+            T v = s[q];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if ((tid & 31) == 0) red[(op0 + q) * kAdjMaxWarps + (tid >> 5)] += double(v);
+        }
     }
+}
+
+// Length of the run of ops starting at op0 on the same sites (same k and tile bits, in order).
+__device__ __forceinline__ int adj_run_length(const AdjSweepArgs& a, int op0) {
+    int r = 1;
+    while (op0 + r < a.n_ops && r < kAdjMaxRun && a.op_k[op0 + r] == a.op_k[op0] &&
+           a.op_pos[op0 + r][0] == a.op_pos[op0][0] && (a.op_k[op0] == 1 || a.op_pos[op0 + r][1] == a.op_pos[op0][1]))
+        ++r;
+    return r;
+}
+
+template <typename T, int K>
+__device__ __forceinline__ int adj_tile_ops(cplx<T>* pt, cplx<T>* lt, int m, const AdjSweepArgs& a, int op0,
+                                            const cplx<T>* ush, double* red, int tid, int nthr) {
+    // longest run kept in registers without spilling under the 512-thread register cap
+    constexpr int kMax = sizeof(T) == 4 ? (K == 1 ? 4 : 2) : (K == 1 ? 2 : 1);
+    int r = adj_run_length(a, op0);
+    if (r > kMax) r = kMax;
+    if (r == 1) adj_tile_run<T, K, 1>(pt, lt, m, a, op0, ush, red, tid, nthr);
+    else if (r == 2) { if constexpr (kMax >= 2) adj_tile_run<T, K, 2>(pt, lt, m, a, op0, ush, red, tid, nthr); }
+    else if (r == 3) { if constexpr (kMax >= 3) adj_tile_run<T, K, 3>(pt, lt, m, a, op0, ush, red, tid, nthr); }
+    else { if constexpr (kMax >= 4) adj_tile_run<T, K, 4>(pt, lt, m, a, op0, ush, red, tid, nthr); }
+    return r;
 }
 
 template <typename T>
@@ -155,10 +202,13 @@ __global__ void __launch_bounds__(kAdjMaxThreads) adjoint_sweep_kernel(cplx<T>* 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int L = a.L, H = a.H, m = a.m;
     const int nwarps = blockDim.x >> 5;
-    // layout: nbuf x (phi tile, lam tile) | hoff (2^H uint64) | red (n_ops x kAdjMaxWarps double)
+    // layout: nbuf x (phi tile, lam tile) | ush (n_ops x 16 complex: U^dagger of the current state) |
+    //         hoff (2^H uint64) | red (n_ops x kAdjMaxWarps double)
     C* bufs = reinterpret_cast<C*>(smem_raw);
-    uint64_t* hoff = reinterpret_cast<uint64_t*>(bufs + (size_t(2 * nbuf) << m));
+    C* ush = bufs + (size_t(2 * nbuf) << m);
+    uint64_t* hoff = reinterpret_cast<uint64_t*>(ush + size_t(a.n_ops) * 16);
     double* red = reinterpret_cast<double*>(hoff + (size_t(1) << H));
+    int64_t staged = -1;  // state whose matrices sit in ush
     for (uint32_t h = threadIdx.x; h < (1u << H); h += blockDim.x) {
         uint64_t o = 0;
         for (int j = 0; j < H; ++j) o |= uint64_t((h >> j) & 1u) << a.high_bits[j];
@@ -202,14 +252,23 @@ __global__ void __launch_bounds__(kAdjMaxThreads) adjoint_sweep_kernel(cplx<T>* 
         } else {
             asm volatile("cp.async.wait_group 0;" ::: "memory");
         }
+        const int64_t b = int64_t(w / a.tiles);
+        if (b != staged) {  // once per chunk: every op's U^dagger for this state (previous readers done: loop-end barrier)
+            const C* mb = mats + b * a.mat_stride;
+            for (int e = threadIdx.x; e < a.n_ops * 16; e += blockDim.x) {
+                const int op = e >> 4, rc = e & 15, d = 1 << a.op_k[op];
+                if (rc < d * d) {
+                    const int r = rc / d, c = rc - r * d;
+                    const C u = mb[a.op_mat[op] + c * d + r];
+                    ush[e] = mk<T>(u.x, -u.y);
+                }
+            }
+            staged = b;
+        }
         __syncthreads();
-        const uint64_t b = w / a.tiles;
-        const C* mb = mats + int64_t(b) * a.mat_stride;
-        for (int op = 0; op < a.n_ops; ++op) {
-            if (a.op_k[op] == 1)
-                adj_tile_op<T, 1>(pt, lt, m, a, op, mb + a.op_mat[op], red + op * kAdjMaxWarps, threadIdx.x, blockDim.x);
-            else
-                adj_tile_op<T, 2>(pt, lt, m, a, op, mb + a.op_mat[op], red + op * kAdjMaxWarps, threadIdx.x, blockDim.x);
+        for (int op = 0; op < a.n_ops;) {
+            op += a.op_k[op] == 1 ? adj_tile_ops<T, 1>(pt, lt, m, a, op, ush, red, threadIdx.x, blockDim.x)
+                                  : adj_tile_ops<T, 2>(pt, lt, m, a, op, ush, red, threadIdx.x, blockDim.x);
             __syncthreads();
         }
         const uint64_t base = base_of(w);
@@ -261,7 +320,7 @@ namespace {
 
 template <typename T>
 size_t adj_smem_bytes(int m, int H, int n_ops, int nbuf) {
-    return sizeof(cplx<T>) * (size_t(2 * nbuf) << m) + sizeof(uint64_t) * (size_t(1) << H) +
+    return sizeof(cplx<T>) * ((size_t(2 * nbuf) << m) + size_t(n_ops) * 16) + sizeof(uint64_t) * (size_t(1) << H) +
            sizeof(double) * size_t(n_ops) * kAdjMaxWarps;
 }
 
