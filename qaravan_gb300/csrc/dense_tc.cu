@@ -272,6 +272,36 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
                  : "memory");
 }
 
+// 32 and 64 columns in one load and one wait (a half row of a 5- or 6-qubit
+// block's accumulator), so a drain makes one tensor-memory round trip.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+                 : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7]), "=f"(v[8]), "=f"(v[9]), "=f"(v[10]), "=f"(v[11]), "=f"(v[12]), "=f"(v[13]), "=f"(v[14]), "=f"(v[15]), "=f"(v[16]), "=f"(v[17]), "=f"(v[18]), "=f"(v[19]), "=f"(v[20]), "=f"(v[21]), "=f"(v[22]), "=f"(v[23]), "=f"(v[24]), "=f"(v[25]), "=f"(v[26]), "=f"(v[27]), "=f"(v[28]), "=f"(v[29]), "=f"(v[30]), "=f"(v[31])
+                 : "r"(taddr)
+                 : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+f"(v[0]), "+f"(v[1]), "+f"(v[2]), "+f"(v[3]), "+f"(v[4]), "+f"(v[5]), "+f"(v[6]), "+f"(v[7]), "+f"(v[8]), "+f"(v[9]), "+f"(v[10]), "+f"(v[11]), "+f"(v[12]), "+f"(v[13]), "+f"(v[14]), "+f"(v[15]), "+f"(v[16]), "+f"(v[17]), "+f"(v[18]), "+f"(v[19]), "+f"(v[20]), "+f"(v[21]), "+f"(v[22]), "+f"(v[23]), "+f"(v[24]), "+f"(v[25]), "+f"(v[26]), "+f"(v[27]), "+f"(v[28]), "+f"(v[29]), "+f"(v[30]), "+f"(v[31])
+                 :
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, float* v) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32, %33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, %45, %46, %47, %48, %49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63}, [%64];"
+                 : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7]), "=f"(v[8]), "=f"(v[9]), "=f"(v[10]), "=f"(v[11]), "=f"(v[12]), "=f"(v[13]), "=f"(v[14]), "=f"(v[15]), "=f"(v[16]), "=f"(v[17]), "=f"(v[18]), "=f"(v[19]), "=f"(v[20]), "=f"(v[21]), "=f"(v[22]), "=f"(v[23]), "=f"(v[24]), "=f"(v[25]), "=f"(v[26]), "=f"(v[27]), "=f"(v[28]), "=f"(v[29]), "=f"(v[30]), "=f"(v[31]), "=f"(v[32]), "=f"(v[33]), "=f"(v[34]), "=f"(v[35]), "=f"(v[36]), "=f"(v[37]), "=f"(v[38]), "=f"(v[39]), "=f"(v[40]), "=f"(v[41]), "=f"(v[42]), "=f"(v[43]), "=f"(v[44]), "=f"(v[45]), "=f"(v[46]), "=f"(v[47]), "=f"(v[48]), "=f"(v[49]), "=f"(v[50]), "=f"(v[51]), "=f"(v[52]), "=f"(v[53]), "=f"(v[54]), "=f"(v[55]), "=f"(v[56]), "=f"(v[57]), "=f"(v[58]), "=f"(v[59]), "=f"(v[60]), "=f"(v[61]), "=f"(v[62]), "=f"(v[63])
+                 : "r"(taddr)
+                 : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+f"(v[0]), "+f"(v[1]), "+f"(v[2]), "+f"(v[3]), "+f"(v[4]), "+f"(v[5]), "+f"(v[6]), "+f"(v[7]), "+f"(v[8]), "+f"(v[9]), "+f"(v[10]), "+f"(v[11]), "+f"(v[12]), "+f"(v[13]), "+f"(v[14]), "+f"(v[15]), "+f"(v[16]), "+f"(v[17]), "+f"(v[18]), "+f"(v[19]), "+f"(v[20]), "+f"(v[21]), "+f"(v[22]), "+f"(v[23]), "+f"(v[24]), "+f"(v[25]), "+f"(v[26]), "+f"(v[27]), "+f"(v[28]), "+f"(v[29]), "+f"(v[30]), "+f"(v[31]), "+f"(v[32]), "+f"(v[33]), "+f"(v[34]), "+f"(v[35]), "+f"(v[36]), "+f"(v[37]), "+f"(v[38]), "+f"(v[39]), "+f"(v[40]), "+f"(v[41]), "+f"(v[42]), "+f"(v[43]), "+f"(v[44]), "+f"(v[45]), "+f"(v[46]), "+f"(v[47]), "+f"(v[48]), "+f"(v[49]), "+f"(v[50]), "+f"(v[51]), "+f"(v[52]), "+f"(v[53]), "+f"(v[54]), "+f"(v[55]), "+f"(v[56]), "+f"(v[57]), "+f"(v[58]), "+f"(v[59]), "+f"(v[60]), "+f"(v[61]), "+f"(v[62]), "+f"(v[63])
+                 :
+                 : "memory");
+}
+
+template <int N> __device__ __forceinline__ void tmem_ld_row(uint32_t taddr, float* v) {
+    static_assert(N == 16 || N == 32 || N == 64, "row width");
+    if constexpr (N == 16) tmem_ld16(taddr, v);
+    else if constexpr (N == 32) tmem_ld32(taddr, v);
+    else tmem_ld64(taddr, v);
+}
+
 // UNIT: the op is unitary; each group's norm is restored after the product.
 template <int K, bool UNIT>
 __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restrict__ sv, const float2* __restrict__ op,
@@ -497,10 +527,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
                 // power of two is a normal float, else the two factors in turn
                 const float su = u * wunscale;
                 const bool one = su >= 1.17549435e-38f && su <= 1.0e38f;
+                float y[D];
+                tmem_ld_row<D>(acc, y);
 #pragma unroll
                 for (int c0 = 0; c0 < D; c0 += 16) {
-                    float r[16];
-                    tmem_ld16(acc + uint32_t(c0), r);
+                    float* r = y + c0;
                     if (one) {
                         const unsigned long long su2 = f2pack(su, su);
 #pragma unroll
@@ -525,8 +556,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
             for (int bk = 0; bk < NB; ++bk) {
                 const uint32_t acc = row + uint32_t(bk * BC + 2 * R + pb * R + h * D);
                 float y[D];
-#pragma unroll
-                for (int c0 = 0; c0 < D; c0 += 16) tmem_ld16(acc + uint32_t(c0), y + c0);
+                tmem_ld_row<D>(acc, y);
                 row_out[pb][bk][h][32 * q + lane] = sumsq8<D>(y);
             }
         };
@@ -546,10 +576,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
                 const float nout = one ? (nraw * su) * su : 0.f;
                 const float g = nout > 0.f ? (nin[bk] - nout) / (2.f * nout) : 0.f;
                 const unsigned long long cg2 = f2pack(su * g, su * g), su2 = f2pack(su, su);
+                float y[D];
+                tmem_ld_row<D>(acc, y);
 #pragma unroll
                 for (int c0 = 0; c0 < D; c0 += 16) {
-                    float r[16];
-                    tmem_ld16(acc + uint32_t(c0), r);
+                    float* r = y + c0;
                     if (one) {
 #pragma unroll
                         for (int e = 0; e < 16; e += 2) {
