@@ -31,7 +31,8 @@ from .engine import Executor, Scratch
 
 def _gate_list(sim):
     from .statevector import circuit_ops
-    gates = [g for g in circuit_ops(sim.circ) if not (g.name == "ID" and getattr(g, "nm", None) is not None)]
+    gates = [g for g in circuit_ops(sim.circ, build=True, nm=getattr(sim, "nm", None))
+             if not (g.name == "ID" and getattr(g, "nm", None) is not None)]
     for g in gates:
         if len(g.indices) > 2:
             raise NotImplementedError("the adjoint sweep handles gates on one or two sites")

@@ -306,6 +306,32 @@ def unitary_flags(ops, tol=1e-6):
     return flags
 
 
+# Plans whose block matrices are all device-composed (Recipe) depend on the op
+# matrices only through the unitarity flags: such a plan is kept per structure
+# (op bits, flags, options) and reused with new op matrices, so a circuit run
+# again with other values (a variational loop, the same circuit rebuilt) skips
+# the fusion planner. Bounded, least recently used first out.
+_PLAN_CACHE: "dict" = {}
+_PLAN_CACHE_SIZE = 32
+
+
+def _cached_plan(key, ops):
+    tpl = _PLAN_CACHE.pop(key, None)
+    if tpl is None:
+        return None
+    _PLAN_CACHE[key] = tpl  # most recently used last
+    plan = Plan(nbits=tpl.nbits, steps=tpl.steps, matrices=tpl.matrices, n_gates=tpl.n_gates)
+    plan.op_matrices = [np.ascontiguousarray(o.matrix, dtype=np.complex128) for o in ops if o is not None]
+    return plan
+
+
+def _remember_plan(key, plan):
+    if plan.matrices and all(isinstance(m, Recipe) for m in plan.matrices):
+        _PLAN_CACHE[key] = plan
+        while len(_PLAN_CACHE) > _PLAN_CACHE_SIZE:
+            _PLAN_CACHE.pop(next(iter(_PLAN_CACHE)))
+
+
 def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, max_sweep_k=5, itemsize=8,
                 device_fusion=False):
     """Compile an op sequence (with ``None`` marking a renormalisation point)
@@ -318,6 +344,14 @@ def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, 
     :class:`Recipe` objects for the executor to compose on the GPU.
     """
     tile_bits = min(tile_bits, 14 if itemsize <= 8 else 13)
+    key = None
+    if device_fusion and mode != "gate" and ops:
+        flags = unitary_flags([o for o in ops if o is not None])
+        key = (nbits, mode, width, tile_bits, low_bits, max_sweep_k, itemsize,
+               tuple(None if o is None else tuple(o.bits) for o in ops), tuple(flags))
+        plan = _cached_plan(key, ops)
+        if plan is not None:
+            return plan
     plan = Plan(nbits=nbits, n_gates=sum(1 for o in ops if o is not None))
     segments, cur = [], []
     for o in ops:
@@ -361,6 +395,8 @@ def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, 
                 tpos[b] = L + h
             sops = [([tpos[b] for b in blk.bits], plan.add_matrix(blk.matrix)) for blk in taken]
             plan.steps.append(SweepStep(L, list(high), sops))
+    if key is not None:
+        _remember_plan(key, plan)
     return plan
 
 

@@ -55,6 +55,10 @@ class Scratch:
         return self.buf
 
 
+# fusion tables per plan structure: id(recipe list) -> (that list, op sizes, tables ...)
+_LAYOUT_CACHE: dict = {}
+
+
 class Executor:
     def __init__(self, plan: Plan, dtype=torch.complex64, device="cuda", mode_normalize="sv"):
         self.plan = plan
@@ -122,26 +126,37 @@ class Executor:
                 op_mats.append(np.ascontiguousarray(m, dtype=np.complex128))
                 bits = list(range(k - 1, -1, -1))
                 recipes.append(Recipe(bits, [(len(op_mats) - 1, bits)]))
-        op_off, o = [], 0
-        for m in op_mats:
-            op_off.append(o)
-            o += m.size
-        n_op_elems = max(o, 1)
-        blocks = np.zeros(len(recipes), dtype=_FUSE_BLOCK)
-        n_ent = sum(len(r.entries) for r in recipes)
-        ents = np.zeros(max(n_ent, 1), dtype=_FUSE_ENTRY)
-        offs, out, e = [], 0, 0
-        for i, r in enumerate(recipes):
-            k = len(r.bits)
-            offs.append(out)
-            blocks[i] = (out, k, e, e + len(r.entries), 0)
-            pos_of = {b: j for j, b in enumerate(r.bits)}
-            for mi, obits in r.entries:
-                ents["k"][e] = len(obits)
-                ents["pos"][e, :len(obits)] = [pos_of[b] for b in obits]
-                ents["mat"][e] = op_off[mi]
-                e += 1
-            out += 4 ** k
+        # the tables depend on the plan's structure only: kept with its (shared) recipe list
+        all_recipes = len(recipes) == len(plan.matrices) and len(recipes) > 0
+        hit = _LAYOUT_CACHE.get(id(plan.matrices)) if all_recipes else None
+        if hit is not None and hit[0] is plan.matrices and hit[1] == [m.size for m in op_mats]:
+            _, _, op_off, n_op_elems, blocks, ents, n_ent, offs, out = hit
+        else:
+            op_off, o = [], 0
+            for m in op_mats:
+                op_off.append(o)
+                o += m.size
+            n_op_elems = max(o, 1)
+            blocks = np.zeros(len(recipes), dtype=_FUSE_BLOCK)
+            n_ent = sum(len(r.entries) for r in recipes)
+            ents = np.zeros(max(n_ent, 1), dtype=_FUSE_ENTRY)
+            offs, out, e = [], 0, 0
+            for i, r in enumerate(recipes):
+                k = len(r.bits)
+                offs.append(out)
+                blocks[i] = (out, k, e, e + len(r.entries), 0)
+                pos_of = {b: j for j, b in enumerate(r.bits)}
+                for mi, obits in r.entries:
+                    ents["k"][e] = len(obits)
+                    ents["pos"][e, :len(obits)] = [pos_of[b] for b in obits]
+                    ents["mat"][e] = op_off[mi]
+                    e += 1
+                out += 4 ** k
+            if all_recipes:
+                _LAYOUT_CACHE[id(plan.matrices)] = (plan.matrices, [m.size for m in op_mats], op_off, n_op_elems,
+                                                    blocks, ents, n_ent, offs, out)
+                while len(_LAYOUT_CACHE) > 32:
+                    _LAYOUT_CACHE.pop(next(iter(_LAYOUT_CACHE)))
         opm = np.concatenate([m.reshape(-1) for m in op_mats]) if op_mats else np.zeros(1, np.complex128)
         sections = [opm.view(np.uint8), blocks.view(np.uint8), ents.view(np.uint8)]
         starts, nbytes = [], 0

@@ -218,7 +218,7 @@ class ParamGate(Gate):
     def __init__(self, name, indices, *args):
         super().__init__(name, indices, None)
         self.backend = "torch" if _is_torch(args[0]) else "numpy"
-        if isinstance(args[0], np.ndarray) and args[0].ndim == 2:
+        if type(args[0]) == np.ndarray:  # a matrix (core/param_gates.py:26-29), angles solved from it
             self.matrix = args[0]
             self.angles = self.solve_angles()
         else:
@@ -350,7 +350,10 @@ class U(ParamGate):
                      [xp.exp(1j * p) * xp.sin(t / 2), xp.exp(1j * (p + l)) * xp.cos(t / 2)]], self.backend)
 
     def solve_angles(self):
-        m = self.matrix / np.exp(1.j * np.angle(self.matrix[0, 0]))
+        # as core/param_gates.py:131-142, the stored matrix loses the phase of its
+        # top-left entry (a U built from a matrix simulates without that global phase)
+        self.matrix = self.matrix / np.exp(1.j * np.angle(self.matrix[0, 0]))
+        m = self.matrix
         t = np.arccos(np.clip(m[0, 0].real, -1, 1)) * 2
         if abs(np.sin(t / 2)) > 1e-12:
             l = np.angle(-m[0, 1] / np.sin(t / 2))
@@ -358,6 +361,15 @@ class U(ParamGate):
         else:
             l = p = np.angle(m[1, 1]) / 2
         return t, p, l
+
+    def decompose(self, basis='ZSX'):
+        """RZ / SX sequence of ``core/param_gates.py:144-156`` (first applied
+        first), from the angles solved from the matrix."""
+        if basis != 'ZSX':
+            raise NotImplementedError(f"{basis} basis decomposition has not been implemented")
+        t, p, l = self.solve_angles()
+        i = self.indices
+        return list(reversed([RZ(i, p + np.pi), SX(i), RZ(i, t + np.pi), SX(i), RZ(i, l)]))
 
 
 class Givens(ParamGate):

@@ -31,10 +31,17 @@ def _to_np(m):
     return np.asarray(m, dtype=np.complex128)
 
 
-def circuit_ops(circ, n=None):
+def circuit_ops(circ, n=None, build=False, nm=None):
     """Flatten a (reference or local) Circuit into the op sequence run() applies:
     layers if the circuit is built (or after building it), Reset as projector
-    plus a renormalisation marker, ID noise carriers as identities (skipped)."""
+    plus a renormalisation marker, ID noise carriers as identities (skipped).
+    ``build``: the caller owns ``circ`` (a simulator's own copy) and it is built
+    in place as ``BaseSim.run`` does (``core/base_sim.py:37``,
+    ``core/circuits.py:86-95``: decomposition when ``requires_decomp``, layers,
+    noise); otherwise an unbuilt circuit is layered on a copy."""
+    if build and hasattr(circ, "build") and not getattr(circ, "built", False):
+        circ.build(nm)
+        return [g for layer in circ.layers for g in layer]
     if getattr(circ, "layers", None) is None and hasattr(circ, "construct_layers"):
         layers = None
         try:
@@ -118,7 +125,7 @@ class StatevectorSim:
 
     def compile(self):
         if self._exec is None:
-            seq = circuit_ops(self.circ)
+            seq = circuit_ops(self.circ, build=True, nm=self.nm)
             ops = gates_to_ops(seq, self.num_sites)
             kcap = 5 if self.dtype == torch.complex64 else 4
             plan = compile_ops(ops, self.num_sites, mode=self.mode, width=self.fusion_width,

@@ -93,6 +93,37 @@ def gen_sv_mixed(R):
     _save("sv_mixed7.npz", n=n, init=init, sv=sv, **pack_gates(gates))
 
 
+def gen_sv_decomp(R):
+    """A circuit with U gates built from angles and from matrices, run with
+    requires_decomp=True: the reference decomposes every U into RZ / SX gates
+    (core/circuits.py:31-40, core/param_gates.py:144-156) inside the
+    simulator's copy; a U built from a matrix stores it without the phase of
+    its top-left entry (core/param_gates.py:131-133)."""
+    c = R.core
+    n = 4
+    rng = np.random.default_rng(5)
+    mats = [workloads.haar_unitary(2, rng) for _ in range(2)]
+    angles = [(0.3, -1.1, 2.0), (1.7, 0.4, -0.6)]
+    gates = [c.U([0], *angles[0]), c.U([2], mats[0]), c.CNOT([1, 0], n), c.U([1], *angles[1]), c.U([3], mats[1]),
+             c.H(2), c.CNOT([3, 2], n)]
+    sim = R.tensorQ.StatevectorSim(c.Circuit(gates, n=n, requires_decomp=True))
+    sim.run(progress_bar=False)
+    sv = np.asarray(sim.get_statevector(), dtype=np.complex128)
+    plain = [c.U([0], *angles[0]), c.U([2], mats[0]), c.CNOT([1, 0], n), c.U([1], *angles[1]), c.U([3], mats[1]),
+             c.H(2), c.CNOT([3, 2], n)]
+    sv_plain, _ = run_ref_sv(R, plain, n)
+    # the simulator's copy drops requires_decomp (core/circuits.py:163-169); Circuit.build()
+    # on the circuit itself decomposes, and a prebuilt circuit runs as built
+    built = c.Circuit([c.U([0], *angles[0]), c.U([2], mats[0]), c.CNOT([1, 0], n), c.U([1], *angles[1]),
+                       c.U([3], mats[1]), c.H(2), c.CNOT([3, 2], n)], n=n, requires_decomp=True).build()
+    sim_b = R.tensorQ.StatevectorSim(built)
+    sim_b.run(progress_bar=False)
+    sv_built = np.asarray(sim_b.get_statevector(), dtype=np.complex128)
+    _save("sv_decomp4.npz", n=n, sv=sv, sv_plain=sv_plain, sv_built=sv_built, angles=np.array(angles),
+          mats=np.array(mats), **pack_gates(sim.circ.gate_list, prefix="d"), **pack_gates(plain, prefix="u"),
+          **pack_gates(built.gate_list, prefix="b"))
+
+
 def gen_sv_observables(R):
     """Pauli-string expectations, partial overlaps and outcome probabilities on
     a random 8-qubit state."""
@@ -260,6 +291,7 @@ def main():
     gen_grad_hea(R)
     gen_traj_dm10(R, steps=10, p=0.02, gamma=0.03, name="traj_dm10_strong.npz")
     gen_traj_dm10(R, steps=40, p=1e-3, gamma=5e-4, name="traj_dm10.npz")
+    gen_sv_decomp(R)
 
 
 if __name__ == "__main__":

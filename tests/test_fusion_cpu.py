@@ -127,3 +127,34 @@ def test_device_fused_plans_match_oracle():
         v0 = np.zeros(2 ** n, complex)
         v0[0] = 1
         assert np.max(np.abs(run_plan_numpy(host, v0) - ref.run_sv(gates, n))) < 1e-12
+
+
+def test_plan_cache_reuses_structure_with_new_matrices():
+    """A second compile of the same structure (bits, unitarity, options) reuses the
+    fusion decisions; its recipes compose the new matrices exactly like a fresh
+    host fusion. A change of bits or of unitarity misses the cache."""
+    from qaravan_gb300.compiler import Op, compile_ops, fuse, recipe_matrix
+    rng = np.random.default_rng(11)
+    n = 9
+
+    def haar(d):
+        q, r = np.linalg.qr(rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d)))
+        return q * (np.diag(r) / np.abs(np.diag(r)))
+
+    bits = [[int(a)] if rng.random() < 0.4 else [int(a), int((a + 1 + rng.integers(n - 1)) % n)]
+            for a in rng.integers(n, size=60)]
+    ops1 = [Op(b, haar(2 ** len(b))) for b in bits]
+    ops2 = [Op(b, haar(2 ** len(b))) for b in bits]
+    p1 = compile_ops(ops1, n, mode="fused", width=4, device_fusion=True)
+    p2 = compile_ops(ops2, n, mode="fused", width=4, device_fusion=True)
+    assert p2.steps is p1.steps and p2.matrices is p1.matrices
+    host = fuse(ops2, 4)
+    assert len(host) == len(p2.matrices)
+    for blk, rec in zip(host, p2.matrices):
+        assert list(blk.bits) == list(rec.bits)
+        assert np.max(np.abs(recipe_matrix(rec, p2.op_matrices) - blk.matrix)) < 1e-12
+    ops3 = [Op(o.bits, o.matrix * (1.5 if i == 7 else 1.0)) for i, o in enumerate(ops2)]  # op 7 not unitary
+    p3 = compile_ops(ops3, n, mode="fused", width=4, device_fusion=True)
+    assert p3.steps is not p1.steps
+    ops4 = [Op(list(reversed(o.bits)), o.matrix) for o in ops2]
+    assert compile_ops(ops4, n, mode="fused", width=4, device_fusion=True).steps is not p1.steps

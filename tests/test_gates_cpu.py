@@ -43,3 +43,36 @@ def test_copy_rebuilds_a_replaced_matrix_from_angles():
     c2 = c.copy()
     assert np.max(np.abs(np.asarray(c2.gate_list[0].matrix) - np.asarray(RX([0], 0.7).matrix))) < 1e-15
     assert c2.gate_list[0].built_from_angles()
+
+
+def _decomp_circuit(z, requires_decomp):
+    from qaravan_gb300.circuits import Circuit
+    from qaravan_gb300.gates import CNOT, H, U
+    n = int(z["n"])
+    a, m = z["angles"], z["mats"]
+    gates = [U([0], *a[0]), U([2], m[0]), CNOT([1, 0], n), U([1], *a[1]), U([3], m[1]), H(2), CNOT([3, 2], n)]
+    return Circuit(gates, n=n, requires_decomp=requires_decomp)
+
+
+def test_u_from_matrix_and_zsx_decomposition_match_the_reference():
+    """Fixture from the reference (tests/golden/make_golden.py gen_sv_decomp): a U
+    built from a matrix stores it without the phase of its top-left entry;
+    Circuit.build() with requires_decomp replaces every U by the reference's
+    RZ / SX sequence (gate for gate); the simulator's copy drops requires_decomp."""
+    from conftest import golden
+    from gateio import unpack_gates
+    from oracle import ref
+    z = golden("sv_decomp4.npz")
+    plain = _decomp_circuit(z, False)
+    for g, want in zip(plain.gate_list, unpack_gates(z, "u")):
+        assert g.name == want.name and g.indices == list(want.indices)
+        assert np.max(np.abs(np.asarray(g.matrix) - want.matrix)) < 1e-12
+    built = _decomp_circuit(z, True).build()
+    want = unpack_gates(z, "b")
+    assert [(g.name, g.indices) for g in built.gate_list] == [(w.name, list(w.indices)) for w in want]
+    for g, w in zip(built.gate_list, want):
+        assert np.max(np.abs(np.asarray(g.matrix) - w.matrix)) < 1e-12
+    n = int(z["n"])
+    assert np.max(np.abs(ref.run_sv(want, n).reshape(-1) - z["sv_built"])) < 1e-12
+    assert np.max(np.abs(ref.run_sv(unpack_gates(z, "u"), n).reshape(-1) - z["sv_plain"])) < 1e-12
+    assert not _decomp_circuit(z, True).copy().requires_decomp

@@ -156,3 +156,25 @@ def test_batched_op_action_per_state_matrices(dtype):
                                         mt.data_ptr(), 16, B, 2 ** n, _lib.stream_ptr()))
     got = st.cpu().numpy()
     assert np.max(np.abs(got - np.stack(exp))) < TOL[dtype]
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.complex64, 1e-5), (torch.complex128, 1e-12)])
+def test_u_gates_requires_decomp_and_prebuilt_circuit_match_the_reference(dtype, tol):
+    """The reference's simulator copies the circuit without requires_decomp, so
+    U gates run undecomposed (and a U built from a matrix without its phase);
+    a circuit built beforehand runs its RZ / SX decomposition."""
+    from qaravan_gb300 import StatevectorSim
+    from qaravan_gb300.circuits import Circuit
+    from qaravan_gb300.gates import CNOT, H, U
+    z = golden("sv_decomp4.npz")
+    n = int(z["n"])
+
+    def circ(requires_decomp):
+        a, m = z["angles"], z["mats"]
+        return Circuit([U([0], *a[0]), U([2], m[0]), CNOT([1, 0], n), U([1], *a[1]), U([3], m[1]), H(2),
+                        CNOT([3, 2], n)], n=n, requires_decomp=requires_decomp)
+
+    sv = StatevectorSim(circ(True), dtype=dtype).get_statevector().cpu().numpy()
+    assert np.max(np.abs(sv - z["sv"])) < tol
+    sv_b = StatevectorSim(circ(True).build(), dtype=dtype).get_statevector().cpu().numpy()
+    assert np.max(np.abs(sv_b - z["sv_built"])) < tol
