@@ -12,8 +12,8 @@ runs in the hand-written CUDA kernels of ``libqgb.so`` (C ABI in
 from . import workloads
 from .circuits import Circuit, brickwall_skeleton, two_local_circ
 from .density_matrix import DensityMatrixSim
-from .gates import (CNOT, CZ, H, ID, RX, RY, RZ, RXX, RYY, RZZ, SDG, SWAP, SX, U, X, Y, Z, Gate, Reset,
-                    iSWAP, kak_unitary)
+from .gates import (CNOT, CZ, H, ID, RX, RY, RZ, RXX, RYY, RZZ, SDG, SWAP, SX, U, X, Y, Z, CUGate, Gate, Reset,
+                    SuperOp, embed_operator, iSWAP, kak_unitary)
 from .hamiltonians import TFI
 from .environments import RunContext, environment_state_prep, environment_update, sv_environment
 from .montecarlo import MonteCarloSim, trotter_mc_sim

@@ -15,7 +15,7 @@ from functools import reduce
 
 import numpy as np
 
-from .gates import ID, Gate, random_unitary, kak_unitary, RX, RY, RZ, RXX, RYY, RZZ, HeisenbergCoupling
+from .gates import ID, Gate, SuperOp, random_unitary, kak_unitary, RX, RY, RZ, RXX, RYY, RZZ, HeisenbergCoupling
 
 
 class Circuit:
@@ -68,6 +68,9 @@ class Circuit:
         from .noise import ThermalNoise, gate_time
         layers = []
         for layer in self.layers:
+            if any(isinstance(g, SuperOp) for g in layer):  # layers holding a superoperator stay noiseless
+                layers.append(layer)
+                continue
             if isinstance(nm, ThermalNoise):
                 t = max(gate_time(g, nm) for g in layer)
                 active = set(np.concatenate([g.indices for g in layer]))

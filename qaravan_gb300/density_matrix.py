@@ -60,6 +60,9 @@ def dm_ops_for_gate(g, n):
         s = np.asarray(g.nm.get_superop(g.time, getattr(g, "dd", False)), dtype=np.complex128)
         s = s.reshape(4 ** len(idx), 4 ** len(idx))
         return [Op(bra + ket, _sorted_rows(s, idx), kind="channel")]
+    if type(g).__name__ == "SuperOp":  # its matrix is the superoperator (tensorQ/density_matrix_sim.py:40)
+        s = np.asarray(g.matrix, dtype=np.complex128).reshape(4 ** len(idx), 4 ** len(idx))
+        return [Op(bra + ket, _sorted_rows(s, idx), kind="channel")]
     m = _sorted_rows(_to_np(g.matrix), idx)
     return [Op(ket, m), Op(bra, np.conj(m))]
 

@@ -69,6 +69,59 @@ class Gate:
         return Gate(self.name, self.indices, self.matrix, time=self.time)
 
 
+def embed_operator(num_sites, active_sites, local_ops, local_dim=2, dense=False, factor=False):
+    """Operator on ``num_sites`` sites from local ones (``core/gates.py:8-30``):
+    a Pauli string (one character per active site), one ndarray on contiguous
+    ``active_sites`` (inserted at the first of them), or a list of one-site
+    matrices (``factor``: each halved, the spin-1/2 convention); dense, or a
+    SciPy CSR matrix."""
+    import scipy.sparse as sp
+    if isinstance(local_ops, str):
+        local_ops = [pauli_mapping[op] for op in local_ops]
+    if isinstance(local_ops, np.ndarray):
+        full = [np.eye(local_dim, dtype=complex) for i in range(num_sites) if i not in active_sites]
+        full.insert(active_sites[0], local_ops)
+        return reduce(np.kron, full)
+    if dense:
+        full = [np.eye(local_dim, dtype=complex) for _ in range(num_sites)]
+        for site, op in zip(active_sites, local_ops):
+            full[site] = op / 2 if factor else op
+        return reduce(np.kron, full)
+    full = [sp.eye(local_dim, format="csr", dtype=complex) for _ in range(num_sites)]
+    for site, op in zip(active_sites, local_ops):
+        full[site] = sp.csr_matrix(op / 2 if factor else op)
+    return reduce(sp.kron, full)
+
+
+class SuperOp:
+    """A superoperator on ``span`` contiguous sites from ``start_idx``
+    (``core/gates.py:57-79``), in the layout of ``Gate.to_superop``;
+    ``DensityMatrixSim`` applies its matrix as is (``tensorQ/density_matrix_sim.py:38-42``).
+    The reference's class has no ``shallow_copy``, so its simulators (which copy
+    the circuit) cannot run one; here it copies like a gate."""
+
+    def __init__(self, name, span, matrix, start_idx=0, time=0.0):
+        self.name = name
+        self.start_idx = start_idx
+        self.indices = [start_idx + i for i in range(span)]
+        self.span = span
+        self.matrix = matrix
+        self.shape = matrix.shape
+        self.time = time
+
+    def shift(self, new_start_idx):
+        return SuperOp(self.name, self.span, self.matrix, start_idx=new_start_idx, time=self.time)
+
+    def shallow_copy(self):
+        return self.shift(self.start_idx)
+
+    def get_local_dim(self):
+        return int(round(np.prod(self.shape) ** (1 / (4 * self.span))))
+
+    def __str__(self):
+        return f"{self.name} superoperator on site(s) {self.indices}"
+
+
 class ID(Gate):
     """Idling / noise carrier (``core/gates.py:81-95``)."""
 
@@ -85,6 +138,36 @@ class ID(Gate):
         # The reference's ID inherits Gate.shallow_copy and silently drops its
         # noise model on Circuit.copy(); here the carrier keeps it.
         return ID(self.get_local_dim(), self.time, self.indices, self.nm, self.dd)
+
+
+class CUGate(Gate):
+    """Controlled ``subgate`` (``core/gates.py:102-135``): ``indices`` = (targets
+    ascending and adjacent, control), the control next to the targets; the
+    subgate acts when the control is 1. A control above the targets
+    (``bottom_heavy``) moves to the front of the stored indices; a control below
+    them keeps its place with the matrix transposed to (control, targets) order
+    by the reference's reshape. Long-range controls are not implemented, as in
+    the reference."""
+
+    def __init__(self, indices, subgate):
+        from scipy.linalg import block_diag
+        d = subgate.get_local_dim()
+        sub = np.asarray(subgate.matrix)
+        s = sub.shape[0]
+        idx = np.array([int(i) for i in indices])
+        if np.min(np.abs(idx[:-1] - idx[-1])) > 1:
+            raise NotImplementedError("Long range CUGate has not been implemented yet")
+        mat = block_diag(*([np.eye(s), sub] + [np.eye(s)] * (d - 2)))
+        if idx[-2] < idx[-1]:
+            mat = mat.reshape(d, s, d, s).transpose(1, 0, 3, 2).reshape(d * s, d * s)
+            bottom = False
+        elif idx[-1] < idx[0]:
+            idx = np.concatenate(([idx[-1]], idx[:-1]))
+            bottom = True
+        else:
+            raise ValueError("indices does not have allowed ordering")
+        super().__init__(f"CU{d}", [int(i) for i in idx], mat)
+        self.bottom_heavy = bottom
 
 
 class CNOTGate(Gate):

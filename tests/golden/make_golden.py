@@ -124,6 +124,33 @@ def gen_sv_decomp(R):
           **pack_gates(built.gate_list, prefix="b"))
 
 
+def gen_gates_misc(R):
+    """CUGate matrices and stored indices (both control placements, 1- and
+    2-site subgates) and embed_operator in its three forms, from the reference."""
+    c = R.core
+    rng = np.random.default_rng(17)
+    sub1, sub2 = workloads.haar_unitary(2, rng), workloads.haar_unitary(4, rng)
+    cases = [([1, 2], sub1), ([2, 1], sub1), ([1, 2, 3], sub2), ([2, 3, 1], sub2)]
+    out = {}
+    for i, (idx, sub) in enumerate(cases):
+        g = c.CUGate(idx, c.Gate("u", list(range(int(np.log2(sub.shape[0])))), sub))
+        out[f"cu{i}_in"] = np.array(idx)
+        out[f"cu{i}_idx"] = np.array(g.indices)
+        out[f"cu{i}_mat"] = np.asarray(g.matrix, dtype=np.complex128)
+        out[f"cu{i}_sub"] = sub
+        out[f"cu{i}_bottom"] = np.array(bool(g.bottom_heavy))
+    a = workloads.haar_unitary(4, rng)
+    out["emb_block"] = np.asarray(c.embed_operator(4, [1, 2], a), dtype=np.complex128)
+    out["emb_block_op"] = a
+    ops = [workloads.haar_unitary(2, rng) for _ in range(2)]
+    out["emb_ops"] = np.array(ops)
+    out["emb_dense"] = np.asarray(c.embed_operator(4, [0, 3], ops, dense=True), dtype=np.complex128)
+    out["emb_dense_half"] = np.asarray(c.embed_operator(4, [0, 3], ops, dense=True, factor=True), dtype=np.complex128)
+    out["emb_sparse"] = c.embed_operator(4, [2, 1], ops).toarray()
+    out["emb_pauli"] = c.embed_operator(3, [0, 1, 2], "xyz").toarray()
+    _save("gates_misc.npz", **out)
+
+
 def gen_sv_observables(R):
     """Pauli-string expectations, partial overlaps and outcome probabilities on
     a random 8-qubit state."""
@@ -292,6 +319,7 @@ def main():
     gen_traj_dm10(R, steps=10, p=0.02, gamma=0.03, name="traj_dm10_strong.npz")
     gen_traj_dm10(R, steps=40, p=1e-3, gamma=5e-4, name="traj_dm10.npz")
     gen_sv_decomp(R)
+    gen_gates_misc(R)
 
 
 if __name__ == "__main__":

@@ -76,3 +76,32 @@ def test_u_from_matrix_and_zsx_decomposition_match_the_reference():
     assert np.max(np.abs(ref.run_sv(want, n).reshape(-1) - z["sv_built"])) < 1e-12
     assert np.max(np.abs(ref.run_sv(unpack_gates(z, "u"), n).reshape(-1) - z["sv_plain"])) < 1e-12
     assert not _decomp_circuit(z, True).copy().requires_decomp
+
+
+def test_cugate_and_embed_operator_match_the_reference():
+    """Fixture from the reference (make_golden.py gen_gates_misc)."""
+    from conftest import golden
+    from qaravan_gb300.gates import CUGate, Gate, embed_operator
+    z = golden("gates_misc.npz")
+    for i in range(4):
+        sub = z[f"cu{i}_sub"]
+        g = CUGate(list(z[f"cu{i}_in"]), Gate("u", list(range(int(np.log2(sub.shape[0])))), sub))
+        assert g.indices == list(z[f"cu{i}_idx"]) and g.bottom_heavy == bool(z[f"cu{i}_bottom"])
+        assert np.max(np.abs(g.matrix - z[f"cu{i}_mat"])) < 1e-15
+    assert np.max(np.abs(embed_operator(4, [1, 2], z["emb_block_op"]) - z["emb_block"])) < 1e-15
+    ops = list(z["emb_ops"])
+    assert np.max(np.abs(embed_operator(4, [0, 3], ops, dense=True) - z["emb_dense"])) < 1e-15
+    assert np.max(np.abs(embed_operator(4, [0, 3], ops, dense=True, factor=True) - z["emb_dense_half"])) < 1e-15
+    assert np.max(np.abs(embed_operator(4, [2, 1], ops).toarray() - z["emb_sparse"])) < 1e-15
+    assert np.max(np.abs(embed_operator(3, [0, 1, 2], "xyz").toarray() - z["emb_pauli"])) < 1e-15
+
+
+def test_superop_layers_skip_noise():
+    from qaravan_gb300.circuits import Circuit
+    from qaravan_gb300.gates import H, SuperOp
+    from qaravan_gb300.noise import depolarizing
+    m = np.kron(np.conj(H(0).matrix), H(0).matrix).reshape([2] * 4)
+    c = Circuit([H(0), SuperOp("s", 1, m, start_idx=0), H(1)], n=3)
+    c.construct_layers()  # [[H0, H1], [SuperOp on 0]]
+    c.add_noise(depolarizing(0.01))
+    assert [len(layer) for layer in c.layers] == [2 + 1, 1]  # the SuperOp's layer gets no noise carrier

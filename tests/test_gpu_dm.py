@@ -125,3 +125,26 @@ def test_dm_noisy_tfi_10q(dtype, mode, width, tile):
     zz = sim.pauli_expectations([(1.0, 'i' * q + 'zz' + 'i' * (n - q - 2)) for q in range(n - 1)]).cpu().numpy()
     assert np.max(np.abs(zz - z["zz"])) < 10 * TOL[dtype]
     assert abs(sim.purity() - float(z["purity"])) < 10 * TOL[dtype]
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+def test_superop_applies_its_matrix(dtype):
+    """A SuperOp holding a gate's to_superop() acts like the gate
+    (tensorQ/density_matrix_sim.py:38-42 applies SuperOp.matrix as is); its
+    layer gets no noise carrier (core/circuits.py:64-84)."""
+    from qaravan_gb300 import DensityMatrixSim, workloads
+    from qaravan_gb300.circuits import Circuit
+    from qaravan_gb300.gates import CNOT, Gate, H, SuperOp
+    rng = np.random.default_rng(21)
+    n = 4
+    u = workloads.haar_unitary(4, rng)
+    g = Gate("u", [1, 2], u)
+    with_gate = Circuit([H(0), CNOT([1, 0], n), g, H(3), CNOT([3, 2], n)], n=n)
+    with_sop = Circuit([H(0), CNOT([1, 0], n), SuperOp("u", 2, g.to_superop(), start_idx=1), H(3),
+                        CNOT([3, 2], n)], n=n)
+    a = DensityMatrixSim(with_gate, dtype=dtype).get_density_matrix()
+    b = DensityMatrixSim(with_sop, dtype=dtype).get_density_matrix()
+    a = a.cpu().numpy() if torch.is_tensor(a) else np.asarray(a)
+    b = b.cpu().numpy() if torch.is_tensor(b) else np.asarray(b)
+    tol = 1e-5 if dtype == torch.complex64 else 1e-12
+    assert np.max(np.abs(a - b)) < tol
