@@ -218,12 +218,14 @@ int qgb_pauli_apply(const void* sv, void* out, int dtype, int n, const char* pau
                     const double* coeff, int nterms, int64_t batch, int64_t sv_stride, void* stream);
 
 /* Replaces partial_overlap (tensorQ/statevector_sim.py:155-180) on sites
- * indices[0..k): out[b, r, c] = sum_rest a_b[r, rest] conj(b_b[c, rest]),
- * rows/cols ordered by `indices` as a gate matrix; float64 complex out
- * (device, batch * 4^k double2). */
+ * indices[0..k), 1 <= k <= 10: out[b, r, c] = sum_rest a_b[r, rest]
+ * conj(b_b[c, rest]), rows/cols ordered by `indices` as a gate matrix;
+ * float64 complex out (device, batch * 4^k double2). Scratch:
+ * qgb_partial_overlap_scratch_bytes (for k <= 2 also qgb_reduce_scratch_bytes(n, 32, batch)). */
 int qgb_partial_overlap(const void* a, const void* b, int dtype, int n, const int* indices, int k,
                         int64_t batch, int64_t sv_stride, double* out, void* scratch,
                         size_t scratch_bytes, void* stream);
+size_t qgb_partial_overlap_scratch_bytes(int n, int k, int64_t batch);
 
 /* One step of the adjoint (reverse-mode) gradient sweep for a gate U on
  * sites indices[0..k), k <= 2, in a single pass over two distinct vectors:

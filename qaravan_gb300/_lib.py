@@ -73,6 +73,7 @@ SIGNATURES = {
     "qgb_param_matrices": (C.c_int, [_vp, _vp, _i, _vp, _i, _i64, _vp, _i, _i64, _i64, _vp]),
     "qgb_param_grads": (C.c_int, [_vp, _vp, _i, _i64, _vp, C.c_double, _vp, _vp]),
     "qgb_adjoint_sweep_scratch_bytes": (C.c_size_t, [_i, _i, _i, _i64]),
+    "qgb_partial_overlap_scratch_bytes": (C.c_size_t, [_i, _i, _i64]),
     "qgb_adjoint_sweep_step": (C.c_int, [_vp, _vp, _i, _i, C.POINTER(AdjointSweep), _vp, _i64, _i64, _i64, _vp, _vp,
                                          _sz, _vp]),
     "qgb_adjoint_step_rotation": (C.c_int, [_vp, _vp, _i, _i, _ip, _i, _vp, _i64, _dp, _i64, _i64, _vp, _vp, _sz, _vp]),

@@ -208,6 +208,65 @@ __global__ void __launch_bounds__(kRedThreads) overlap_kernel(const cplx<T>* __r
     block_reduce_store<2 * D * D>(acc.d, partials + (b * 2 * D * D) * gridDim.x + blockIdx.x, gridDim.x);
 }
 
+// Partial overlap on any k <= kOvlMaxK sites: a warp per (row r, column c,
+// chunk of the other bits) sums a[r, rest] conj(b[c, rest]) with lane-strided
+// reads (Acc rule, fixed xor tree); the chunks of a pair are added in order by
+// finish(). partials[((bt * pairs + pair) * 2 + re/im) * chunks + chunk].
+constexpr int kOvlMaxK = 10;
+
+struct OvlArgs {
+    int n, k;
+    int pos[kOvlMaxK];     // flat bit of matrix bit (k-1-j), j = 0 .. k-1
+    int sorted[kOvlMaxK];  // the same bits ascending
+    uint64_t chunks, chunk;  // chunks per pair, rest values per chunk
+};
+
+__host__ __device__ inline uint64_t ovl_chunks(int n, int k) {
+    // about 2^22 / 4^k warps (at least one chunk), each chunk at least 1024 values
+    const uint64_t rest = uint64_t(1) << (n - k);
+    uint64_t c = rest / 1024;
+    const uint64_t cap = (uint64_t(1) << 22) >> (2 * k);
+    if (c > cap) c = cap;
+    return c < 1 ? 1 : c;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) overlap_pair_kernel(const cplx<T>* __restrict__ a,
+                                                                   const cplx<T>* __restrict__ bv, int64_t stride_ab,
+                                                                   const __grid_constant__ OvlArgs o,
+                                                                   double* __restrict__ partials) {
+    const uint64_t w = (uint64_t(blockIdx.x) * kRedThreads + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const uint64_t pairs = uint64_t(1) << (2 * o.k);
+    if (w >= pairs * o.chunks) return;  // whole warps leave together
+    const int64_t bt = blockIdx.y;
+    const cplx<T>* x = a + bt * stride_ab;
+    const cplx<T>* y = bv + bt * stride_ab;
+    const uint64_t pair = w / o.chunks, ch = w - pair * o.chunks;
+    const int r = int(pair >> o.k), c = int(pair & ((uint64_t(1) << o.k) - 1));
+    const uint64_t offr = matrix_offset(r, o.pos, o.k), offc = matrix_offset(c, o.pos, o.k);
+    Acc<T, 2> acc;
+    for (uint64_t t = ch * o.chunk + lane; t < (ch + 1) * o.chunk; t += 32) {
+        const uint64_t base = insert_zeros(t, o.sorted, o.k);
+        const cplx<T> u = x[base | offr], v = y[base | offc];
+        acc.add(0, u.x * v.x + u.y * v.y);  // u conj(v)
+        acc.add(1, u.y * v.x - u.x * v.y);
+        acc.step();
+    }
+    acc.flush();
+    double re = acc.d[0], im = acc.d[1];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        re += __shfl_xor_sync(0xffffffffu, re, off);
+        im += __shfl_xor_sync(0xffffffffu, im, off);
+    }
+    if (lane == 0) {
+        double* p = partials + ((uint64_t(bt) * pairs + pair) * 2) * o.chunks + ch;
+        p[0] = re;
+        p[o.chunks] = im;
+    }
+}
+
 // DM: Tr(rho P) for one Pauli group: sum_x rho[x, x ^ xmask] i^ny (-1)^{pop(x & zmask)}.
 template <typename T, int NT>
 __global__ void __launch_bounds__(kRedThreads) dm_pauli_kernel(const cplx<T>* __restrict__ rho, int n, int64_t stride,
@@ -595,13 +654,68 @@ extern "C" int qgb_dm_pauli_expectation(const void* rho, int dtype, int n, const
                              (cudaStream_t)stream);
 }
 
+extern "C" size_t qgb_partial_overlap_scratch_bytes(int n, int k, int64_t batch) {
+    if (n < 1 || n > 2 * QGB_MAX_QUBITS || k < 1 || k > n || k > kOvlMaxK || batch < 1) return 0;
+    if (k <= 2) return red_scratch(n, 2 << (2 * k), batch);
+    return sizeof(double) * size_t(batch) * (size_t(2) << (2 * k)) * size_t(ovl_chunks(n, k));
+}
+
+namespace {
+
+// k > 2: the warp-per-pair kernel.
+int partial_overlap_wide(const void* a, const void* b, int dtype, int n, const int* indices, int k, int64_t batch,
+                         int64_t sv_stride, double* out, void* scratch, size_t scratch_bytes, cudaStream_t st) {
+    OvlArgs o{};
+    o.n = n;
+    o.k = k;
+    uint64_t seen = 0;
+    for (int j = 0; j < k; ++j) {
+        if (indices[j] < 0 || indices[j] >= n) return set_error(QGB_EINVAL, "site out of range");
+        const int p = n - 1 - indices[j];
+        if ((seen >> p) & 1ull) return set_error(QGB_EINVAL, "repeated site");
+        seen |= 1ull << p;
+        o.pos[j] = o.sorted[j] = p;
+    }
+    for (int i = 1; i < k; ++i)
+        for (int j = i; j > 0 && o.sorted[j - 1] > o.sorted[j]; --j) {
+            const int t = o.sorted[j];
+            o.sorted[j] = o.sorted[j - 1];
+            o.sorted[j - 1] = t;
+        }
+    o.chunks = ovl_chunks(n, k);
+    o.chunk = (uint64_t(1) << (n - k)) / o.chunks;
+    const uint64_t pairs = uint64_t(1) << (2 * k);
+    const size_t need = sizeof(double) * size_t(batch) * size_t(2 * pairs) * size_t(o.chunks);
+    if (!scratch || scratch_bytes < need)
+        return set_error(QGB_ESCRATCH, "scratch of %zu bytes needed (qgb_partial_overlap_scratch_bytes)", need);
+    const uint64_t blocks = (pairs * o.chunks * 32 + kRedThreads - 1) / kRedThreads;
+    if (blocks > 0x7fffffffull) return set_error(QGB_EINVAL, "partial overlap too large");
+    const dim3 grid(static_cast<unsigned>(blocks), static_cast<unsigned>(batch));
+    if (dtype == QGB_C64)
+        overlap_pair_kernel<float><<<grid, kRedThreads, 0, st>>>((const float2*)a, (const float2*)b, sv_stride, o,
+                                                                 (double*)scratch);
+    else
+        overlap_pair_kernel<double><<<grid, kRedThreads, 0, st>>>((const double2*)a, (const double2*)b, sv_stride, o,
+                                                                  (double*)scratch);
+    int rc = check_launch("partial overlap (wide)");
+    if (rc) return rc;
+    // out[bt * 2 pairs + 2 pair + re/im] = sum over chunks: the same layout as the k <= 2 path
+    return finish((const double*)scratch, int(o.chunks), int(2 * pairs), batch, nullptr, out, st);
+}
+
+}  // namespace
+
 extern "C" int qgb_partial_overlap(const void* a, const void* b, int dtype, int n, const int* indices, int k,
                                    int64_t batch, int64_t sv_stride, double* out, void* scratch, size_t scratch_bytes,
                                    void* stream) {
     int rc = check_common(a, dtype, n, batch, sv_stride);
     if (rc) return rc;
     if (!b || !out || !indices) return set_error(QGB_EINVAL, "null pointer");
-    if (k < 1 || k > 2 || k > n) return set_error(QGB_EINVAL, "partial overlap supports 1 or 2 sites (k=%d)", k);
+    if (k < 1 || k > n || k > kOvlMaxK)
+        return set_error(QGB_EINVAL, "partial overlap supports 1 to %d sites (k=%d)", kOvlMaxK, k);
+    if (k > 2)
+        return partial_overlap_wide(a, b, dtype, n, indices, k, batch, sv_stride, out, scratch, scratch_bytes,
+                                    (cudaStream_t)stream);
     const int slots = 2 << (2 * k);
     if (!scratch || scratch_bytes < red_scratch(n, slots, batch)) return set_error(QGB_ESCRATCH, "scratch too small");
     OverlapArgs o{};

@@ -465,6 +465,9 @@ class Givens(ParamGate):
         c, s = xp.cos(th / 2), xp.sin(th / 2)
         return _arr([[1, 0, 0, 0], [0, c, -s, 0], [0, s, c, 0], [0, 0, 0, 1]], self.backend)
 
+    def solve_angles(self):
+        return (np.arccos(self.matrix[1, 1]) * 2,)  # core/param_gates.py:185-187
+
 
 def kak_unitary(params):
     """15-parameter two-qubit unitary (``core/param_gates.py:247-259``)."""
