@@ -82,9 +82,8 @@ class _Runner:
         else:
             plan = compile_ops(ops, n, mode=self.sim.mode, width=self.sim.fusion_width, tile_bits=self.sim.tile_bits,
                                low_bits=self.sim.low_bits, max_sweep_k=kcap, itemsize=isz, device_fusion=True)
-        psi = torch.empty(2 ** n, dtype=self.dtype, device=self.device)
-        L = _lib.lib()
-        _lib.check(L.qgb_init_basis(psi.data_ptr(), self.code, n, 0, 1, 0, _lib.stream_ptr(self.device)), "init")
+        self.sim.initialize_state()  # |0..0>, a bitstring or a given array, as the simulator starts
+        psi = self.sim.state.detach().reshape(-1).clone()
         Executor(plan, self.dtype, self.device).run(psi)
         return psi
 

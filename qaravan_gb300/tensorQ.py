@@ -27,15 +27,65 @@ import torch
 
 from . import _lib
 from . import measure as _measure
-from .density_matrix import DensityMatrixSim
+from .density_matrix import DensityMatrixSim as _DensityMatrixSim
 from .environments import environment_state_prep, environment_update, sv_environment
 from .montecarlo import MonteCarloSim
 from .paulis import pauli_masks
-from .statevector import StatevectorSim, inner_product
+from .statevector import StatevectorSim as _StatevectorSim
+from .statevector import inner_product
 
 __all__ = ["StatevectorSim", "DensityMatrixSim", "MonteCarloSim", "locs_to_indices", "op_action", "all_zero_sv",
            "random_sv", "partial_overlap", "rdm_from_sv", "measure_sv", "measure_and_collapse_sv",
            "pauli_expectation_sv", "sv_environment", "environment_update", "environment_state_prep"]
+
+
+# --------------------------------------------------------------- simulators
+
+class StatevectorSim(_StatevectorSim):
+    """``StatevectorSim`` with the reference's constructor defaults
+    (``tensorQ/statevector_sim.py:13-29``): ``backend="numpy"`` gives NumPy
+    results in complex128 (the reference's NumPy path), ``backend="torch"``
+    torch results in complex64 (its ``to_backend`` cast) on ``device``
+    (default ``"cpu"``, differentiable when gate matrices require grad). The
+    state itself lives and evolves on the GPU; ``dtype`` and the execution
+    options of ``qaravan_gb300.StatevectorSim`` may be given as keywords."""
+
+    def __init__(self, circ, init_state=None, backend="numpy", device="cpu", **kw):
+        dtype = kw.pop("dtype", torch.complex128 if backend == "numpy" else torch.complex64)
+        super().__init__(circ, init_state=init_state, backend=backend, device="cuda", dtype=dtype, **kw)
+        self.result_device = torch.device(device)
+
+    def _result(self, t):
+        if self.backend == "numpy":
+            return t.detach().cpu().numpy()
+        return t.to(self.result_device) if t.device != self.result_device else t
+
+    def run(self, progress_bar=True, debug=0):
+        """Runs the circuit and returns the state as a rank-n array (``core/base_sim.py:30-53``)."""
+        return self._result(super().run(progress_bar=progress_bar, debug=debug))
+
+    def get_statevector(self):
+        if not self.ran:
+            super().run(progress_bar=False)
+        return self._result(self.state.reshape(2 ** self.num_sites))
+
+
+class DensityMatrixSim(_DensityMatrixSim):
+    """``DensityMatrixSim(circ, init_state=None, nm=None)`` with the reference's
+    NumPy results in complex128 (``tensorQ/density_matrix_sim.py:8-89``); the
+    density matrix lives and evolves on the GPU."""
+
+    def __init__(self, circ, init_state=None, nm=None, **kw):
+        kw.setdefault("dtype", torch.complex128)
+        super().__init__(circ, init_state=init_state, nm=nm, **kw)
+
+    def run(self, progress_bar=True, debug=0):
+        """Runs the circuit and returns rho as a rank-2n array (``core/base_sim.py:30-53``)."""
+        out = super().run(progress_bar=progress_bar, debug=debug)
+        return out.detach().cpu().numpy().reshape([2] * (2 * self.num_sites))
+
+    def get_density_matrix(self):
+        return super().get_density_matrix().detach().cpu().numpy()
 
 
 # ----------------------------------------------------------------- helpers

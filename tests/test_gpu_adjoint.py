@@ -200,3 +200,44 @@ def test_rotation_angles_mixed_with_matrix_leaves_and_replaced_gates(when):
     else:
         assert abs(g_th[6]) > 1e-3
     assert np.max(np.abs(fr.grad.numpy() - g_fr)) < 1e-10
+
+
+@pytest.mark.parametrize("init", ["bitstring", "array"])
+def test_adjoint_energy_starts_from_the_initial_state(init):
+    """The differentiable run starts where StatevectorSim.initialize_state does
+    (core/base_sim.py:30-53 with tensorQ/statevector_sim.py:31-48): energy and
+    gradients against the oracle's autograd from the same initial state."""
+    from qaravan_gb300 import StatevectorSim, workloads
+    from qaravan_gb300.adjoint import adjoint_energy
+    from qaravan_gb300.hamiltonians import TFI
+    n, layers = 6, 2
+    params = workloads.hea_params(n, layers, 31)
+    rng = np.random.default_rng(32)
+    if init == "bitstring":
+        init_state = "011010"
+    else:
+        v = rng.normal(size=2 ** n) + 1j * rng.normal(size=2 ** n)
+        init_state = v / np.linalg.norm(v)
+    terms = TFI(n, 1, 0.6).pauli_sum()
+    th = torch.tensor(params, dtype=torch.float64, requires_grad=True)
+    e = adjoint_energy(StatevectorSim(workloads.hea_circuit(n, layers, th), init_state=init_state,
+                                      dtype=torch.complex128), terms)
+    e.backward()
+    th2 = torch.tensor(params, dtype=torch.float64, requires_grad=True)
+    circ = workloads.hea_circuit(n, layers, th2)
+    st = torch.tensor(ref.initial_sv(n, init_state), dtype=torch.complex128).reshape([2] * n)
+    for layer in ref.construct_layers(circ.gate_list):
+        for g in layer:
+            m = g.matrix if torch.is_tensor(g.matrix) else torch.tensor(np.asarray(g.matrix), dtype=torch.complex128)
+            st = ref.op_action_torch(m, g.indices, st)
+    pauli = {"x": [[0, 1], [1, 0]], "y": [[0, -1j], [1j, 0]], "z": [[1, 0], [0, -1]]}
+    e2 = 0
+    for c, s in terms:
+        v = st
+        for q, ch in enumerate(s):
+            if ch != "i":
+                v = ref.op_action_torch(torch.tensor(pauli[ch], dtype=torch.complex128), [q], v)
+        e2 = e2 + c * torch.vdot(st.reshape(-1), v.reshape(-1)).real
+    e2.backward()
+    assert abs(float(e) - float(e2)) < 1e-12
+    assert torch.max(torch.abs(th.grad - th2.grad)).item() < 1e-9

@@ -127,3 +127,60 @@ def test_measurements_repeatable_distributed_and_collapsed():
     want = ref.collapse_sv(sv, [4, 0], out) if hasattr(ref, "collapse_sv") else None
     if want is not None:
         assert np.max(np.abs(post - want.reshape(-1))) < 1e-12
+
+
+def test_reference_default_simulators_return_numpy_complex128():
+    """tensorQ.StatevectorSim(circ) / DensityMatrixSim(circ, nm=...) with the
+    reference's defaults: NumPy results in complex128, against the reference's
+    own outputs (fixtures)."""
+    from conftest import golden
+    from gateio import unpack_gates
+    from qaravan_gb300.circuits import Circuit
+    from qaravan_gb300.gates import CNOT, H
+    from qaravan_gb300.noise import QubitNoise
+    from qaravan_gb300.paulis import pauli_Z
+    from qaravan_gb300.tensorQ import DensityMatrixSim, StatevectorSim
+    z = golden("sv_brickwork12.npz")
+    sim = StatevectorSim(Circuit(unpack_gates(z), n=int(z["n"])))
+    sv = sim.get_statevector()
+    assert isinstance(sv, np.ndarray) and sv.dtype == np.complex128
+    assert np.max(np.abs(sv - z["sv"])) < 1e-12
+    state = sim.run(progress_bar=False)
+    assert isinstance(state, np.ndarray) and state.shape == (2,) * int(z["n"])
+    k = golden("dm_kats.npz")
+    dm = DensityMatrixSim(Circuit([H(0), CNOT([1, 0], 3), CNOT([2, 1], 3)], 3), nm=QubitNoise(1000, 1000, 1, 5))
+    rho = dm.get_density_matrix()
+    assert isinstance(rho, np.ndarray) and np.max(np.abs(rho - k["thermal_dm"])) < 1e-12
+    assert abs(dm.local_expectation([pauli_Z] * 3) - 0.020609303627304454) < 1e-12
+
+
+def test_reference_torch_backend_compilation_pattern():
+    """The reference's compilation loss (applications/compilation.py:73-90):
+    StatevectorSim(ansatz, backend="torch", init_state=...) on the default CPU
+    device, torch.dot against a CPU target, backward to the angles -- against
+    the same loss through the oracle's torch op_action (complex64 results)."""
+    from qaravan_gb300 import workloads
+    from qaravan_gb300.tensorQ import StatevectorSim
+    n, layers = 6, 2
+    params = workloads.hea_params(n, layers, 13)
+    rng = np.random.default_rng(14)
+    in_state, out_state = _sv(n, 15), _sv(n, 16)
+    th = torch.tensor(params, dtype=torch.float64, requires_grad=True)
+    sim = StatevectorSim(workloads.hea_circuit(n, layers, th), backend="torch", init_state=in_state)
+    sim.run(progress_bar=False)
+    ansatz_sv = sim.get_statevector()
+    assert ansatz_sv.device.type == "cpu" and ansatz_sv.dtype == torch.complex64
+    target = torch.tensor(out_state, dtype=torch.complex128)
+    loss = 1 - torch.abs(torch.dot(ansatz_sv.to(torch.complex128).conj(), target)) ** 2
+    loss.backward()
+    th2 = torch.tensor(params, dtype=torch.float64, requires_grad=True)
+    circ = workloads.hea_circuit(n, layers, th2)
+    st = torch.tensor(in_state, dtype=torch.complex128).reshape([2] * n)
+    for layer in ref.construct_layers(circ.gate_list):
+        for g in layer:
+            m = g.matrix if torch.is_tensor(g.matrix) else torch.tensor(np.asarray(g.matrix), dtype=torch.complex128)
+            st = ref.op_action_torch(m, g.indices, st)
+    loss2 = 1 - torch.abs(torch.dot(st.reshape(-1).conj(), target)) ** 2
+    loss2.backward()
+    assert abs(loss.item() - loss2.item()) < 1e-5
+    assert torch.max(torch.abs(th.grad - th2.grad)).item() < 1e-4
