@@ -59,7 +59,8 @@ class DensityMatrixBatch:
         for i, s in enumerate(self.sims):
             ops = s.op_sequence()
             nb = 2 * s.num_sites
-            (small if (nb <= self.small_max and None not in ops) else large).append((i, s, ops))
+            one_kernel = None not in ops and not any(o.kind == "pauli_mix" for o in ops)  # else per-circuit plans
+            (small if (nb <= self.small_max and one_kernel) else large).append((i, s, ops))
         self._prep_small(small)
         self._prep_large(large, max_streams)
         self.graph = None

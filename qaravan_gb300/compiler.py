@@ -39,7 +39,8 @@ from ._lib import QGB_SWEEP_MAX_HIGH, QGB_SWEEP_MAX_OPS, QGB_SWEEP_MAX_TILE_BITS
 class Op:
     bits: list
     matrix: np.ndarray  # complex128, 2^k x 2^k
-    kind: str = "unitary"  # "unitary" | "nonunitary"
+    kind: str = "unitary"  # "unitary" | "nonunitary" | "channel" | "pauli_mix"
+    terms: list = None  # "pauli_mix": [(coeff, Pauli string over the vector's bits, char j <-> bit nbits-1-j)]
 
 
 @dataclass
@@ -59,6 +60,13 @@ class SweepStep:
 @dataclass
 class NormalizeStep:
     pass
+
+
+@dataclass
+class PauliMixStep:
+    """v <- sum_t coeff_t P_t v over the whole vector (a Pauli channel on vec(rho)
+    wider than a dense block: rho -> sum_k p_k P_k rho P_k^dagger)."""
+    terms: list
 
 
 @dataclass
@@ -345,7 +353,7 @@ def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, 
     """
     tile_bits = min(tile_bits, 14 if itemsize <= 8 else 13)
     key = None
-    if device_fusion and mode != "gate" and ops:
+    if device_fusion and mode != "gate" and ops and not any(o is not None and o.kind == "pauli_mix" for o in ops):
         flags = unitary_flags([o for o in ops if o is not None])
         key = (nbits, mode, width, tile_bits, low_bits, max_sweep_k, itemsize,
                tuple(None if o is None else tuple(o.bits) for o in ops), tuple(flags))
@@ -355,9 +363,9 @@ def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, 
     plan = Plan(nbits=nbits, n_gates=sum(1 for o in ops if o is not None))
     segments, cur = [], []
     for o in ops:
-        if o is None:
+        if o is None or o.kind == "pauli_mix":
             segments.append(cur)
-            segments.append(None)
+            segments.append(o)
             cur = []
         else:
             cur.append(o)
@@ -365,6 +373,9 @@ def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, 
     for seg in segments:
         if seg is None:
             plan.steps.append(NormalizeStep())
+            continue
+        if isinstance(seg, Op):  # a Pauli mixture: its own pass
+            plan.steps.append(PauliMixStep(list(seg.terms)))
             continue
         if not seg:
             continue

@@ -51,12 +51,32 @@ def _sorted_rows(mat, idx):
     return mat[perm, :]
 
 
+def _pauli_mix_op(nm, idx, n):
+    """A Pauli channel on sites ``idx`` too wide for a dense superoperator block,
+    as a Pauli mixture on vec(rho): rho -> sum_k w_k P_k rho P_k^dagger is
+    sum_k w_k (P_k on the ket sites) (conj(P_k) = (-1)^#Y P_k on the bra sites).
+    w_k = conj(sqrt p_k) sqrt p_k with the reference's Kraus operators
+    sqrt(p_k) P_k (core/noise.py:90-129, emath square root: |p_k|)."""
+    terms = []
+    for p, s in zip(nm.probs, nm.strings):
+        r = np.emath.sqrt(p)
+        w = float((np.conj(r) * r).real)
+        chars = ["i"] * (2 * n)
+        for j, q in enumerate(idx):
+            chars[q] = s[j]  # ket site q: vec bit 2n-1-q
+            chars[n + q] = s[j]  # bra site q: vec bit n-1-q
+        terms.append((w * (-1) ** s.lower().count("y"), "".join(chars)))
+    return Op([], None, kind="pauli_mix", terms=terms)
+
+
 def dm_ops_for_gate(g, n):
     """Ops on vec(rho) for one reference op (gate, Reset projector or noise carrier)."""
     idx = [int(q) for q in g.indices]
     ket = [2 * n - 1 - q for q in idx]
     bra = [n - 1 - q for q in idx]
     if g.name == "ID" and getattr(g, "nm", None) is not None:
+        if 2 * len(idx) > 6 and hasattr(g.nm, "strings") and hasattr(g.nm, "probs"):
+            return [_pauli_mix_op(g.nm, idx, n)]
         s = np.asarray(g.nm.get_superop(g.time, getattr(g, "dd", False)), dtype=np.complex128)
         s = s.reshape(4 ** len(idx), 4 ** len(idx))
         return [Op(bra + ket, _sorted_rows(s, idx), kind="channel")]

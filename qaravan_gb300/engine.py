@@ -19,7 +19,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .compiler import DenseStep, NormalizeStep, Plan, Recipe, SweepStep
+from .compiler import DenseStep, NormalizeStep, PauliMixStep, Plan, Recipe, SweepStep
 
 # Unitary fused blocks go through qgb_op_action_unitary, whose tensor-core path
 # restores each amplitude group's norm (removing the round-toward-zero shrinkage
@@ -105,6 +105,11 @@ class Executor:
                 self._steps.append(("sweep", sw))
             elif isinstance(s, NormalizeStep):
                 self._steps.append(("normalize",))
+            elif isinstance(s, PauliMixStep):
+                if len(s.terms) > 128:
+                    raise NotImplementedError("Pauli channels of more than 128 terms")
+                strings = "".join(t[1].lower() for t in s.terms).encode()
+                self._steps.append(("pauli_mix", strings, _lib.double_array([t[0] for t in s.terms]), len(s.terms)))
         self.scratch = Scratch(self.device)
         self.norm = torch.empty(1, dtype=torch.float64, device=self.device)
         self.launches = 0
@@ -210,6 +215,18 @@ class Executor:
                 _lib.check(L.qgb_apply_sweep(ptr, self.code, nb, C.byref(s[1]), mptr, mat_stride, batch, stride, st),
                            "apply_sweep")
                 launches += 1
+            elif s[0] == "pauli_mix":
+                _, strings, coeff, nterms = s
+                if getattr(self, "_mix_buf", None) is None or self._mix_buf.numel() < state.numel():
+                    self._mix_buf = torch.empty(state.numel(), dtype=self.dtype, device=state.device)
+                tmp = self._mix_buf[:state.numel()]
+                _lib.check(L.qgb_pauli_apply(ptr, tmp.data_ptr(), self.code, nb, strings, coeff, nterms, batch,
+                                             stride, st), "pauli_apply")
+                flat, dim = state.view(-1), 2 ** nb
+                for b in range(batch):  # only the vectors (a stride may leave gaps)
+                    o = b * (stride if batch > 1 else 0)
+                    flat[o:o + dim].copy_(tmp[o:o + dim])
+                launches += 1 + batch
             else:
                 launches += self.normalize(state, batch, stride)
             if events is not None and s[0] != "normalize":

@@ -36,7 +36,8 @@ from .statevector import inner_product
 
 __all__ = ["StatevectorSim", "DensityMatrixSim", "MonteCarloSim", "locs_to_indices", "op_action", "all_zero_sv",
            "random_sv", "partial_overlap", "rdm_from_sv", "measure_sv", "measure_and_collapse_sv",
-           "pauli_expectation_sv", "sv_environment", "environment_update", "environment_state_prep"]
+           "pauli_expectation_sv", "sv_environment", "environment_update", "environment_state_prep", "random_dm",
+           "all_zero_dm", "partial_trace", "expectation"]
 
 
 # --------------------------------------------------------------- simulators
@@ -255,6 +256,43 @@ def partial_overlap(sv1, sv2, local_dim=2, skip=None):
 def rdm_from_sv(sv, sites, local_dim=2):
     """Reduced density matrix of ``sites`` (ascending) (``:182-183``)."""
     return partial_overlap(sv, sv, local_dim=local_dim, skip=sites)
+
+
+def random_dm(n):
+    """a a^H / Tr with uniform [0, 1) real and imaginary parts of a from NumPy's
+    global random state (``tensorQ/density_matrix_sim.py:108-111``)."""
+    a = np.random.rand(2 ** n, 2 ** n) + 1.j * np.random.rand(2 ** n, 2 ** n)
+    a = a @ a.conj().T
+    return a / np.trace(a)
+
+
+def all_zero_dm(n, local_dim=2):
+    """|0..0><0..0| (``tensorQ/density_matrix_sim.py:113-116``)."""
+    dm = np.zeros((local_dim ** n, local_dim ** n))
+    dm[0, 0] = 1.0
+    return dm
+
+
+def partial_trace(dm, sites, local_dim=2):
+    """Reduced density matrix of the kept ``sites`` (ascending) of a host
+    density matrix (``tensorQ/density_matrix_sim.py:118-145``): the real trace
+    for no site, ``dm`` itself for all sites."""
+    size = int(round(np.log(dm.shape[0]) / np.log(local_dim)))
+    sites = sorted(int(q) for q in sites)
+    if not sites:
+        return np.trace(dm).real
+    if len(sites) == size:
+        return dm
+    t = np.asarray(dm).reshape([local_dim] * (2 * size))
+    rest = [q for q in range(size) if q not in sites]
+    t = t.transpose(sites + rest + [size + q for q in sites] + [size + q for q in rest])
+    d, r = local_dim ** len(sites), local_dim ** len(rest)
+    return np.einsum("arbr->ab", t.reshape(d, r, d, r))
+
+
+def expectation(dm, op):
+    """Re Tr(dm op) (``tensorQ/density_matrix_sim.py:147-148``)."""
+    return np.trace(dm @ op).real
 
 
 def _global_seed():

@@ -1,0 +1,87 @@
+"""Trotter applications (applications/trotter.py) on the GPU against the
+oracle's restatement: the statevector run step by step (dense magnetisation
+and a Pauli sum), the noisy density-matrix run step by step and from scratch,
+and the host helpers of tensorQ/density_matrix_sim.py."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import ref
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built(cuda_ok):
+    from qaravan_gb300 import build
+    build.build()
+
+
+def test_trotter_sv_sim_matches_oracle():
+    from qaravan_gb300.applications import magnetization, trotter_sv_sim
+    from qaravan_gb300.hamiltonians import TFI
+    n, dt, steps = 6, 0.1, 5
+    ham = TFI(n, jz=1.0, h=0.7)
+    op = magnetization(n)
+    got = trotter_sv_sim(ham, dt, steps, op)
+    gates = ham.trotter_circ(dt, 1).gate_list
+    cur = ref.initial_sv(n)
+    want = []
+    for _ in range(steps):
+        cur = ref.run_sv(gates, n, init_state=cur).reshape(-1)
+        want.append(np.vdot(cur, op @ cur).real)
+    assert np.max(np.abs(np.array(got) - want)) < 1e-12
+    terms = [(1.0, "z" + "i" * (n - 1)), (0.5, "i" * (n - 2) + "xx")]
+    got_p = trotter_sv_sim(ham, dt, 3, terms)
+    cur = ref.initial_sv(n)
+    for s in range(3):
+        cur = ref.run_sv(gates, n, init_state=cur).reshape(-1)
+        assert abs(got_p[s] - sum(c * ref.pauli_expectation_sv(cur, p) for c, p in terms)) < 1e-12
+
+
+def test_trotter_dm_sim_cached_and_uncached_match_oracle():
+    from qaravan_gb300.applications import magnetization, trotter_dm_sim, trotter_dm_sim_uncached
+    from qaravan_gb300.circuits import Circuit
+    from qaravan_gb300.hamiltonians import TFI
+    from qaravan_gb300.noise import PauliNoise
+    n, dt, steps = 4, 0.1, 4
+    ham = TFI(n, jz=1.0, h=0.9)
+    # circuit-level Pauli noise is one channel over all sites after each layer (core/circuits.py:64-84)
+    ch = PauliNoise(["iiii", "xiii", "iziz", "yyii", "iixx"], [0.92, 0.02, 0.03, 0.01, 0.02])
+    op = magnetization(n)
+    got = trotter_dm_sim(ham, dt, steps, ch, op)
+    got_u = trotter_dm_sim_uncached(ham, dt, steps, ch, op)
+    # cached: one step's layers (each followed by the channel) applied again and again
+    c = ham.trotter_circ(dt, 1)
+    c.build(ch)
+    seq = [g for layer in c.layers for g in layer]
+    rho = None
+    want = []
+    for _ in range(steps):
+        rho = ref.run_dm(seq, n, init_state=rho, layered=False)
+        want.append(np.trace(op @ rho.reshape(2 ** n, 2 ** n)).real)
+    assert np.max(np.abs(np.array(got) - want)) < 1e-12
+    # uncached: the layers of the whole num_steps circuit (the greedy layering may merge steps)
+    want_u = []
+    for k in range(1, steps + 1):
+        c = ham.trotter_circ(dt, k)
+        c.build(ch)
+        r = ref.run_dm([g for layer in c.layers for g in layer], n, layered=False)
+        want_u.append(np.trace(op @ r.reshape(2 ** n, 2 ** n)).real)
+    assert np.max(np.abs(np.array(got_u) - want_u)) < 1e-12
+
+
+def test_dm_host_helpers():
+    from qaravan_gb300.tensorQ import all_zero_dm, expectation, partial_trace, random_dm, rdm_from_sv
+    np.random.seed(3)
+    rho = random_dm(4)
+    assert abs(np.trace(rho) - 1) < 1e-12 and np.max(np.abs(rho - rho.conj().T)) < 1e-12
+    assert all_zero_dm(3)[0, 0] == 1 and all_zero_dm(3).sum() == 1
+    v = np.random.default_rng(1).normal(size=16) + 1j * np.random.default_rng(2).normal(size=16)
+    v /= np.linalg.norm(v)
+    full = np.outer(v, v.conj())
+    for sites in ([2], [3, 0], [1, 2, 3]):
+        assert np.max(np.abs(partial_trace(full, sites) - rdm_from_sv(v, sites))) < 1e-12
+    assert abs(partial_trace(full, []) - 1) < 1e-12
+    z = np.kron(np.diag([1, -1]), np.eye(8))
+    assert abs(expectation(full, z) - np.vdot(v, z @ v).real) < 1e-12
