@@ -15,11 +15,11 @@ from __future__ import annotations
 import numpy as np
 import torch
 
-from .density_matrix import DensityMatrixSim
-from .gates import embed_operator
-from .montecarlo import MonteCarloSim, trotter_mc_sim
-from .paulis import pauli_Z
-from .statevector import StatevectorSim, inner_product, pauli_expectations
+from ..density_matrix import DensityMatrixSim
+from ..gates import embed_operator
+from ..montecarlo import MonteCarloSim, trotter_mc_sim
+from ..paulis import pauli_Z
+from ..statevector import StatevectorSim, inner_product, pauli_expectations
 
 __all__ = ["magnetization", "trotter_sv_sim", "trotter_dm_sim", "trotter_dm_sim_uncached", "trotter_mc_sim",
            "trotter_mc_sim_uncached"]

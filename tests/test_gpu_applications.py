@@ -85,3 +85,41 @@ def test_dm_host_helpers():
     assert abs(partial_trace(full, []) - 1) < 1e-12
     z = np.kron(np.diag([1, -1]), np.eye(8))
     assert abs(expectation(full, z) - np.vdot(v, z @ v).real) < 1e-12
+
+
+def test_msp_infidelity_gradient_and_autodiff_loop():
+    """The compilation loss (applications/compilation.py:73-90) with the torch
+    backend: value and gradient against the oracle's autograd through the same
+    dressed-CNOT circuit; a few Adam steps lower it."""
+    from qaravan_gb300.applications import dressed_cnot_circ, msp_infidelity, msp_via_autodiff
+    from qaravan_gb300.circuits import brickwall_skeleton
+    from qaravan_gb300.environments import RunContext
+    n = 3
+    sk = brickwall_skeleton(n, 1, 2)
+    rng = np.random.default_rng(51)
+    in_states = [np.eye(2 ** n)[i] for i in (0, 5)]
+    out_states = []
+    for _ in range(2):
+        v = rng.normal(size=2 ** n) + 1j * rng.normal(size=2 ** n)
+        out_states.append(v / np.linalg.norm(v))
+    p0 = rng.uniform(0, 2 * np.pi, size=len(sk) * 6 + n * 3)
+    th = torch.tensor(p0, requires_grad=True)
+    loss = msp_infidelity(th, sk, in_states, out_states, backend="torch")
+    loss.backward()
+    th2 = torch.tensor(p0, requires_grad=True)
+    circ = dressed_cnot_circ(sk, n, th2)
+    want = 0
+    for a, b in zip(in_states, out_states):
+        st = torch.tensor(a, dtype=torch.complex128).reshape([2] * n)
+        for layer in ref.construct_layers(circ.gate_list):
+            for g in layer:
+                m = g.matrix if torch.is_tensor(g.matrix) else torch.tensor(np.asarray(g.matrix), dtype=torch.complex128)
+                st = ref.op_action_torch(m, g.indices, st)
+        want = want + 1 - torch.abs(torch.dot(st.reshape(-1).conj(), torch.tensor(b))) ** 2
+    want = want / 2
+    want.backward()
+    assert abs(loss.item() - want.item()) < 1e-5  # complex64 statevector, as the reference's torch path
+    assert torch.max(torch.abs(th.grad - th2.grad)).item() < 1e-4
+    params, state = msp_via_autodiff(in_states, out_states, sk, init_params=p0, lr=0.05,
+                                     context=RunContext(max_iter=15, quiet=True))
+    assert state["cost_list"][-1] < state["cost_list"][0]
