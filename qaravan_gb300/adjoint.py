@@ -82,8 +82,9 @@ class _Runner:
         else:
             plan = compile_ops(ops, n, mode=self.sim.mode, width=self.sim.fusion_width, tile_bits=self.sim.tile_bits,
                                low_bits=self.sim.low_bits, max_sweep_k=kcap, itemsize=isz, device_fusion=True)
-        self.sim.initialize_state()  # |0..0>, a bitstring or a given array, as the simulator starts
-        psi = self.sim.state.detach().reshape(-1).clone()
+        self.sim.initialize_state()  # |0..0>, a bitstring or a given array (copied), as the simulator starts
+        psi = self.sim.state.detach().reshape(-1)
+        self.sim.state = None  # psi is the only reference: no extra state-sized buffer
         Executor(plan, self.dtype, self.device).run(psi)
         return psi
 

@@ -122,7 +122,7 @@ def test_adjoint_memory_is_state_sized():
     torch.cuda.synchronize()
     peak = torch.cuda.max_memory_allocated() - base
     state = 2 ** n * 8
-    assert peak < 5 * state, peak / state
+    assert peak < 3.5 * state, peak / state  # state, co-state and the uncomputed copy
     assert np.all(np.isfinite(th.grad.numpy()))
 
 
