@@ -116,9 +116,18 @@ class _Runner:
         run = []
 
         def flush():
-            for lo, high, ops in _plan_reverse(run, n, tile):
-                sw = _adjoint_sweep_struct(lo, high, [(bits, int(offs[i]), i * 32 if kind else -1, kind)
-                                                      for (i, kind), bits in ops])
+            if not run:
+                return
+            key = (n, tile, tuple((i, kind, tuple(bits), int(offs[i])) for (i, kind), bits in run))
+            sweeps = _REV_CACHE.pop(key, None)
+            if sweeps is None:
+                sweeps = [_adjoint_sweep_struct(lo, high, [(bits, int(offs[i]), i * 32 if kind else -1, kind)
+                                                           for (i, kind), bits in ops])
+                          for lo, high, ops in _plan_reverse(run, n, tile)]
+            _REV_CACHE[key] = sweeps  # most recently used last
+            while len(_REV_CACHE) > 16:
+                _REV_CACHE.pop(next(iter(_REV_CACHE)))
+            for sw in sweeps:
                 _lib.check(L.qgb_adjoint_sweep_step(phi.data_ptr(), lam.data_ptr(), self.code, n, C.byref(sw), base,
                                                     0, 1, 0, gbase, scr.data_ptr(), nbytes, st), "adjoint_sweep_step")
             run.clear()
@@ -164,6 +173,11 @@ _GEN_C = {k: _lib.double_array(np.stack([m.real, m.imag], axis=-1).reshape(-1)) 
 # per kind: (column, value) of the one nonzero of each generator row
 _GEN_ROWS = {k: [(int(np.flatnonzero(m[r])[0]), complex(m[r, np.flatnonzero(m[r])[0]])) for r in range(m.shape[0])]
              for k, m in _GEN.items()}
+
+
+# tile-pass descriptions of a reverse sweep per structure (gates, sites, derivative slots,
+# matrix offsets): a training loop re-plans nothing
+_REV_CACHE: dict = {}
 
 
 def _tile_bits(dtype):
@@ -261,7 +275,8 @@ class _Inputs:
                 angles.append(a.reshape(()).to(torch.float64))
         rs = set(self.rot)
         self.other = [i for i in range(len(gates)) if i not in rs]
-        self.angles = torch.stack([a.cpu() for a in angles]) if angles else torch.zeros(0, dtype=torch.float64)
+        self.angles = (torch.stack([a.cpu() if a.is_cuda else a for a in angles]) if angles
+                       else torch.zeros(0, dtype=torch.float64))
         self.kinds = np.array([_KIND[gates[i].name] for i in self.rot], dtype=np.int64)
 
     def args(self):
