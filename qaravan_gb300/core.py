@@ -9,3 +9,5 @@ from .gates import *  # noqa: F401,F403
 from .hamiltonians import *  # noqa: F401,F403
 from .noise import *  # noqa: F401,F403
 from .paulis import *  # noqa: F401,F403
+from .skeletons import *  # noqa: F401,F403
+from .applications.compilation import string_to_sv  # noqa: F401  (core/utils.py:46-50)
