@@ -563,6 +563,19 @@ def gpu_arm(args):
     if rank != 0:
         return
     launches = args.steps * (1 + ex.launches)
+    # accuracy of the timed path: the final state (the last timed step's) against the same circuit
+    # run in complex128 (CUDA-core tile sweeps, the path pinned to the reference fixtures at 1e-12)
+    accuracy = None
+    if rank == 0 and dtype == torch.complex64 and not args.no_accuracy:
+        ref_sim = StatevectorSim(circ, dtype=torch.complex128)
+        ref_state = ref_sim.get_statevector().reshape(-1)
+        diff = (state.to(torch.complex128) - ref_state).abs()
+        accuracy = {"reference": "same circuit in complex128 (CUDA-core tile sweeps)",
+                    "max_abs_amplitude_error": float(diff.max().item()),
+                    "rms_amplitude_error": float(diff.square().mean().sqrt().item()),
+                    "max_abs_amplitude": float(ref_state.abs().max().item()),
+                    "norm_error": float(abs(torch.linalg.vector_norm(state.to(torch.complex128)).item() - 1.0))}
+        del ref_sim, ref_state, diff
     del state, ex, sim
     torch.cuda.empty_cache()
     sections = {}
@@ -591,7 +604,7 @@ def gpu_arm(args):
                    "parallelism": f"replicas x{world}"},
         "hbm_gbs_effective": round(passes * alg_bytes / (ms_step / 1e3) / 1e9, 1),
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks.summary(),
-        "gpu_launches": launches, "sections": sections,
+        "gpu_launches": launches, "accuracy": accuracy, "sections": sections,
     }
     print(json.dumps(out), flush=True)
 
@@ -649,6 +662,7 @@ def main():
     p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-accuracy", action="store_true", help="skip the complex128 comparison of the final state")
     p.add_argument("--cpu-budget", type=float, default=12.0)
     p.add_argument("--ref-gates", type=int, default=2)
     p.add_argument("--sections", default="all",
