@@ -11,3 +11,4 @@ from .noise import *  # noqa: F401,F403
 from .paulis import *  # noqa: F401,F403
 from .skeletons import *  # noqa: F401,F403
 from .applications.compilation import string_to_sv  # noqa: F401  (core/utils.py:46-50)
+from .measure import pretty_print_dm, pretty_print_sv  # noqa: F401  (core/utils.py:52-89)

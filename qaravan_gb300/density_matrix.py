@@ -175,6 +175,13 @@ class DensityMatrixSim:
         d = 2 ** self.num_sites
         return self.state.reshape(d, d)
 
+    def __str__(self):
+        """rho as a mixture of pure states (``tensorQ/density_matrix_sim.py:78-80``)."""
+        from .measure import pretty_print_dm
+        self._ensure_ran()
+        d = 2 ** self.num_sites
+        return pretty_print_dm(self.state.detach().reshape(d, d).cpu().numpy())
+
     def normalize_state(self):
         Executor(compile_ops([], 2 * self.num_sites), self.dtype, self.device, mode_normalize="dm").normalize(self.state)
 

@@ -90,6 +90,21 @@ def measure_and_collapse_sv(state, n, meas_sites, rng=None):
 
 
 def pretty_print_sv(sv, threshold=1e-3):
+    """Basis-state expansion of a state, amplitudes above ``threshold`` (``core/utils.py:77-89``)."""
     n = int(round(np.log2(len(sv))))
     terms = [f"{sv[i]:.4f}|{np.binary_repr(i, width=n)}⟩" for i in np.where(np.abs(sv) > threshold)[0]]
     return " + ".join(terms)
+
+
+def pretty_print_dm(dmat, threshold=1e-3):
+    """A density matrix as a mixture of its eigenvectors, weights above
+    ``threshold`` by decreasing magnitude, each written as ``pretty_print_sv``
+    does (``core/utils.py:52-75``)."""
+    dmat = np.asarray(dmat)
+    evals, evecs = np.linalg.eigh(dmat)
+    order = np.argsort(np.abs(evals))[::-1]
+    out = []
+    for ev, vec in zip(evals[order], evecs[:, order].T):
+        if abs(ev) > threshold:
+            out.append(f"{ev.real:.4f} * ({pretty_print_sv(vec, threshold)})")
+    return "\n ".join(out)

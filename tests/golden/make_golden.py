@@ -151,6 +151,14 @@ def gen_gates_misc(R):
     _save("gates_misc.npz", **out)
 
 
+def gen_pretty(R):
+    """The reference's pretty-printed statevector and density matrix (core/utils.py:52-89)."""
+    u = R.core
+    v = np.array([1, 0, 0.5j, 0, 0, 0, 0, 1]) / np.sqrt(2.25)
+    rho = 0.6 * np.outer(v, v.conj()) + 0.4 * np.diag([0, 0, 0, 1, 0, 0, 0, 0])
+    _save("pretty.npz", sv=v, dm=rho, sv_str=np.array(u.pretty_print_sv(v)), dm_str=np.array(u.pretty_print_dm(rho)))
+
+
 def gen_sv_observables(R):
     """Pauli-string expectations, partial overlaps and outcome probabilities on
     a random 8-qubit state."""
@@ -320,6 +328,7 @@ def main():
     gen_traj_dm10(R, steps=40, p=1e-3, gamma=5e-4, name="traj_dm10.npz")
     gen_sv_decomp(R)
     gen_gates_misc(R)
+    gen_pretty(R)
 
 
 if __name__ == "__main__":

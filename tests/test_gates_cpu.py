@@ -105,3 +105,11 @@ def test_superop_layers_skip_noise():
     c.construct_layers()  # [[H0, H1], [SuperOp on 0]]
     c.add_noise(depolarizing(0.01))
     assert [len(layer) for layer in c.layers] == [2 + 1, 1]  # the SuperOp's layer gets no noise carrier
+
+
+def test_pretty_print_matches_the_reference():
+    from conftest import golden
+    from qaravan_gb300.core import pretty_print_dm, pretty_print_sv
+    z = golden("pretty.npz")
+    assert pretty_print_sv(z["sv"]) == str(z["sv_str"])
+    assert pretty_print_dm(z["dm"]) == str(z["dm_str"])
