@@ -105,6 +105,10 @@ class PauliNoise(Noise):
     def sample(self, rng=None):
         return pauli_string_to_gates(self.sample_string(rng))
 
+    def __str__(self):
+        """``{string: probability rounded to 3 decimals}`` (``core/noise.py:156-158``)."""
+        return str({str(s): np.around(p, 3) for s, p in zip(self.strings, self.probs)})
+
 
 class PauliLindbladNoise(Noise):
     def __init__(self, strings, lindblad_coefficients, dense=True):
@@ -114,16 +118,20 @@ class PauliLindbladNoise(Noise):
         self.num_sites = len(strings[0])
         self.local_dim = 2
         self.gamma = np.exp(2 * sum(lindblad_coefficients))
-        self.superop = self._make_superop() if dense else None
+        self.superop = self.make_superop() if dense else None
 
     def get_kraus_for_string(self, i):
         d = 2 ** self.num_sites
         return [np.emath.sqrt(1 - self.rates[i]) * np.eye(d),
                 np.emath.sqrt(self.rates[i]) * _embed_dense(self.strings[i])]
 
-    def _make_superop(self):
-        ops = [sum(np.kron(np.conj(k), k) for k in self.get_kraus_for_string(i))
-               for i in range(len(self.strings))]
+    def get_superop_for_string(self, i):
+        """sum_k conj(K) (x) K over the two Kraus operators of generator i (``core/noise.py:183-185``)."""
+        return sum(np.kron(np.conj(k), k) for k in self.get_kraus_for_string(i))
+
+    def make_superop(self):
+        """Product of the generators' superoperators (``core/noise.py:187-189``)."""
+        ops = [self.get_superop_for_string(i) for i in range(len(self.strings))]
         return np.linalg.multi_dot(ops) if len(ops) > 1 else ops[0]
 
     def get_superop(self, *args, **kwargs):
@@ -151,6 +159,16 @@ class PauliLindbladNoise(Noise):
         gamma * (-1)^(layer non-empty) (``core/noise.py:206-210``)."""
         layer = self.sample(rng)
         return layer, self.gamma * (-1) ** (len(layer) != 0)
+
+
+def random_pauli_channel(n, n_strings=5, c=0.1):
+    """Pauli channel on n sites: the identity with weight 1 and n_strings - 1
+    random strings with weights c * U[0, 1), normalised, from NumPy's global
+    random state (``core/noise.py:232-236``)."""
+    from .paulis import random_pauli_string
+    strings = ['i' * n] + [random_pauli_string(n) for _ in range(n_strings - 1)]
+    probs = np.array([1.0] + [c * np.random.rand() for _ in range(n_strings - 1)])
+    return PauliNoise(strings, probs / np.sum(probs))
 
 
 def depolarizing(p):

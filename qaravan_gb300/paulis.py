@@ -94,3 +94,10 @@ def pauli_masks(pstr: str):
         elif c != 'i':
             raise ValueError(f"invalid Pauli character {c!r} in {pstr!r}")
     return xm, zm, ny
+
+
+def random_pauli_string(n):
+    """n characters from 'ixyz', each drawn with ``numpy.random.choice(4)`` from
+    NumPy's global random state (``core/paulis.py:53-58``)."""
+    chars = 'ixyz'
+    return ''.join(chars[np.random.choice(len(chars))] for _ in range(n))

@@ -159,6 +159,17 @@ def gen_pretty(R):
     _save("pretty.npz", sv=v, dm=rho, sv_str=np.array(u.pretty_print_sv(v)), dm_str=np.array(u.pretty_print_dm(rho)))
 
 
+def gen_noise_misc(R):
+    """random_pauli_channel under a fixed global seed (strings, weights, str())
+    and the Pauli-Lindblad superoperators, from the reference (core/noise.py)."""
+    c = R.core
+    np.random.seed(3)
+    ch = c.random_pauli_channel(3, 5, 0.2)
+    lb = c.PauliLindbladNoise(['xi', 'zz', 'yx'], [0.05, 0.1, 0.02])
+    _save("noise_misc.npz", strings=np.array(ch.strings), probs=np.array(ch.probs), text=np.array(str(ch)),
+          lb_superop=lb.make_superop(), lb_superop_1=lb.get_superop_for_string(1))
+
+
 def gen_sv_observables(R):
     """Pauli-string expectations, partial overlaps and outcome probabilities on
     a random 8-qubit state."""
@@ -329,6 +340,7 @@ def main():
     gen_sv_decomp(R)
     gen_gates_misc(R)
     gen_pretty(R)
+    gen_noise_misc(R)
 
 
 if __name__ == "__main__":

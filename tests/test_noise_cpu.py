@@ -38,3 +38,19 @@ def test_lindblad_samples_and_inverse_prefactors():
         if f:
             want, _ = pauli_multiply(want, st)
     assert nm.sample_string(np.random.default_rng(11)) == want
+
+
+def test_random_pauli_channel_and_lindblad_superops_match_the_reference():
+    """Fixture from the reference (make_golden.py gen_noise_misc)."""
+    import numpy as np
+    from conftest import golden
+    from qaravan_gb300.noise import PauliLindbladNoise, random_pauli_channel
+    z = golden("noise_misc.npz")
+    np.random.seed(3)
+    ch = random_pauli_channel(3, 5, 0.2)
+    assert list(ch.strings) == [str(x) for x in z["strings"]]
+    assert np.max(np.abs(np.array(ch.probs) - z["probs"])) < 1e-15
+    assert str(ch) == str(z["text"])
+    lb = PauliLindbladNoise(['xi', 'zz', 'yx'], [0.05, 0.1, 0.02])
+    assert np.max(np.abs(lb.make_superop() - z["lb_superop"])) < 1e-14
+    assert np.max(np.abs(lb.get_superop_for_string(1) - z["lb_superop_1"])) < 1e-15
