@@ -91,8 +91,23 @@ class Circuit:
             self.built = True
         return self
 
+    def old_build(self, nm=None):
+        """The reference's deprecated form of ``build`` (``core/circuits.py:97-107``):
+        a deep copy, decomposed, layered and with noise; this circuit is left unchanged."""
+        c = copy.deepcopy(self)
+        c.decompose()
+        c.construct_layers()
+        if nm is not None:
+            c.add_noise(nm)
+        c.built = True
+        return c
+
     def add_meas(self, meas_sites):
         self.meas_sites = meas_sites
+
+    def draw(self):
+        """Not drawn (the reference's ``draw`` returns None as well, ``core/circuits.py:159-161``)."""
+        return None
 
     def dag(self):
         return Circuit([g.dag() for g in self.gate_list[::-1]], n=self.num_sites, local_dim=self.local_dim)
@@ -142,6 +157,17 @@ class Circuit:
             c.layers = [[g.shallow_copy() for g in layer] for layer in self.layers]
         c.built = self.built
         return c
+
+
+def shift_gate_list(circ, start_site):
+    """Deep copies of the circuit's gates with every site index moved by
+    ``start_site`` (``core/circuits.py:194-204``)."""
+    out = []
+    for g in circ.gate_list:
+        h = copy.deepcopy(g)
+        h.indices = np.array(g.indices) + start_site
+        out.append(h)
+    return out
 
 
 def compose_circuits(circ_list):
