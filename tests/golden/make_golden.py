@@ -170,6 +170,23 @@ def gen_noise_misc(R):
           lb_superop=lb.make_superop(), lb_superop_1=lb.get_superop_for_string(1))
 
 
+def gen_trotter_apps(R):
+    """applications/trotter.py run by the reference itself: the statevector run
+    (TFI, 6 sites, 5 steps, normalised magnetisation) and the noisy
+    density-matrix run (4 sites, 4 steps, a 4-site Pauli channel after every
+    layer), cached and uncached."""
+    import importlib
+    t = importlib.import_module("qaravan.applications.trotter")
+    c = R.core
+    ham = c.TFI(6, jz=1.0, h=0.7)
+    sv = t.trotter_sv_sim(ham, 0.1, 5, t.magnetization(6))
+    ham4 = c.TFI(4, jz=1.0, h=0.9)
+    ch = c.PauliNoise(["iiii", "xiii", "iziz", "yyii", "iixx"], [0.92, 0.02, 0.03, 0.01, 0.02])
+    dm = t.trotter_dm_sim(ham4, 0.1, 4, ch, t.magnetization(4))
+    dm_u = t.trotter_dm_sim_uncached(ham4, 0.1, 4, ch, t.magnetization(4))
+    _save("trotter_apps.npz", sv=np.array(sv), dm=np.array(dm), dm_uncached=np.array(dm_u))
+
+
 def gen_sv_observables(R):
     """Pauli-string expectations, partial overlaps and outcome probabilities on
     a random 8-qubit state."""
@@ -341,6 +358,7 @@ def main():
     gen_gates_misc(R)
     gen_pretty(R)
     gen_noise_misc(R)
+    gen_trotter_apps(R)
 
 
 if __name__ == "__main__":

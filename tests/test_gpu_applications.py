@@ -123,3 +123,18 @@ def test_msp_infidelity_gradient_and_autodiff_loop():
     params, state = msp_via_autodiff(in_states, out_states, sk, init_params=p0, lr=0.05,
                                      context=RunContext(max_iter=15, quiet=True))
     assert state["cost_list"][-1] < state["cost_list"][0]
+
+
+def test_trotter_applications_match_the_reference_outputs():
+    """Fixture produced by the reference's own applications/trotter.py
+    (make_golden.py gen_trotter_apps)."""
+    from conftest import golden
+    from qaravan_gb300.applications import magnetization, trotter_dm_sim, trotter_dm_sim_uncached, trotter_sv_sim
+    from qaravan_gb300.hamiltonians import TFI
+    from qaravan_gb300.noise import PauliNoise
+    z = golden("trotter_apps.npz")
+    assert np.max(np.abs(np.array(trotter_sv_sim(TFI(6, jz=1.0, h=0.7), 0.1, 5, magnetization(6))) - z["sv"])) < 1e-12
+    ch = PauliNoise(["iiii", "xiii", "iziz", "yyii", "iixx"], [0.92, 0.02, 0.03, 0.01, 0.02])
+    ham = TFI(4, jz=1.0, h=0.9)
+    assert np.max(np.abs(np.array(trotter_dm_sim(ham, 0.1, 4, ch, magnetization(4))) - z["dm"])) < 1e-12
+    assert np.max(np.abs(np.array(trotter_dm_sim_uncached(ham, 0.1, 4, ch, magnetization(4))) - z["dm_uncached"])) < 1e-12
