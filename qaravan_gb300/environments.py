@@ -72,32 +72,47 @@ class _Dev:
     def __init__(self, n, dtype, device):
         self.n, self.dtype, self.device = n, dtype, torch.device(device)
         self.code = _lib.dtype_code(dtype)
-        L = _lib.lib()
-        self.nbytes = L.qgb_reduce_scratch_bytes(n, 16, 1)
-        self.scratch = torch.empty(self.nbytes // 8 + 1, dtype=torch.float64, device=self.device)
-        self.out = torch.empty(2 * 4 ** 6, dtype=torch.float64, device=self.device)
+        self.nbytes = 0
+        self.scratch = None
+        self.out = None
+
+    def _buffers(self, k, batch):
+        """Scratch and output of a batched partial overlap on k sites, grown on demand."""
+        nbytes = _lib.lib().qgb_partial_overlap_scratch_bytes(self.n, k, batch)
+        if nbytes == 0:
+            raise ValueError(f"partial overlap on {k} of {self.n} sites is not supported")
+        if nbytes > self.nbytes:
+            self.nbytes = nbytes
+            self.scratch = torch.empty(nbytes // 8 + 1, dtype=torch.float64, device=self.device)
+        if self.out is None or self.out.numel() < 2 * batch * 4 ** k:
+            self.out = torch.empty(2 * batch * 4 ** k, dtype=torch.float64, device=self.device)
 
     def vec(self, v):
         t = v if torch.is_tensor(v) else torch.as_tensor(np.asarray(v))
         return t.reshape(-1).to(device=self.device, dtype=self.dtype).contiguous().clone()
 
-    def op_action(self, mat, indices, state):
-        """In place: state <- mat on ``indices`` (``op_action``, ``statevector_sim.py:124-140``)."""
+    def op_action(self, mat, indices, state, batch=1):
+        """In place: state <- mat on ``indices`` (``op_action``, ``statevector_sim.py:124-140``);
+        ``batch`` contiguous vectors of 2^n amplitudes."""
         m = torch.as_tensor(np.asarray(mat)).to(device=self.device, dtype=self.dtype).contiguous()
         _lib.check(_lib.lib().qgb_op_action(state.data_ptr(), self.code, self.n, _lib.int_array(list(indices)),
-                                            len(indices), m.data_ptr(), 0, 1, 0, _lib.stream_ptr(self.device)),
-                   "op_action")
+                                            len(indices), m.data_ptr(), 0, batch, 2 ** self.n,
+                                            _lib.stream_ptr(self.device)), "op_action")
         return state
 
-    def partial_overlap(self, a, b, skip):
-        """Host complex128 ``partial_overlap(a, b, skip)``, skipped sites ascending."""
+    def partial_overlap(self, a, b, skip, batch=None):
+        """Host complex128 ``partial_overlap(a, b, skip)``, skipped sites ascending; with
+        ``batch`` set, one 2^k x 2^k matrix per pair of contiguous vectors."""
         sites = sorted(int(s) for s in skip)
         k = len(sites)
+        nb = 1 if batch is None else batch
+        self._buffers(k, nb)
         _lib.check(_lib.lib().qgb_partial_overlap(a.data_ptr(), b.data_ptr(), self.code, self.n, _lib.int_array(sites),
-                                                  k, 1, 0, self.out.data_ptr(), self.scratch.data_ptr(), self.nbytes,
-                                                  _lib.stream_ptr(self.device)), "partial_overlap")
-        o = self.out[:2 * 4 ** k].cpu().numpy()
-        return (o[0::2] + 1j * o[1::2]).reshape(2 ** k, 2 ** k)
+                                                  k, nb, 2 ** self.n, self.out.data_ptr(), self.scratch.data_ptr(),
+                                                  self.nbytes, _lib.stream_ptr(self.device)), "partial_overlap")
+        o = self.out[:2 * nb * 4 ** k].cpu().numpy()
+        o = (o[0::2] + 1j * o[1::2]).reshape(nb, 2 ** k, 2 ** k)
+        return o[0] if batch is None else o
 
     def overlap(self, a, b):
         """<a|b> (complex, host)."""

@@ -343,6 +343,44 @@ def gen_grad_hea(R):
           grad=th.grad.numpy(), sv=sv.detach().numpy().astype(np.complex128))
 
 
+def gen_msp_env(R):
+    """applications/compilation.py run by the reference itself on 4 qubits:
+    environments of single gates, three sweeps of ``msp_via_environments``
+    (final gate matrices and costs) and ``msp_cost`` with a matrix target and
+    with output states. (The reference's ``unitary_embedding`` raises NameError:
+    its module does not import scipy.)"""
+    import contextlib
+    import importlib
+    import io
+    comp = importlib.import_module("qaravan.applications.compilation")
+    rng = np.random.default_rng(31)
+    n, sk = 4, [[0, 1], [1, 2], [2, 3], [0, 1], [1, 2]]
+    params = rng.uniform(0, 2 * np.pi, size=len(sk) * 6 + n * 3)
+    in_strings = ["0000", "0110", "1011"]
+    ins = [comp.string_to_sv(s) for s in in_strings]
+    outs = []
+    for _ in in_strings:
+        v = rng.normal(size=2 ** n) + 1j * rng.normal(size=2 ** n)
+        outs.append(v / np.linalg.norm(v))
+    ansatz = comp.dressed_cnot_circ(sk, n, params)
+    env_idx = [0, 1, 4, len(ansatz.gate_list) - 1]
+    envs = np.array([comp.msp_environment(ins[1], ansatz, outs[1], i) for i in env_idx])
+    with contextlib.redirect_stdout(io.StringIO()), contextlib.redirect_stderr(io.StringIO()):
+        new, costs, term = comp.msp_via_environments(ins, comp.dressed_cnot_circ(sk, n, params), outs, num_sweeps=3)
+    mats = np.zeros((len(new.gate_list), 16), dtype=np.complex128)
+    for i, g in enumerate(new.gate_list):
+        m = np.asarray(g.matrix, dtype=np.complex128).reshape(-1)
+        mats[i, :m.size] = m
+    sizes = np.array([np.asarray(g.matrix).size for g in new.gate_list])
+    target = np.linalg.qr(rng.normal(size=(2 ** n, 2 ** n)) + 1j * rng.normal(size=(2 ** n, 2 ** n)))[0]
+    cost_mat = comp.msp_cost(params, sk, ins, target)
+    cost_states = comp.msp_cost(params, sk, ins, outs)
+    _save("msp_env.npz", n=n, skeleton=np.array(sk), params=params, in_strings=np.array(in_strings),
+          outs=np.array(outs), env_idx=np.array(env_idx), envs=envs, costs=np.array(costs), term=np.array(term),
+          mats=mats, sizes=sizes, target=target,
+          cost_mat=np.array(cost_mat), cost_states=np.array(cost_states))
+
+
 def main():
     R = refload.load()
     np.random.seed(0)
@@ -359,6 +397,7 @@ def main():
     gen_pretty(R)
     gen_noise_misc(R)
     gen_trotter_apps(R)
+    gen_msp_env(R)
 
 
 if __name__ == "__main__":

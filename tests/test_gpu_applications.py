@@ -138,3 +138,101 @@ def test_trotter_applications_match_the_reference_outputs():
     ham = TFI(4, jz=1.0, h=0.9)
     assert np.max(np.abs(np.array(trotter_dm_sim(ham, 0.1, 4, ch, magnetization(4))) - z["dm"])) < 1e-12
     assert np.max(np.abs(np.array(trotter_dm_sim_uncached(ham, 0.1, 4, ch, magnetization(4))) - z["dm_uncached"])) < 1e-12
+
+
+def _msp_problem(n, sk, npairs, seed):
+    rng = np.random.default_rng(seed)
+    ins = [np.eye(2 ** n)[i] for i in rng.choice(2 ** n, size=npairs, replace=False)]
+    outs = []
+    for _ in range(npairs):
+        v = rng.normal(size=2 ** n) + 1j * rng.normal(size=2 ** n)
+        outs.append(v / np.linalg.norm(v))
+    return ins, outs, rng.uniform(0, 2 * np.pi, size=len(sk) * 6 + n * 3)
+
+
+def test_msp_environments_match_the_reference_outputs():
+    """Fixture produced by the reference's own applications/compilation.py
+    (make_golden.py gen_msp_env): single-gate environments, three sweeps of
+    msp_via_environments (costs and every final gate matrix) and msp_cost."""
+    from conftest import golden
+    from qaravan_gb300.applications import (dressed_cnot_circ, msp_cost, msp_environment, msp_via_environments,
+                                            string_to_sv)
+    z = golden("msp_env.npz")
+    n, sk, params = int(z["n"]), z["skeleton"].tolist(), z["params"]
+    ins = [string_to_sv(str(s)) for s in z["in_strings"]]
+    outs = list(z["outs"])
+    ansatz = dressed_cnot_circ(sk, n, params)
+    for i, want in zip(z["env_idx"], z["envs"]):
+        assert np.max(np.abs(msp_environment(ins[1], ansatz, outs[1], int(i)) - want)) < 1e-12
+    new, costs, term = msp_via_environments(ins, dressed_cnot_circ(sk, n, params), outs, num_sweeps=3)
+    assert term == str(z["term"])
+    assert np.max(np.abs(np.array(costs) - z["costs"])) < 1e-10
+    for g, m, size in zip(new.gate_list, z["mats"], z["sizes"]):
+        assert np.asarray(g.matrix).size == size
+        assert np.max(np.abs(np.asarray(g.matrix).reshape(-1) - m[:size])) < 1e-10
+    assert abs(msp_cost(params, sk, ins, z["target"]) - float(z["cost_mat"])) < 1e-12
+    assert abs(msp_cost(params, sk, ins, outs) - float(z["cost_states"])) < 1e-12
+
+
+def test_msp_environment_general_sites_against_oracle():
+    """Environments on 9 qubits with pairs that are neither adjacent nor
+    ascending, for one-site and two-site gates: env[a, b] equals the oracle's
+    <out| ansatz with the gate set to |b><a| |in>, each matrix unit run through
+    the whole circuit."""
+    from qaravan_gb300.applications import dressed_cnot_circ, msp_environment
+    n, sk = 9, [[0, 5], [7, 2], [3, 4], [8, 1], [6, 0]]
+    ins, outs, params = _msp_problem(n, sk, 1, 3)
+    ansatz = dressed_cnot_circ(sk, n, params)
+    for gate_idx in (0, 3, 5, 11, len(ansatz.gate_list) - 2):
+        g = ansatz.gate_list[gate_idx]
+        d = 2 ** len(g.indices)
+        env = msp_environment(ins[0], ansatz, outs[0], gate_idx)
+        want = np.zeros((d, d), dtype=np.complex128)
+        for a in range(d):
+            for b in range(d):
+                unit = np.zeros((d, d))
+                unit[b, a] = 1.0
+                gates = [type("G", (), {"name": h.name, "indices": list(h.indices),
+                                        "matrix": unit if j == gate_idx else np.asarray(h.matrix)})()
+                         for j, h in enumerate(ansatz.gate_list)]
+                want[a, b] = np.vdot(outs[0], ref.run_sv(gates, n, init_state=ins[0]))
+        if len(g.indices) == 1:
+            assert np.max(np.abs(env - want)) < 1e-12
+        else:  # the environment's rows and columns follow the sites in ascending order
+            perm = [0, 2, 1, 3] if g.indices[0] > g.indices[1] else [0, 1, 2, 3]
+            assert np.max(np.abs(env - want[np.ix_(perm, perm)])) < 1e-12
+
+
+def test_msp_via_environments_cost_is_the_final_overlap():
+    """Nine qubits, four pairs: every sweep's cost is non-increasing (each update
+    is the optimal unitary for its environment) and the last cost squared is
+    npairs - Re sum_p <out_p|A|in_p> of the final ansatz, run by the oracle."""
+    from qaravan_gb300.applications import dressed_cnot_circ, msp_via_environments
+    n, sk = 9, [[0, 1], [2, 3], [4, 5], [6, 7], [1, 2], [3, 4], [5, 6], [7, 8], [8, 0]]
+    ins, outs, params = _msp_problem(n, sk, 4, 9)
+    new, costs, term = msp_via_environments(ins, dressed_cnot_circ(sk, n, params), outs, num_sweeps=6)
+    assert all(b <= a + 1e-12 for a, b in zip(costs, costs[1:]))
+    gates = [type("G", (), {"name": g.name, "indices": list(g.indices), "matrix": np.asarray(g.matrix)})()
+             for g in new.gate_list]
+    amp = sum(np.vdot(o, ref.run_sv(gates, n, init_state=i)) for i, o in zip(ins, outs))
+    assert abs(costs[-1] ** 2 - (len(ins) - amp.real)) < 1e-10
+    for g in new.gate_list:
+        if g.name[0] == "U":
+            m = np.asarray(g.matrix)
+            assert np.max(np.abs(m @ m.conj().T - np.eye(2))) < 1e-12
+
+
+def test_unitary_embedding_keeps_the_given_columns():
+    """The deprecated embedding: the given input columns map to their outputs,
+    the other columns are an orthonormal basis of the null space of (out^T in)^T."""
+    from qaravan_gb300.applications import unitary_embedding
+    rng = np.random.default_rng(4)
+    outs = []
+    for _ in range(2):
+        v = rng.normal(size=8) + 1j * rng.normal(size=8)
+        outs.append(v / np.linalg.norm(v))
+    a = unitary_embedding(["010", "111"], outs)
+    assert np.max(np.abs(a[:, 2] - outs[0])) < 1e-15 and np.max(np.abs(a[:, 7] - outs[1])) < 1e-15
+    rest = a[:, [0, 1, 3, 4, 5, 6]]
+    assert np.max(np.abs(rest.conj().T @ rest - np.eye(6))) < 1e-12
+    assert np.max(np.abs(a[:, [2, 7]].T @ rest)) < 1e-12
