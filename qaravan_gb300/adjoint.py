@@ -265,8 +265,8 @@ class _Inputs:
     rotation form of the reverse step reduces directly, so autograd never walks
     back through ``matrix_exp``. Every other gate contributes its matrix."""
 
-    def __init__(self, gates):
-        self.mats = _matrices(gates)
+    def __init__(self, gates, closed_form=False):
+        self.mats = _matrices(gates, closed_form)
         self.rot, angles = [], []
         for i, g in enumerate(gates):
             a = _rotation_angle(g)
@@ -350,23 +350,48 @@ class _EnergyFn(torch.autograd.Function):
         return (None, None, None, *inputs.grads(blocks, 2.0 * float(g_e), ctx.needs_input_grad, 3))
 
 
-def _matrices(gates):
-    return [g.matrix if torch.is_tensor(g.matrix) else torch.as_tensor(np.asarray(g.matrix, dtype=np.complex128))
-            for g in gates]
+_GEN_T = {k: torch.from_numpy(m) for k, m in _GEN.items()}
+
+
+def _matrices(gates, closed_form=False):
+    """Every gate's matrix as a torch tensor. With ``closed_form``, rotation gates
+    whose matrix has not been built yet (torch angles, see ``ParamGate``) get
+    cos(theta) I - i sin(theta) P from their construction-time angles, all of a
+    kind in one vectorised step, instead of one ``matrix_exp`` each; the two
+    differ by the series truncation of ``matrix_exp`` (about 2e-10), far below
+    complex64 rounding, so the complex64 paths use it."""
+    mats = [None] * len(gates)
+    if closed_form:
+        by_kind = {}
+        for i, g in enumerate(gates):
+            kind = _KIND.get(getattr(g, "name", None))
+            if kind is not None and getattr(g, "matrix_pending", lambda: False)() and _rotation_angle(g) is not None:
+                by_kind.setdefault(kind, []).append(i)
+        for kind, idx in by_kind.items():
+            th = torch.stack([gates[i].angle_values()[0].reshape(()).to(torch.float64).cpu() for i in idx])
+            gen = _GEN_T[kind]
+            eye = torch.eye(gen.shape[0], dtype=torch.complex128)
+            m = torch.cos(th)[:, None, None] * eye - 1j * torch.sin(th)[:, None, None] * gen
+            for j, i in enumerate(idx):
+                mats[i] = m[j]
+    for i, g in enumerate(gates):
+        if mats[i] is None:
+            mats[i] = g.matrix if torch.is_tensor(g.matrix) else torch.as_tensor(np.asarray(g.matrix, dtype=np.complex128))
+    return mats
 
 
 def run_with_adjoint(sim):
     """Differentiable ``StatevectorSim.run``: the returned state carries an
     adjoint backward to every gate matrix (or rotation angle) that requires grad."""
     gates = _gate_list(sim)
-    inputs = _Inputs(gates)
+    inputs = _Inputs(gates, closed_form=sim.dtype == torch.complex64)
     return _StateFn.apply(_Runner(sim, gates), inputs, *inputs.args())
 
 
 def adjoint_energy(sim, terms):
     """Differentiable ``sum_t c_t <psi|P_t|psi>`` (float64) of ``sim``'s circuit."""
     gates = _gate_list(sim)
-    inputs = _Inputs(gates)
+    inputs = _Inputs(gates, closed_form=sim.dtype == torch.complex64)
     return _EnergyFn.apply(_Runner(sim, gates), list(terms), inputs, *inputs.args())
 
 

@@ -6,12 +6,13 @@
 // (core/noise.py:29-49). Here all trajectories advance together, one gate at a
 // time, each keeping its own normalised 2^n state:
 //
-//  * traj_gate_kernel: per (trajectory, block) CTA, compose in shared memory
-//    the trajectory's op on the union U of the gate's sites and the previous
-//    gate's sites (at most 4 bits): the previous gate's pending Kraus
-//    operators (normalised), then the gate, then the depolarising Paulis
-//    sampled for this trajectory and gate; apply it to every group of 2^|U|
-//    amplitudes; accumulate |out_r|^2 per output row r (float64 partials).
+//  * traj_gate_kernel: per (trajectory, block) CTA, apply the trajectory's op
+//    on the union U of the gate's sites and the previous gate's sites (at
+//    most 4 bits) to every group of 2^|U| amplitudes, in factors held in
+//    registers: the previous gate's pending Kraus operators (normalised), then
+//    the gate with the depolarising Paulis sampled for this trajectory and
+//    gate folded in; accumulate |out|^2 per value of the gate sites' bits
+//    (float64 partials).
 //  * traj_decide_kernel: one thread per trajectory sums the partials into the
 //    joint populations of the gate's sites and draws the amplitude-damping
 //    branches site by site (exact sequential probabilities gamma * P(1)),
@@ -41,160 +42,156 @@ struct TrajGateArgs {
     int log_paulis;    // write the sampled Pauli indices to the log
 };
 
-// out = A (2x2 on U position p) applied to the rows of X (D x D), i.e. X <- (A on p) X
-template <typename C>
-__device__ void left_apply_1q(C* X, int D, int ku, int p, const C A[4], C* tmp) {
-    const int bit = 1 << (ku - 1 - p);
-    for (int idx = threadIdx.x; idx < D * D; idx += blockDim.x) {
-        const int r = idx / D, c = idx % D;
-        const int r0 = r & ~bit, a = (r & bit) ? 1 : 0;
-        C acc;
-        acc.x = 0;
-        acc.y = 0;
-        for (int bb = 0; bb < 2; ++bb) {
-            const C m = A[2 * a + bb];
-            const C x = X[(r0 | (bb ? bit : 0)) * D + c];
-            cfma(acc, m, x);
-        }
-        tmp[idx] = acc;
+// v <- K on local position P (bit K_-1-P of the local index), K real 2x2.
+template <int K_, int P, typename C, typename T>
+__device__ __forceinline__ void kraus_at(C (&v)[1 << K_], T k00, T k01, T k10, T k11) {
+    constexpr int D = 1 << K_, bit = 1 << (K_ - 1 - P);
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+        if (c & bit) continue;
+        const C a = v[c], b = v[c | bit];
+        v[c].x = k00 * a.x + k01 * b.x;
+        v[c].y = k00 * a.y + k01 * b.y;
+        v[c | bit].x = k10 * a.x + k11 * b.x;
+        v[c | bit].y = k10 * a.y + k11 * b.y;
     }
-    __syncthreads();
-    for (int idx = threadIdx.x; idx < D * D; idx += blockDim.x) X[idx] = tmp[idx];
-    __syncthreads();
 }
 
-template <typename T, int K>
-__global__ void __launch_bounds__(256) traj_gate_kernel(cplx<T>* __restrict__ sv, const cplx<T>* __restrict__ gate,
+template <int K_, typename C, typename T>
+__device__ __forceinline__ void kraus_dispatch(C (&v)[1 << K_], int p, const T k[4]) {
+    switch (p) {
+        case 0: kraus_at<K_, 0>(v, k[0], k[1], k[2], k[3]); break;
+        case 1: if constexpr (K_ > 1) kraus_at<K_, 1>(v, k[0], k[1], k[2], k[3]); break;
+        case 2: if constexpr (K_ > 2) kraus_at<K_, 2>(v, k[0], k[1], k[2], k[3]); break;
+        case 3: if constexpr (K_ > 3) kraus_at<K_, 3>(v, k[0], k[1], k[2], k[3]); break;
+    }
+}
+
+// The trajectory's op on the union U of the gate's sites (local positions
+// 0..KG-1, the top bits of the local index) and the pending sites, applied in
+// factors: out = (Paulis . G on the gate positions) (K_1 K_0 on the pending
+// positions) v. The Kraus operators of amplitude damping are real (diag(1,
+// sqrt(1-gamma)) / sqrt(1-p) or sqrt(gamma/p) |0><1|); the Paulis, sampled
+// per trajectory, are folded into the gd x gd gate matrix in registers.
+// Per amplitude that is 4 * (kp + gd) real FMAs instead of the 4 * 2^K of the
+// composed 2^K x 2^K product.
+template <typename T, int K, int KG>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) traj_gate_kernel(cplx<T>* __restrict__ sv, const cplx<T>* __restrict__ gate,
                                                         const cplx<T>* __restrict__ kraus, double* __restrict__ partials,
                                                         uint8_t* __restrict__ pauli_log, const __grid_constant__ TrajGateArgs a) {
     using C = cplx<T>;
-    constexpr int D = 1 << K;
-    __shared__ C W[D * D], tmp[D * D];
+    constexpr int D = 1 << K, GD = 1 << KG, LOW = K - KG;
     __shared__ double red[8][4];
     const int64_t t = blockIdx.y;
-    // ---- compose W = (Paulis on gate sites) (gate on gate sites) (pending Kraus on their sites)
-    for (int idx = threadIdx.x; idx < D * D; idx += blockDim.x) {
-        const int r = idx / D, c = idx % D;
-        W[idx] = mk<T>(r == c ? T(1) : T(0), T(0));
-    }
-    __syncthreads();
-    for (int j = 0; j < a.kp; ++j) {
-        C A[4];
-        const C* kj = kraus + (t * 2 + j) * 4;
-        for (int e = 0; e < 4; ++e) A[e] = kj[e];
-        left_apply_1q<C>(W, D, K, a.ppos[j], A, tmp);
-    }
-    if (a.kg > 0) {
-        // X <- G X with G on gate positions (kg = 1 or 2)
-        const int gd = 1 << a.kg;
-        for (int idx = threadIdx.x; idx < D * D; idx += blockDim.x) {
-            const int r = idx / D, c = idx % D;
-            int gr = 0, rest = r;
-            for (int j = 0; j < a.kg; ++j) {
-                const int bit = 1 << (K - 1 - a.gpos[j]);
-                gr |= ((r & bit) ? 1 : 0) << (a.kg - 1 - j);
-                rest &= ~bit;
-            }
-            C acc = mk<T>(0, 0);
-            for (int gc = 0; gc < gd; ++gc) {
-                int rr = rest;
-                for (int j = 0; j < a.kg; ++j)
-                    if ((gc >> (a.kg - 1 - j)) & 1) rr |= 1 << (K - 1 - a.gpos[j]);
-                cfma(acc, gate[gr * gd + gc], W[rr * D + c]);
-            }
-            tmp[idx] = acc;
-        }
-        __syncthreads();
-        for (int idx = threadIdx.x; idx < D * D; idx += blockDim.x) W[idx] = tmp[idx];
-        __syncthreads();
+    // ---- G' = (P_0 x P_1) G on the gate positions, every thread the same values
+    C G[GD * GD];
+#pragma unroll
+    for (int e = 0; e < GD * GD; ++e) G[e] = KG > 0 ? gate[e] : mk<T>(T(1), T(0));
+    if constexpr (KG > 0) {
         if (a.p_dep > 0) {
-            for (int j = 0; j < a.kg; ++j) {
+#pragma unroll
+            for (int j = 0; j < KG; ++j) {
                 const double u = Philox::uniform(a.event, uint32_t(t), 2u * j, a.seed0, a.seed1);
                 // I with 1-p, X, Y, Z with p/3 each
                 int pk = 0;
                 if (u >= 1.0 - a.p_dep) pk = 1 + min(2, int((u - (1.0 - a.p_dep)) / (a.p_dep / 3.0)));
                 if (a.log_paulis && blockIdx.x == 0 && threadIdx.x == 0) pauli_log[t * 2 + j] = uint8_t(pk);
                 if (pk == 0) continue;
-                C P[4];
-                P[0] = P[1] = P[2] = P[3] = mk<T>(0, 0);
-                if (pk == 1) { P[1] = mk<T>(1, 0); P[2] = mk<T>(1, 0); }
-                else if (pk == 2) { P[1] = mk<T>(0, -1); P[2] = mk<T>(0, 1); }
-                else { P[0] = mk<T>(1, 0); P[3] = mk<T>(-1, 0); }
-                left_apply_1q<C>(W, D, K, a.gpos[j], P, tmp);
+                const int bit = 1 << (KG - 1 - j);
+                // rows r (bit clear) and r | bit: X swaps them, Y swaps with (-i, i), Z negates the second
+#pragma unroll
+                for (int r = 0; r < GD; ++r) {
+                    if (r & bit) continue;
+#pragma unroll
+                    for (int c = 0; c < GD; ++c) {
+                        const C lo = G[r * GD + c], hi = G[(r | bit) * GD + c];
+                        if (pk == 1) {
+                            G[r * GD + c] = hi;
+                            G[(r | bit) * GD + c] = lo;
+                        } else if (pk == 2) {
+                            G[r * GD + c] = mk<T>(hi.y, -hi.x);        // -i * hi
+                            G[(r | bit) * GD + c] = mk<T>(-lo.y, lo.x);  //  i * lo
+                        } else {
+                            G[(r | bit) * GD + c] = mk<T>(-hi.x, -hi.y);
+                        }
+                    }
+                }
             }
         }
     }
-    // ---- apply W to every group of the trajectory's state, accumulate |out_r|^2
-    int srt[K > 0 ? K : 1];
-    for (int j = 0; j < K; ++j) srt[j] = a.ubits[j];
-    for (int i = 1; i < K; ++i)
-        for (int j = i; j > 0 && srt[j - 1] > srt[j]; --j) {
-            const int x = srt[j];
-            srt[j] = srt[j - 1];
-            srt[j - 1] = x;
-        }
-    // bucket(r): the gate sites' bits of output row r (2 bits per row, packed)
-    uint32_t bk = 0;
-    for (int r = 0; r < D; ++r) {
-        int b = 0;
-        for (int j = 0; j < a.kg; ++j) b |= ((r >> (K - 1 - a.gpos[j])) & 1) << (a.kg - 1 - j);
-        bk |= uint32_t(b) << (2 * r);
+    T kr[2][4];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) kr[j][e] = j < a.kp ? kraus[(t * 2 + j) * 4 + e].x : T(0);
     }
+    int srt[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) srt[j] = a.ubits[j];
+#pragma unroll
+    for (int i = 1; i < K; ++i)
+#pragma unroll
+        for (int j = i; j > 0; --j)
+            if (srt[j - 1] > srt[j]) {
+                const int x = srt[j];
+                srt[j] = srt[j - 1];
+                srt[j - 1] = x;
+            }
+    uint32_t m[K];  // n <= 32: offsets within a trajectory's state fit 32 bits
+#pragma unroll
+    for (int j = 0; j < K; ++j) m[j] = uint32_t(1) << a.ubits[j];
     C* s = sv + t * a.stride;
     const uint64_t groups = uint64_t(1) << (a.n - K), step = uint64_t(a.nblk) * blockDim.x;
     // per-thread partial sums in the state's precision (a few dozen terms each; float64 across threads)
-    T p0 = 0, p1 = 0, p2 = 0, p3 = 0;
-    auto add_pop = [&](int r, const C& o) {
-        const T w = o.x * o.x + o.y * o.y;
-        const uint32_t b = (bk >> (2 * r)) & 3u;
-        p0 += b == 0 ? w : T(0);
-        p1 += b == 1 ? w : T(0);
-        p2 += b == 2 ? w : T(0);
-        p3 += b == 3 ? w : T(0);
-    };
+    T pop[GD];
+#pragma unroll
+    for (int b = 0; b < GD; ++b) pop[b] = 0;
     for (uint64_t g = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; g < groups; g += step) {
         uint64_t base = g;
+#pragma unroll
         for (int j = 0; j < K; ++j) base = ((base >> srt[j]) << (srt[j] + 1)) | (base & ((uint64_t(1) << srt[j]) - 1));
+        C* sb = s + base;
         C v[D];
 #pragma unroll
         for (int c = 0; c < D; ++c) {
-            uint64_t o = 0;
+            uint32_t o = 0;
 #pragma unroll
-            for (int j = 0; j < K; ++j) o |= uint64_t((c >> (K - 1 - j)) & 1) << a.ubits[j];
-            v[c] = s[base + o];
+            for (int j = 0; j < K; ++j)
+                if ((c >> (K - 1 - j)) & 1) o += m[j];
+            v[c] = sb[o];
         }
-        if constexpr (K <= 2) {
+        if (a.kp > 0) kraus_dispatch<K>(v, a.ppos[0], kr[0]);
+        if (a.kp > 1) kraus_dispatch<K>(v, a.ppos[1], kr[1]);
+        if constexpr (KG > 0) {
 #pragma unroll
-            for (int r = 0; r < D; ++r) {
-                C acc = mk<T>(0, 0);
+            for (int l = 0; l < (1 << LOW); ++l) {
+                C in[GD];
 #pragma unroll
-                for (int c = 0; c < D; ++c) cfma(acc, W[r * D + c], v[c]);
-                uint64_t o = 0;
+                for (int c = 0; c < GD; ++c) in[c] = v[(c << LOW) | l];
 #pragma unroll
-                for (int j = 0; j < K; ++j) o |= uint64_t((r >> (K - 1 - j)) & 1) << a.ubits[j];
-                s[base + o] = acc;
-                add_pop(r, acc);
+                for (int r = 0; r < GD; ++r) {
+                    C acc = mk<T>(0, 0);
+#pragma unroll
+                    for (int c = 0; c < GD; ++c) cfma(acc, G[r * GD + c], in[c]);
+                    v[(r << LOW) | l] = acc;
+                    pop[r] += acc.x * acc.x + acc.y * acc.y;
+                }
             }
-        } else {
-#pragma unroll 1
-            for (int r = 0; r < D; ++r) {
-                const C* wr = W + r * D;
-                C acc = mk<T>(0, 0);
+        }
 #pragma unroll
-                for (int c = 0; c < D; ++c) cfma(acc, wr[c], v[c]);
-                uint64_t o = 0;
-                for (int j = 0; j < K; ++j) o |= uint64_t((r >> (K - 1 - j)) & 1) << a.ubits[j];
-                s[base + o] = acc;
-                add_pop(r, acc);
-            }
+        for (int c = 0; c < D; ++c) {
+            uint32_t o = 0;
+#pragma unroll
+            for (int j = 0; j < K; ++j)
+                if ((c >> (K - 1 - j)) & 1) o += m[j];
+            sb[o] = v[c];
         }
     }
-    // block reduction of the 4 joint populations -> partials[(t * nblk + blk) * 4 + b]
+    // block reduction of the joint populations of the gate sites -> partials[(t * nblk + blk) * 4 + b]
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double pv[4] = {double(p0), double(p1), double(p2), double(p3)};
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
-        double x = pv[b];
+        double x = b < GD && KG > 0 ? double(pop[b < GD ? b : 0]) : 0.0;
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
         if (lane == 0) red[warp][b] = x;
     }
@@ -271,13 +268,24 @@ using namespace qgb_host;
 
 namespace {
 
-template <typename T, int K>
+template <typename T, int K, int KG>
 int launch_gate(void* sv, const void* gate, const void* kraus, double* partials, uint8_t* plog, const TrajGateArgs& a,
                 cudaStream_t st) {
     dim3 grid(unsigned(a.nblk), unsigned(a.ntraj));
-    traj_gate_kernel<T, K><<<grid, 256, 0, st>>>((cplx<T>*)sv, (const cplx<T>*)gate, (const cplx<T>*)kraus, partials,
-                                                 plog, a);
+    traj_gate_kernel<T, K, KG><<<grid, 256, 0, st>>>((cplx<T>*)sv, (const cplx<T>*)gate, (const cplx<T>*)kraus,
+                                                     partials, plog, a);
     return check_launch("trajectory gate kernel");
+}
+
+template <typename T, int K>
+int launch_gate(void* sv, const void* gate, const void* kraus, double* partials, uint8_t* plog, const TrajGateArgs& a,
+                cudaStream_t st) {
+    switch (a.kg) {
+        case 0: return launch_gate<T, K, 0>(sv, gate, kraus, partials, plog, a, st);
+        case 1: return launch_gate<T, K, 1>(sv, gate, kraus, partials, plog, a, st);
+        case 2: if constexpr (K >= 2) return launch_gate<T, K, 2>(sv, gate, kraus, partials, plog, a, st); break;
+    }
+    return set_error(QGB_EINVAL, "gate width %d with %d union bits", a.kg, a.ku);
 }
 
 template <typename T>
@@ -309,7 +317,7 @@ extern "C" int qgb_traj_step(void* sv, int dtype, int n, int64_t ntraj, int64_t 
                              uint8_t* jump_log, void* stream) {
     if (!sv || !kraus || !partials) return set_error(QGB_EINVAL, "null pointer");
     if (dtype != QGB_C64 && dtype != QGB_C128) return set_error(QGB_EINVAL, "dtype %d unknown", dtype);
-    if (n < 1 || n > QGB_MAX_QUBITS) return set_error(QGB_EINVAL, "n=%d invalid", n);
+    if (n < 1 || n > 32) return set_error(QGB_EINVAL, "n=%d invalid (trajectories of 1 to 32 qubits)", n);
     if (ntraj < 1 || ntraj > 65535) return set_error(QGB_EINVAL, "ntraj %lld not in [1, 65535]", (long long)ntraj);
     if (ntraj > 1 && stride < (int64_t(1) << n)) return set_error(QGB_EINVAL, "trajectory stride too small");
     if (k < 0 || k > 2 || kprev < 0 || kprev > 2) return set_error(QGB_EINVAL, "gate and pending widths must be 0..2");

@@ -296,7 +296,13 @@ def _arr(x, backend):
 
 class ParamGate(Gate):
     """Angle-parametrised gate (``core/param_gates.py:21-49``). Torch angles keep
-    the autograd graph through ``torch.linalg.matrix_exp``."""
+    the autograd graph through ``torch.linalg.matrix_exp``.
+
+    With torch angles the matrix is built when ``matrix`` is first read (the
+    reference builds it in the constructor): the values are the same, computed
+    from the angles as they were at construction (an angle changed in place
+    afterwards still contributes its gradient, at the old value). Paths that
+    take the angles directly, such as the complex64 adjoint, never build it."""
 
     def __init__(self, name, indices, *args):
         super().__init__(name, indices, None)
@@ -306,8 +312,54 @@ class ParamGate(Gate):
             self.angles = self.solve_angles()
         else:
             self.angles = args
-            self.matrix = self.construct_matrix()
-            self._angle_matrix = self.matrix  # identity marks "matrix still the one built from the angles"
+            if self.backend == "torch":
+                self._angle_values = tuple(a.detach().clone() if _is_torch(a) else a for a in args)
+                self._angle_versions = tuple(a._version if _is_torch(a) else None for a in args)
+                self._built = {}  # shared with shallow copies, which then share the built matrix
+                self._lazy = True
+            else:
+                self.matrix = self.construct_matrix()
+                self._angle_matrix = self.matrix  # identity marks "matrix still the one built from the angles"
+
+    @property
+    def matrix(self):
+        if self.__dict__.get("_lazy"):
+            self._build_matrix()
+        return self.__dict__.get("_matrix")
+
+    @matrix.setter
+    def matrix(self, m):
+        self.__dict__["_lazy"] = False
+        self.__dict__["_matrix"] = m
+
+    def matrix_pending(self):
+        """True while the matrix built from torch angles has not been read yet."""
+        return bool(self.__dict__.get("_lazy"))
+
+    def angle_values(self):
+        """The angles' values at construction (detached)."""
+        return self.__dict__.get("_angle_values", tuple(
+            a.detach() if _is_torch(a) else a for a in self.angles))
+
+    def _build_matrix(self):
+        m = self._built.get("matrix")
+        if m is None:
+            live = self.angles
+            args = live
+            if any(_is_torch(a) and a._version != v for a, v in zip(live, self._angle_versions)):
+                # changed in place since construction: the construction-time value, same gradient
+                args = tuple(v + (a - a.detach()) if _is_torch(a) else a for a, v in zip(live, self._angle_values))
+            self.angles = args
+            try:
+                m = self.construct_matrix()
+            finally:
+                self.angles = live
+            self._built["matrix"] = m
+        self.matrix = m
+        self._angle_matrix = m
+
+    def get_local_dim(self):
+        return 2 if self.__dict__.get("_lazy") else super().get_local_dim()
 
     def __str__(self):
         return f"{self.name} gate on site(s) {self.indices} with angle(s) {self.angles}"
@@ -324,6 +376,8 @@ class ParamGate(Gate):
     def built_from_angles(self):
         """True while ``matrix`` is the one constructed from ``angles`` (not
         replaced by ``update_matrix`` / ``Circuit.update_gate``)."""
+        if self.__dict__.get("_lazy"):
+            return True
         return self.matrix is not None and self.matrix is getattr(self, "_angle_matrix", None)
 
     def shallow_copy(self):

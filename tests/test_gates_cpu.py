@@ -113,3 +113,55 @@ def test_pretty_print_matches_the_reference():
     z = golden("pretty.npz")
     assert pretty_print_sv(z["sv"]) == str(z["sv_str"])
     assert pretty_print_dm(z["dm"]) == str(z["dm_str"])
+
+
+def test_torch_angle_matrices_are_built_on_first_read():
+    """A ParamGate with a torch angle builds its matrix when ``matrix`` is first
+    read: bitwise the reference's eager ``matrix_exp`` value, with its autograd
+    graph; building a circuit, layering it and copying it read no matrix."""
+    th = torch.tensor([0.3, -1.1], dtype=torch.float64, requires_grad=True)
+    Y = torch.tensor([[0, -1j], [1j, 0]], dtype=torch.complex128)
+    g = RY(0, th[0])
+    assert g.matrix_pending() and g.built_from_angles()
+    c = Circuit([g, RZZ([0, 1], th[1])], n=2)
+    c.construct_layers()
+    cp = c.copy()
+    assert all(h.matrix_pending() for h in c.gate_list + cp.gate_list)
+    m = g.matrix
+    assert torch.equal(m, torch.linalg.matrix_exp(-1.j * th[0] * Y)) and m.grad_fn is not None
+    assert g.matrix is m and not g.matrix_pending() and g.built_from_angles()
+    assert torch.equal(cp.gate_list[0].matrix, m)
+    c.update_gate(1, np.eye(4))
+    assert not c.gate_list[1].matrix_pending() and not c.gate_list[1].built_from_angles()
+    assert not RZ(0, 0.3).matrix_pending()  # NumPy angles: built in the constructor, as before
+
+
+def test_angle_changed_in_place_before_the_first_read():
+    """The matrix has the angle's value at construction, as an eagerly built one
+    would, and the gradient still reaches the angle."""
+    th = torch.tensor([0.3, 0.5], dtype=torch.float64, requires_grad=True)
+    g = RX(0, th[0])
+    with torch.no_grad():
+        th.add_(1.0)
+    m = g.matrix
+    X = torch.tensor([[0, 1], [1, 0]], dtype=torch.complex128)
+    assert torch.equal(m.detach(), torch.linalg.matrix_exp(-1.j * torch.tensor(0.3, dtype=torch.float64) * X))
+    m.real.sum().backward()  # 2 cos(theta)
+    assert abs(th.grad[0].item() + 2 * np.sin(0.3)) < 1e-12 and th.grad[1].item() == 0
+
+
+def test_closed_form_rotations_for_complex64_adjoint():
+    """The complex64 adjoint takes cos(theta) I - i sin(theta) P for rotation
+    gates not yet built, without building them; it agrees with matrix_exp to
+    its series truncation."""
+    from qaravan_gb300.adjoint import _matrices
+    from qaravan_gb300.gates import CNOT
+    rng = np.random.default_rng(3)
+    th = torch.tensor(rng.uniform(0, 2 * np.pi, size=6), dtype=torch.float64, requires_grad=True)
+    gates = [RX(0, th[0]), RY(1, th[1]), RZ(2, th[2]), RXX([0, 1], th[3]), RYY([1, 2], th[4]), RZZ([2, 0], th[5]),
+             CNOT([0, 1], 3)]
+    fast = _matrices(gates, closed_form=True)
+    assert all(g.matrix_pending() for g in gates[:6])
+    slow = _matrices(gates)
+    for a, b in zip(fast, slow):
+        assert a.shape == b.shape and torch.max(torch.abs(a - b.detach())).item() < 1e-9
