@@ -115,6 +115,32 @@ class TrajectorySim:
         self.graph.replay()
         return self.state
 
+    def time_gates(self):
+        """One run with CUDA events around every gate's launches on the launching
+        stream: a list of (gate index, union bits, lowest union bit, ms). The
+        union is the gate's sites plus the previous gate's (pending damping)."""
+        L = _lib.lib()
+        n, T = self.n, self.ntraj
+        code = _lib.dtype_code(self.dtype)
+        st = _lib.stream_ptr(self.device)
+        stream = torch.cuda.current_stream(self.device)
+        sv, isz = self.state.data_ptr(), self.mats.element_size()
+        _lib.check(L.qgb_init_basis(sv, code, n, 0, T, 2 ** n, st), "init_basis")
+        rows, prev, kprev, prev_sites = [], None, 0, []
+        for i, g in enumerate(self.gates):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            _lib.check(L.qgb_traj_step(sv, code, n, T, 2 ** n, self._site_arrays[i], len(g.indices),
+                                       self.mats.data_ptr() + self.offs[i] * isz, prev, kprev, self.kraus.data_ptr(),
+                                       self.p_dep, self.gamma, self.seed, i, self.partials.data_ptr(), None, None, st),
+                       "traj_step")
+            e1.record(stream)
+            union = set(g.indices) | set(prev_sites)
+            rows.append((i, len(union), n - 1 - max(union), e0, e1))
+            prev, kprev, prev_sites = self._site_arrays[i], len(g.indices), list(g.indices)
+        torch.cuda.synchronize(self.device)
+        return [(i, k, lo, e0.elapsed_time(e1)) for i, k, lo, e0, e1 in rows]
+
     def expectations(self, terms):
         """(ntraj, nterms) float64 of c_t <psi|P_t|psi> per trajectory."""
         return pauli_expectations(self.state, self.n, terms, batch=self.ntraj, stride=2 ** self.n)
@@ -136,3 +162,31 @@ def z_terms(n):
     zs = [(1.0, 'i' * q + 'z' + 'i' * (n - q - 1)) for q in range(n)]
     zz = [(1.0, 'i' * q + 'zz' + 'i' * (n - q - 2)) for q in range(n - 1)]
     return zs + zz
+
+
+def _main(argv=None):
+    """``python -m qaravan_gb300.trajectories [qubits] [trajectories] [trotter steps]``:
+    per-gate device time of the noisy TFI trajectory workload (depolarising
+    1e-3 and amplitude damping 5e-4 after every gate), grouped by the width of
+    the gate's union with the pending sites and by whether it reaches bits 0..2."""
+    import sys
+    from . import workloads
+    args = [int(a) for a in (sys.argv[1:] if argv is None else argv)]
+    n, T, steps = (args + [20, 1024, 2][len(args):])[:3]
+    sim = TrajectorySim(workloads.tfi_trotter_circuit(n, 0.05, steps), T, p_dep=1e-3, gamma=5e-4, seed=2026)
+    sim.run()
+    rows = sim.time_gates()
+    alg = 2 * T * 2 ** n * np.dtype(np.complex64 if sim.dtype == torch.complex64 else np.complex128).itemsize
+    groups = {}
+    for _, k, lo, ms in rows:
+        groups.setdefault((k, "low" if lo < 3 else "high"), []).append(ms)
+    total = sum(ms for *_, ms in rows)
+    print(f"{n} qubits, {T} trajectories, {len(rows)} gates: {total / len(rows):.3f} ms/gate, "
+          f"{alg / 1e9:.2f} GB algorithmic per gate")
+    for key in sorted(groups):
+        v = groups[key]
+        print(f"union {key[0]} {key[1]}: {len(v)} gates, {np.mean(v):.3f} ms, {alg / np.mean(v) / 1e6:.0f} GB/s")
+
+
+if __name__ == "__main__":
+    _main()
