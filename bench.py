@@ -189,13 +189,14 @@ def section_variants(n, gates):
             ("c64_fused_w4_tensorcores", torch.complex64, "fused", 4, 14, 2),
             ("c64_fused_w5_tensorcores", torch.complex64, "fused", 5, 14, 2),
             ("c64_fused_w6_tensorcores", torch.complex64, "fused", 6, 14, 2),
+            ("c64_fused_w6_tensorcores_row_norm_restore", torch.complex64, "fused", 6, 14, 4),
             ("c64_fused_w6_tensorcores_no_norm_restore", torch.complex64, "fused", 6, 14, 3),
             ("c64_sweep_w3_t12", torch.complex64, "sweep", 3, 12, 0),
             ("c64_sweep_w4_t14", torch.complex64, "sweep", 4, 14, 0),
             ("c128_sweep_w3_t13", torch.complex128, "sweep", 3, 13, 0)]:
         try:
             _lib.check(L.qgb_set_dense_impl(min(impl, 2)))
-            engine.set_norm_restore(impl != 3)
+            engine.set_norm_restore({3: "off", 4: "row"}.get(impl, "chain"))
             ex = StatevectorSim(circ, dtype=dtype, mode=mode, fusion_width=width, tile_bits=tile).compile()
             st = torch.empty(2 ** n, dtype=dtype, device="cuda")
             code = _lib.dtype_code(dtype)
@@ -211,7 +212,7 @@ def section_variants(n, gates):
             out[name] = {"error": str(e)[:200]}
         torch.cuda.empty_cache()
     _lib.check(L.qgb_set_dense_impl(before))
-    engine.set_norm_restore(True)
+    engine.set_norm_restore("chain")
     return out
 
 

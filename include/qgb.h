@@ -110,6 +110,23 @@ int qgb_op_action(void* sv, int dtype, int n, const int* indices, int k, const v
 int qgb_op_action_unitary(void* sv, int dtype, int n, const int* indices, int k, const void* op,
                           int64_t op_stride, int64_t batch, int64_t sv_stride, void* stream);
 
+/* qgb_op_action_unitary for one state (batch 1) as link `link` of a chain of
+ * consecutive unitary passes over the same state: instead of restoring every
+ * group's norm, the tensor-core path works in epochs of 4 passes. The pass that
+ * starts the chain records its input's squared norm (the reference) in `chain`
+ * (6 doubles of device memory, 3 rotating slots), the last pass of each epoch
+ * its output's squared norm, and the first pass of the next epoch scales its
+ * matrix by sqrt(reference / that norm); the norm stays within about one
+ * epoch's drift (~4e-7 relative) of the reference. The caller numbers the
+ * passes 0, 1, 2, ... and restarts at 0 after anything else touched the state;
+ * link 0 clears the buffer. A pass that does not run on the tensor cores
+ * (complex128, k < 4, batch > 1) clears the chain, so that a new one starts.
+ * Replaces, like qgb_op_action, the reference's per-gate op_action
+ * (tensorQ/statevector_sim.py:124-140), which has no norm control. */
+int qgb_op_action_unitary_chain(void* sv, int dtype, int n, const int* indices, int k, const void* op,
+                                int64_t op_stride, int64_t batch, int64_t sv_stride, double* chain, int link,
+                                void* stream);
+
 /* A fused pass (several gates per read+write of the state), planned by the
  * host compiler from a Circuit's gate list (core/base_sim.py:30-53 loop). */
 int qgb_apply_sweep(void* sv, int dtype, int n, const qgb_sweep* sweep, const void* mats,

@@ -235,7 +235,7 @@ namespace qgb_host {
 // j is out_bits[j] (same set of bits) to `batch` vectors of 2^nbits entries.
 int apply_dense_bits(void* sv, int dtype, int nbits, const int* in_bits, const int* out_bits, int k,
                      const void* op, int64_t op_stride, int64_t batch, int64_t sv_stride, cudaStream_t st,
-                     int unitary = 0) {
+                     int unitary = 0, double* chain = nullptr, int link = 0) {
     if (!sv || !op) return set_error(QGB_EINVAL, "null state or operator pointer");
     if (dtype != QGB_C64 && dtype != QGB_C128) return set_error(QGB_EINVAL, "dtype %d unknown", dtype);
     if (k < 1 || k > QGB_MAX_K) return set_error(QGB_EINVAL, "gate width k=%d not in [1, %d]", k, QGB_MAX_K);
@@ -274,6 +274,16 @@ int apply_dense_bits(void* sv, int dtype, int nbits, const int* in_bits, const i
     a.batch = batch;
     a.sv_stride = sv_stride;
     a.groups = uint64_t(1) << (nbits - k);
+    if (unitary == 2) {
+        if (dtype == QGB_C64) {
+            const int rc = try_dense_tc(sv, op, nbits, a.sorted, in_bits, out_bits, k, op_stride, batch, sv_stride, 2,
+                                        st, chain, link);
+            if (rc != QGB_EDECLINE) return rc;
+        }
+        // not on the chain kernel: clear the chain, so that the next pass starts a new one
+        if (cudaMemsetAsync(chain, 0, 6 * sizeof(double), st) != cudaSuccess) return check_launch("norm chain reset");
+        unitary = 1;
+    }
     if (dtype == QGB_C64) {
         const int rc =
             try_dense_tc(sv, op, nbits, a.sorted, in_bits, out_bits, k, op_stride, batch, sv_stride, unitary, st);
@@ -287,7 +297,7 @@ int apply_dense_bits(void* sv, int dtype, int nbits, const int* in_bits, const i
 namespace {
 
 int op_action(void* sv, int dtype, int n, const int* indices, int k, const void* op, int64_t op_stride,
-              int64_t batch, int64_t sv_stride, void* stream, int unitary) {
+              int64_t batch, int64_t sv_stride, void* stream, int unitary, double* chain = nullptr, int link = 0) {
     if (n < 1 || n > QGB_MAX_QUBITS) return set_error(QGB_EINVAL, "n=%d not in [1, %d]", n, QGB_MAX_QUBITS);
     if (!indices) return set_error(QGB_EINVAL, "null indices");
     if (k < 1 || k > QGB_MAX_K) return set_error(QGB_EINVAL, "gate width k=%d not in [1, %d]", k, QGB_MAX_K);
@@ -297,7 +307,7 @@ int op_action(void* sv, int dtype, int n, const int* indices, int k, const void*
         bits[j] = n - 1 - indices[j];
     }
     return apply_dense_bits(sv, dtype, n, bits, bits, k, op, op_stride, batch, sv_stride, (cudaStream_t)stream,
-                            unitary);
+                            unitary, chain, link);
 }
 
 }  // namespace
@@ -310,6 +320,15 @@ extern "C" int qgb_op_action(void* sv, int dtype, int n, const int* indices, int
 extern "C" int qgb_op_action_unitary(void* sv, int dtype, int n, const int* indices, int k, const void* op,
                                      int64_t op_stride, int64_t batch, int64_t sv_stride, void* stream) {
     return op_action(sv, dtype, n, indices, k, op, op_stride, batch, sv_stride, stream, 1);
+}
+
+extern "C" int qgb_op_action_unitary_chain(void* sv, int dtype, int n, const int* indices, int k, const void* op,
+                                           int64_t op_stride, int64_t batch, int64_t sv_stride, double* chain,
+                                           int link, void* stream) {
+    if (!chain || (reinterpret_cast<uintptr_t>(chain) % sizeof(double)))
+        return set_error(QGB_EINVAL, "norm chain buffer missing or not 8-byte aligned");
+    if (link < 0) return set_error(QGB_EINVAL, "negative chain link %d", link);
+    return op_action(sv, dtype, n, indices, k, op, op_stride, batch, sv_stride, stream, 2, chain, link);
 }
 
 extern "C" int qgb_dm_apply_superop(void* rho, int dtype, int n, const int* indices, int k, const void* superop,

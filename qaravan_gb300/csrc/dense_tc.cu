@@ -83,8 +83,12 @@ struct TcArgs {
     uint64_t tiles_per_state;            // 2^(n - 13)
     uint64_t tiles;                      // tiles_per_state * batch
     int64_t sv_stride;
+    double* chain;                       // norm chain (3 slots of {reference, output} squared norms) or null
+    int c_prev, c_cur, c_next;           // slots of the previous epoch, this epoch, the next epoch (-1: none)
+    int c_head, c_tail;                  // this pass opens its epoch (corrects) / closes it (measures its output)
 };
 
+constexpr int kChainEpoch = 4;                 // passes per norm-chain epoch
 constexpr int kTcDataThreads = 256;           // 8 data warps
 constexpr int kTcThreads = kTcDataThreads + 32;  // + the MMA warp
 constexpr unsigned long long kTcWaitNs = 2000000000ull;
@@ -302,10 +306,19 @@ template <int N> __device__ __forceinline__ void tmem_ld_row(uint32_t taddr, flo
     else tmem_ld64(taddr, v);
 }
 
-// UNIT: the op is unitary; each group's norm is restored after the product.
-template <int K, bool UNIT>
+// MODE 0: any op. MODE 1 (unitary op): each group's norm is restored after the
+// product. MODE 2 (unitary op, one state): a norm chain across consecutive
+// passes, in epochs of kChainEpoch passes -- the pass that starts a chain records
+// its input's squared norm as the chain's reference; the last pass of an epoch
+// records its output's squared norm; the first pass of the next epoch scales its
+// matrix by sqrt(reference / that output), undoing the norm drift of the epoch
+// (the tensor cores' round-toward-zero accumulation, ~1e-7 per pass). The passes
+// in between run as MODE 0. The norm stays within about one epoch's drift of the
+// reference, without the row-wise exchange of MODE 1.
+template <int K, int MODE>
 __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restrict__ sv, const float2* __restrict__ op,
                                                                  const __grid_constant__ TcArgs a) {
+    constexpr bool UNIT = MODE == 1;
     using G = TcGeom<K>;
     constexpr int D = G::D, H = G::H, R = G::R, NB = G::NB, BC = G::BCOLS;
     extern __shared__ unsigned char tc_smem_raw[];
@@ -321,8 +334,36 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
     __shared__ int row_exp[NB][2][128];    // per block, thread half and row: that half's scale exponent
     __shared__ float row_in[NB][2][128];   // ... that half's squared input norm (unitary ops)
     __shared__ float row_out[2][NB][2][128];  // per buffer pair: that half's squared output norm (unitary ops)
+    __shared__ double chain_red[8][2];        // per data warp: squared norms of its inputs and outputs (MODE 2)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int q = warp & 3, h = (warp >> 2) & 1;
+    // MODE 2, the pass that opens an epoch: it starts the chain (measures its input)
+    // unless the previous epoch left a reference and an output norm; its matrix is
+    // scaled by 1 + gcorr = sqrt(ref / out_prev)
+    bool chain_start = false;
+    float gcorr = 0.f;
+    if constexpr (MODE == 2) {
+        if (a.c_head) {
+            double chain_ref = 0.0;
+            chain_start = true;
+            if (a.c_prev >= 0) {
+                const double ref = a.chain[2 * a.c_prev], out = a.chain[2 * a.c_prev + 1];
+                if (ref > 0.0 && out > 0.0) {
+                    chain_start = false;
+                    chain_ref = ref;
+                    gcorr = float(sqrt(ref / out) - 1.0);
+                }
+            }
+            if (blockIdx.x == 0 && tid == 0) {
+                a.chain[2 * a.c_next] = 0.0;
+                a.chain[2 * a.c_next + 1] = 0.0;
+                if (!chain_start) a.chain[2 * a.c_cur] = chain_ref;
+            }
+        }
+    }
+    double acc_in = 0.0, acc_out = 0.0;  // float sums of up to 16 tiles folded into these
+    float f_in = 0.f, f_out = 0.f;
+    int n_in = 0, n_out = 0;
 
     // B operand: W = [[Mr, Mi], [-Mi, Mr]] in (output, input) memory order, scaled by 2^sw, split hi/lo.
     if (tid == 0) wmax_bits = 0;
@@ -341,7 +382,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
     for (int p = tid; p < D * D; p += kTcThreads) {
         const int i = p / D, j = p - (p / D) * D;
         const float2 m = op[a.perm_out[i] * D + a.perm_in[j]];
-        const float w[4] = {m.x * wscale, -m.y * wscale, m.y * wscale, m.x * wscale};  // (2i,2j) (2i,2j+1) (2i+1,2j) (2i+1,2j+1)
+        float w[4] = {m.x * wscale, -m.y * wscale, m.y * wscale, m.x * wscale};  // (2i,2j) (2i,2j+1) (2i+1,2j) (2i+1,2j+1)
+        if constexpr (MODE == 2) {
+            // the chain's correction 1 + g (|g| ~ 1e-7) goes into W: w + w g in one rounding; the
+            // hi/lo split then carries it like any other matrix value
+#pragma unroll
+            for (int e = 0; e < 4; ++e) w[e] = fmaf(w[e], gcorr, w[e]);
+        }
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
             const uint32_t o = b_off(2 * i + (e >> 1), 2 * j + (e & 1), R);
@@ -457,6 +504,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
                 for (int j = 0; j < H; ++j) m = fmaxf(m, fmaxf(fabsf(v[bk][j].x), fabsf(v[bk][j].y)));
                 row_exp[bk][h][32 * q + lane] = scale_exp(m);
                 if constexpr (UNIT) row_in[bk][h][32 * q + lane] = sumsq8<2 * H>(reinterpret_cast<const float*>(v[bk]));
+                if constexpr (MODE == 2)
+                    if (chain_start) f_in += sumsq8<2 * H>(reinterpret_cast<const float*>(v[bk]));
             }
             asm volatile("bar.sync %0, 64;" ::"r"(1 + q) : "memory");  // warps q and q + 4 share these rows
 #pragma unroll
@@ -482,6 +531,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
                 }
             }
             asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+            if constexpr (MODE == 2) {
+                if (++n_in == 16) {
+                    acc_in += double(f_in);
+                    f_in = 0.f;
+                    n_in = 0;
+                }
+            }
         };
         // Stores one 16-column chunk (8 components) of this thread's result row.
         auto put16 = [&](float2* p, int c0, const float* r) {
@@ -540,7 +596,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
 #pragma unroll
                         for (int e = 0; e < 16; ++e) r[e] = (r[e] * wunscale) * u;
                     }
+                    if constexpr (MODE == 2)
+                        if (a.c_tail) f_out += sumsq8<16>(r);
                     put16(p, c0, r);
+                }
+            }
+            if constexpr (MODE == 2) {
+                if (++n_out == 16) {
+                    acc_out += double(f_out);
+                    f_out = 0.f;
+                    n_out = 0;
                 }
             }
         };
@@ -675,9 +740,33 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
             }
         }
         asm volatile("cp.async.wait_all;" ::: "memory");
+        if constexpr (MODE == 2) {
+            acc_in += double(f_in);
+            acc_out += double(f_out);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                acc_in += __shfl_down_sync(0xffffffffu, acc_in, o);
+                acc_out += __shfl_down_sync(0xffffffffu, acc_out, o);
+            }
+            if (lane == 0) {
+                chain_red[warp][0] = acc_in;
+                chain_red[warp][1] = acc_out;
+            }
+        }
     }
     tc_fence_before();
     __syncthreads();
+    if constexpr (MODE == 2) {
+        if (tid == 0) {
+            double in = 0.0, out = 0.0;
+            for (int w = 0; w < 8; ++w) {
+                in += chain_red[w][0];
+                out += chain_red[w][1];
+            }
+            if (chain_start) atomicAdd(&a.chain[2 * a.c_cur], in);
+            if (a.c_tail) atomicAdd(&a.chain[2 * a.c_cur + 1], out);
+        }
+    }
     if (warp == 0) {
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(G::NCOLS) : "memory");
@@ -702,16 +791,16 @@ int dense_impl() {
     return g_dense_impl;
 }
 
-template <int K, bool UNIT>
+template <int K, int MODE>
 int launch_tc(float2* sv, const float2* op, const TcArgs& a, cudaStream_t st) {
     using G = TcGeom<K>;
     static int per_sm = 0;
     if (per_sm == 0) {
-        if (cudaFuncSetAttribute(dense_tc_kernel<K, UNIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        if (cudaFuncSetAttribute(dense_tc_kernel<K, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  int(G::SMEM)) != cudaSuccess)
             return qgb_host::check_launch("dense_tc attribute");
         int occ = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dense_tc_kernel<K, UNIT>, kTcThreads, G::SMEM) !=
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dense_tc_kernel<K, MODE>, kTcThreads, G::SMEM) !=
             cudaSuccess)
             return qgb_host::check_launch("dense_tc occupancy");
         per_sm = occ < 1 ? occ : 1;  // each CTA holds all 512 TMEM columns
@@ -719,7 +808,7 @@ int launch_tc(float2* sv, const float2* op, const TcArgs& a, cudaStream_t st) {
     }
     const uint64_t cap = uint64_t(qgb_host::sm_count()) * uint64_t(per_sm);
     const unsigned grid = unsigned(a.tiles < cap ? a.tiles : cap);
-    dense_tc_kernel<K, UNIT><<<grid, kTcThreads, G::SMEM, st>>>(sv, op, a);
+    dense_tc_kernel<K, MODE><<<grid, kTcThreads, G::SMEM, st>>>(sv, op, a);
     return qgb_host::check_launch("dense_tc kernel");
 }
 
@@ -747,8 +836,10 @@ int set_dense_impl(int mode) {
 // nothing) when the op is not one it takes, so that the caller runs the
 // CUDA-core kernel instead.
 int try_dense_tc(void* sv, const void* op, int nbits, const int* sorted, const int* in_bits, const int* out_bits,
-                 int k, int64_t op_stride, int64_t batch, int64_t sv_stride, int unitary, cudaStream_t st) {
+                 int k, int64_t op_stride, int64_t batch, int64_t sv_stride, int unitary, cudaStream_t st,
+                 double* chain, int link) {
     const int mode = dense_impl();
+    if (unitary == 2 && (batch > 1 || !chain)) return QGB_EDECLINE;  // the chain follows one state
     if (mode == 0 || k < 4 || k > 6 || (k == 4 && mode < 2)) return QGB_EDECLINE;
     if (nbits < 13) return QGB_EDECLINE;              // fewer than one 8192-amplitude tile
     if (batch > 1 && op_stride != 0) return QGB_EDECLINE;  // one operator for the whole batch
@@ -820,10 +911,31 @@ int try_dense_tc(void* sv, const void* op, int nbits, const int* sorted, const i
     a.sv_stride = batch > 1 ? sv_stride : 0;
     float2* s = static_cast<float2*>(sv);
     const float2* m = static_cast<const float2*>(op);
+    if (unitary == 2) {
+        // epochs of kChainEpoch passes: the first corrects (and starts the chain), the
+        // last measures its output; the passes between run without norm control
+        if (link == 0 && cudaMemsetAsync(chain, 0, 6 * sizeof(double), st) != cudaSuccess)
+            return check_launch("norm chain reset");
+        const int e = link / kChainEpoch, pos = link % kChainEpoch;
+        a.chain = chain;
+        a.c_head = pos == 0;
+        a.c_tail = pos == kChainEpoch - 1;
+        a.c_prev = e > 0 ? (e - 1) % 3 : -1;
+        a.c_cur = e % 3;
+        a.c_next = (e + 1) % 3;
+        if (a.c_head || a.c_tail) {
+            switch (k) {
+                case 4: return launch_tc<4, 2>(s, m, a, st);
+                case 5: return launch_tc<5, 2>(s, m, a, st);
+                default: return launch_tc<6, 2>(s, m, a, st);
+            }
+        }
+        unitary = 0;
+    }
     switch (k) {
-        case 4: return unitary ? launch_tc<4, true>(s, m, a, st) : launch_tc<4, false>(s, m, a, st);
-        case 5: return unitary ? launch_tc<5, true>(s, m, a, st) : launch_tc<5, false>(s, m, a, st);
-        default: return unitary ? launch_tc<6, true>(s, m, a, st) : launch_tc<6, false>(s, m, a, st);
+        case 4: return unitary ? launch_tc<4, 1>(s, m, a, st) : launch_tc<4, 0>(s, m, a, st);
+        case 5: return unitary ? launch_tc<5, 1>(s, m, a, st) : launch_tc<5, 0>(s, m, a, st);
+        default: return unitary ? launch_tc<6, 1>(s, m, a, st) : launch_tc<6, 0>(s, m, a, st);
     }
 }
 

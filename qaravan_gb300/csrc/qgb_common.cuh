@@ -120,7 +120,8 @@ int sm_count();
 // declines an op, and the caller runs the general kernel instead.
 constexpr int QGB_EDECLINE = 1000;
 int try_dense_tc(void* sv, const void* op, int nbits, const int* sorted, const int* in_bits, const int* out_bits,
-                 int k, int64_t op_stride, int64_t batch, int64_t sv_stride, int unitary, cudaStream_t st);
+                 int k, int64_t op_stride, int64_t batch, int64_t sv_stride, int unitary, cudaStream_t st,
+                 double* chain = nullptr, int link = 0);
 int tc_status_read_clear();
 int fuse_status_read_clear();
 }  // namespace qgb_host

@@ -21,17 +21,28 @@ import torch
 from . import _lib
 from .compiler import DenseStep, NormalizeStep, PauliMixStep, Plan, Recipe, SweepStep
 
-# Unitary fused blocks go through qgb_op_action_unitary, whose tensor-core path
-# restores each amplitude group's norm (removing the round-toward-zero shrinkage
-# of tensor-core accumulation, ~1e-7 of the norm per pass) at ~10 % of the
-# kernel's speed; QGB_NORM_RESTORE=0 or set_norm_restore(False) skips it.
-_NORM_RESTORE = os.environ.get("QGB_NORM_RESTORE", "1") != "0"
+# Unitary fused blocks control the norm on the tensor-core path, removing the
+# round-toward-zero shrinkage of tensor-core accumulation (~1e-7 of the norm per
+# pass). "chain" (default, one state): consecutive unitary blocks form a norm
+# chain (qgb_op_action_unitary_chain), each pass scaling its output back to the
+# chain's reference norm. "row": every amplitude group's norm is restored in the
+# pass (qgb_op_action_unitary; also what batches use under "chain"), ~10 % of the
+# kernel's speed. "off": neither. QGB_NORM_RESTORE=chain|row|0 or set_norm_restore().
+_NORM_MODES = {"1": "chain", "chain": "chain", "row": "row", "0": "off", "off": "off"}
+_NORM_RESTORE = _NORM_MODES.get(os.environ.get("QGB_NORM_RESTORE", "chain"), "chain")
 
 
-def set_norm_restore(flag: bool):
-    """Process-wide: restore group norms on unitary tensor-core blocks (default True)."""
+def set_norm_restore(mode="chain"):
+    """Process-wide norm control of unitary tensor-core blocks: "chain" (default),
+    "row", or "off" (True / False mean "chain" / "off")."""
     global _NORM_RESTORE
-    _NORM_RESTORE = bool(flag)
+    if mode is True:
+        mode = "chain"
+    elif mode is False:
+        mode = "off"
+    if mode not in ("chain", "row", "off"):
+        raise ValueError(f"norm restore mode {mode!r} (chain, row, off)")
+    _NORM_RESTORE = mode
 
 
 _FUSE_BLOCK = np.dtype([("out", "<i8"), ("k", "<i4"), ("op_begin", "<i4"), ("op_end", "<i4"), ("pad", "<i4")])
@@ -200,6 +211,7 @@ class Executor:
         mats = self.mats if mats is None else mats
         mptr = mats.data_ptr()
         launches = 0
+        link = 0  # position in the current norm chain of consecutive unitary blocks
         for s in self._steps:
             if events is not None and s[0] != "normalize":
                 e0 = torch.cuda.Event(enable_timing=True)
@@ -207,14 +219,25 @@ class Executor:
             if s[0] == "dense":
                 _, sites, k, off, unitary = s
                 # per-vector matrices (mat_stride) need not be unitary: only the plan's own are flagged
-                fn = L.qgb_op_action_unitary if (unitary and _NORM_RESTORE and mats is self.mats) else L.qgb_op_action
-                _lib.check(fn(ptr, self.code, nb, sites, k, mptr + off * self.itemsize, mat_stride if mat_stride else 0,
-                              batch, stride, st), "op_action")
+                mode = _NORM_RESTORE if (unitary and mats is self.mats) else "off"
+                if mode == "chain" and batch == 1:
+                    if getattr(self, "_chain", None) is None:
+                        self._chain = torch.zeros(6, dtype=torch.float64, device=self.device)
+                    _lib.check(L.qgb_op_action_unitary_chain(ptr, self.code, nb, sites, k, mptr + off * self.itemsize,
+                                                             0, 1, stride, self._chain.data_ptr(), link, st),
+                               "op_action")
+                    link += 1
+                else:
+                    fn = L.qgb_op_action if mode == "off" else L.qgb_op_action_unitary
+                    _lib.check(fn(ptr, self.code, nb, sites, k, mptr + off * self.itemsize,
+                                  mat_stride if mat_stride else 0, batch, stride, st), "op_action")
+                    link = 0
                 launches += 1
             elif s[0] == "sweep":
                 _lib.check(L.qgb_apply_sweep(ptr, self.code, nb, C.byref(s[1]), mptr, mat_stride, batch, stride, st),
                            "apply_sweep")
                 launches += 1
+                link = 0
             elif s[0] == "pauli_mix":
                 _, strings, coeff, nterms = s
                 if getattr(self, "_mix_buf", None) is None or self._mix_buf.numel() < state.numel():
@@ -227,8 +250,10 @@ class Executor:
                     o = b * (stride if batch > 1 else 0)
                     flat[o:o + dim].copy_(tmp[o:o + dim])
                 launches += 1 + batch
+                link = 0
             else:
                 launches += self.normalize(state, batch, stride)
+                link = 0
             if events is not None and s[0] != "normalize":
                 e1 = torch.cuda.Event(enable_timing=True)
                 e1.record()

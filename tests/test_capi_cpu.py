@@ -79,6 +79,14 @@ def test_abi_version_and_host_validation(lib):
     assert lib.qgb_pauli_expectation(4096, 0, 3, b"ixq", None, 1, 1, 0, 1, 1, 1 << 20, None) == -1
     assert lib.qgb_reduce_scratch_bytes(20, 3, 1) > 0
     assert lib.qgb_dm_apply_superop(4096, 0, 3, _lib.int_array([0, 1, 2, 0]), 4, 1, 1, 0, None) == -1
+    # norm chain: a missing or misaligned chain buffer and a negative link, then the op checks
+    assert lib.qgb_op_action_unitary_chain(4096, 0, 4, idx, 1, 4096, 0, 1, 0, None, 0, None) == -1
+    assert b"chain" in lib.qgb_last_error()
+    assert lib.qgb_op_action_unitary_chain(4096, 0, 4, idx, 1, 4096, 0, 1, 0, 4100, 0, None) == -1
+    assert lib.qgb_op_action_unitary_chain(4096, 0, 4, idx, 1, 4096, 0, 1, 0, 4096, -1, None) == -1
+    assert b"link" in lib.qgb_last_error()
+    assert lib.qgb_op_action_unitary_chain(4096, 0, 4, _lib.int_array([5]), 1, 4096, 0, 1, 0, 4096, 0, None) == -1
+    assert b"out of range" in lib.qgb_last_error()
 
 
 ADJ_FIELDS = ["op_k", "op_pos", "op_mat", "op_out", "op_gen_col", "op_gen_val"]

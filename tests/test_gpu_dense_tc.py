@@ -184,3 +184,67 @@ def test_unitary_entry_point_matches_and_preserves_group_norms(k, bits):
     assert abs(np.linalg.norm(got) - 1.0) < 2e-6
     assert np.max(np.abs(got - want)) / np.max(np.abs(want)) < 2e-5
     assert ref128.shape == got.shape
+
+
+@pytest.mark.parametrize("k,bits", [(6, [0, 1, 2, 3, 4, 5]), (6, [3, 8, 11, 14, 17, 19]), (5, [2, 7, 12, 16, 19]),
+                                    (4, [0, 1, 9, 18])])
+def test_norm_chain_holds_the_reference_norm(k, bits):
+    """50 applications of a unitary as links 0..49 of one norm chain
+    (qgb_op_action_unitary_chain), from a state of norm 0.7: the norm stays at
+    0.7 to within a pass's shrinkage, amplitudes match complex128; halfway a
+    3-qubit link (not a tensor-core block) clears the chain and the next link
+    starts a new one from the state as it is."""
+    from qaravan_gb300 import _lib
+    L = _lib.lib()
+    _lib.check(L.qgb_set_dense_impl(2))
+    n = 20
+    u = _rand_op(k, 11 + k)
+    u3 = _rand_op(3, 77)
+    v0 = _rand_state(n, 1, 5 * k) * 0.7
+    sv = v0.to(torch.complex64).cuda().contiguous()
+    ref = v0.to(torch.complex128).cuda().contiguous()
+    m = torch.as_tensor(u).to(torch.complex64).cuda().contiguous()
+    m3 = torch.as_tensor(u3).to(torch.complex64).cuda().contiguous()
+    mref = torch.as_tensor(u).to(torch.complex128).cuda().contiguous()
+    m3ref = torch.as_tensor(u3).to(torch.complex128).cuda().contiguous()
+    sites = _lib.int_array([n - 1 - b for b in bits])
+    sites3 = _lib.int_array([2, 9, 15])
+    chain = torch.zeros(6, dtype=torch.float64, device="cuda")
+    st = _lib.stream_ptr()
+    for i in range(50):
+        if i == 25:
+            _lib.check(L.qgb_op_action_unitary_chain(sv.data_ptr(), _lib.QGB_C64, n, sites3, 3, m3.data_ptr(), 0, 1, 0,
+                                                     chain.data_ptr(), i, st))
+            _lib.check(L.qgb_op_action(ref.data_ptr(), _lib.QGB_C128, n, sites3, 3, m3ref.data_ptr(), 0, 1, 0, st))
+        _lib.check(L.qgb_op_action_unitary_chain(sv.data_ptr(), _lib.QGB_C64, n, sites, k, m.data_ptr(), 0, 1, 0,
+                                                 chain.data_ptr(), i + (i >= 25), st))
+        _lib.check(L.qgb_op_action(ref.data_ptr(), _lib.QGB_C128, n, sites, k, mref.data_ptr(), 0, 1, 0, st))
+    _lib.check(L.qgb_check_status(st))
+    got, want = sv.to(torch.complex128).cpu().numpy(), ref.cpu().numpy()
+    assert abs(np.linalg.norm(got) - 0.7) < 0.7 * 1e-6
+    assert np.max(np.abs(got - want)) / np.max(np.abs(want)) < 2e-5
+
+
+def test_norm_modes_of_the_executor_agree():
+    """The same 20-qubit brickwork with the norm chain (default), group norms
+    restored in every pass, and no norm control: chain and row modes keep the
+    norm, all agree with complex128 within the complex64 bar, and without
+    control the norm drifts by the tensor cores' shrinkage."""
+    from qaravan_gb300 import StatevectorSim, _lib, engine, workloads
+    from qaravan_gb300.circuits import Circuit
+    _lib.check(_lib.lib().qgb_set_dense_impl(2))
+    n = 20
+    circ = Circuit(workloads.brickwork_gates(n, 20, 31), n=n)
+    v128 = StatevectorSim(circ, dtype=torch.complex128).get_statevector().cpu().numpy()
+    out = {}
+    try:
+        for mode in ("chain", "row", "off"):
+            engine.set_norm_restore(mode)
+            out[mode] = StatevectorSim(circ, dtype=torch.complex64).get_statevector().to(torch.complex128).cpu().numpy()
+    finally:
+        engine.set_norm_restore("chain")
+    for mode in ("chain", "row"):
+        assert abs(np.linalg.norm(out[mode]) - 1.0) < 1.5e-6
+    for v in out.values():
+        assert np.max(np.abs(v - v128)) < 1e-6
+    assert np.linalg.norm(out["off"]) < np.linalg.norm(out["chain"])
