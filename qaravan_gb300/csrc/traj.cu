@@ -40,6 +40,12 @@ struct TrajGateArgs {
     uint32_t seed0, seed1, event;
     int nblk;
     int log_paulis;    // write the sampled Pauli indices to the log
+    // staged access (a union bit below 5): a warp's 32 groups span the union bits and
+    // the 5 lowest other bits W (K + 5 bits, W's lowest five are bits 0..4); rank r of
+    // W has global offset wg[r] and shared-memory offset ws[r] in the warp's
+    // [component c][lane] array (row pitch 33)
+    int staged;
+    uint32_t wg[9], ws[9];
 };
 
 // v <- K on local position P (bit K_-1-P of the local index), K real 2x2.
@@ -75,13 +81,14 @@ __device__ __forceinline__ void kraus_dispatch(C (&v)[1 << K_], int p, const T k
 // per trajectory, are folded into the gd x gd gate matrix in registers.
 // Per amplitude that is 4 * (kp + gd) real FMAs instead of the 4 * 2^K of the
 // composed 2^K x 2^K product.
-template <typename T, int K, int KG>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) traj_gate_kernel(cplx<T>* __restrict__ sv, const cplx<T>* __restrict__ gate,
+template <typename T, int K, int KG, bool STAGED>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? (K <= 2 ? 4 : 2) : 1) traj_gate_kernel(cplx<T>* __restrict__ sv, const cplx<T>* __restrict__ gate,
                                                         const cplx<T>* __restrict__ kraus, double* __restrict__ partials,
                                                         uint8_t* __restrict__ pauli_log, const __grid_constant__ TrajGateArgs a) {
     using C = cplx<T>;
     constexpr int D = 1 << K, GD = 1 << KG, LOW = K - KG;
     __shared__ double red[8][4];
+    __shared__ C stg[STAGED ? 8 : 1][STAGED ? D * 33 : 1];
     const int64_t t = blockIdx.y;
     // ---- G' = (P_0 x P_1) G on the gate positions, every thread the same values
     C G[GD * GD];
@@ -146,19 +153,46 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) traj_gate_kernel(
     T pop[GD];
 #pragma unroll
     for (int b = 0; b < GD; ++b) pop[b] = 0;
+    uint32_t ws_lane = 0;  // staged: this lane's contribution to the shared-memory offset
+    if constexpr (STAGED) {
+#pragma unroll
+        for (int r = 0; r < 5; ++r)
+            if ((threadIdx.x >> r) & 1) ws_lane += a.ws[r];
+    }
     for (uint64_t g = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; g < groups; g += step) {
         uint64_t base = g;
+        if constexpr (STAGED) base &= ~uint64_t(31);
 #pragma unroll
         for (int j = 0; j < K; ++j) base = ((base >> srt[j]) << (srt[j] + 1)) | (base & ((uint64_t(1) << srt[j]) - 1));
         C* sb = s + base;
         C v[D];
+        if constexpr (STAGED) {
+            // the warp's 32 x D amplitudes in memory order, 256 contiguous bytes per load
+            const int lane = threadIdx.x & 31;
+            C* st = stg[threadIdx.x >> 5];
 #pragma unroll
-        for (int c = 0; c < D; ++c) {
-            uint32_t o = 0;
+            for (int i = 0; i < D; ++i) {
+                uint32_t go = lane, so = ws_lane;
 #pragma unroll
-            for (int j = 0; j < K; ++j)
-                if ((c >> (K - 1 - j)) & 1) o += m[j];
-            v[c] = sb[o];
+                for (int b = 0; b < K; ++b)
+                    if ((i >> b) & 1) {
+                        go += a.wg[5 + b];
+                        so += a.ws[5 + b];
+                    }
+                st[so] = sb[go];
+            }
+            __syncwarp();
+#pragma unroll
+            for (int c = 0; c < D; ++c) v[c] = st[c * 33 + lane];
+        } else {
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                uint32_t o = 0;
+#pragma unroll
+                for (int j = 0; j < K; ++j)
+                    if ((c >> (K - 1 - j)) & 1) o += m[j];
+                v[c] = sb[o];
+            }
         }
         if (a.kp > 0) kraus_dispatch<K>(v, a.ppos[0], kr[0]);
         if (a.kp > 1) kraus_dispatch<K>(v, a.ppos[1], kr[1]);
@@ -178,13 +212,33 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) traj_gate_kernel(
                 }
             }
         }
+        if constexpr (STAGED) {
+            const int lane = threadIdx.x & 31;
+            C* st = stg[threadIdx.x >> 5];
 #pragma unroll
-        for (int c = 0; c < D; ++c) {
-            uint32_t o = 0;
+            for (int c = 0; c < D; ++c) st[c * 33 + lane] = v[c];
+            __syncwarp();
 #pragma unroll
-            for (int j = 0; j < K; ++j)
-                if ((c >> (K - 1 - j)) & 1) o += m[j];
-            sb[o] = v[c];
+            for (int i = 0; i < D; ++i) {
+                uint32_t go = lane, so = ws_lane;
+#pragma unroll
+                for (int b = 0; b < K; ++b)
+                    if ((i >> b) & 1) {
+                        go += a.wg[5 + b];
+                        so += a.ws[5 + b];
+                    }
+                sb[go] = st[so];
+            }
+            __syncwarp();  // every lane's reads done before the next groups are staged
+        } else {
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                uint32_t o = 0;
+#pragma unroll
+                for (int j = 0; j < K; ++j)
+                    if ((c >> (K - 1 - j)) & 1) o += m[j];
+                sb[o] = v[c];
+            }
         }
     }
     // block reduction of the joint populations of the gate sites -> partials[(t * nblk + blk) * 4 + b]
@@ -272,8 +326,15 @@ template <typename T, int K, int KG>
 int launch_gate(void* sv, const void* gate, const void* kraus, double* partials, uint8_t* plog, const TrajGateArgs& a,
                 cudaStream_t st) {
     dim3 grid(unsigned(a.nblk), unsigned(a.ntraj));
-    traj_gate_kernel<T, K, KG><<<grid, 256, 0, st>>>((cplx<T>*)sv, (const cplx<T>*)gate, (const cplx<T>*)kraus,
-                                                     partials, plog, a);
+    if constexpr (sizeof(T) == 4) {
+        if (a.staged) {
+            traj_gate_kernel<T, K, KG, true><<<grid, 256, 0, st>>>((cplx<T>*)sv, (const cplx<T>*)gate,
+                                                                   (const cplx<T>*)kraus, partials, plog, a);
+            return check_launch("trajectory gate kernel");
+        }
+    }
+    traj_gate_kernel<T, K, KG, false><<<grid, 256, 0, st>>>((cplx<T>*)sv, (const cplx<T>*)gate, (const cplx<T>*)kraus,
+                                                            partials, plog, a);
     return check_launch("trajectory gate kernel");
 }
 
@@ -355,6 +416,31 @@ extern "C" int qgb_traj_step(void* sv, int dtype, int n, int64_t ntraj, int64_t 
     if (nu == 0) return QGB_OK;
     a.ku = nu;
     for (int j = 0; j < nu; ++j) a.ubits[j] = ub[j];
+    // staged access when a union bit is below 5 (complex64, at least one warp of groups)
+    int lowest = n;
+    for (int j = 0; j < nu; ++j) lowest = ub[j] < lowest ? ub[j] : lowest;
+    a.staged = (dtype == QGB_C64 && lowest < 5 && n - nu >= 5) ? 1 : 0;
+    if (a.staged) {
+        // W: the union bits and the 5 lowest other bits, ascending
+        int lane_bits[5], nl = 0, w = 0;
+        for (int b = 0; b < n && nl < 5; ++b) {
+            bool in_u = false;
+            for (int j = 0; j < nu; ++j) in_u |= ub[j] == b;
+            if (!in_u) lane_bits[nl++] = b;
+        }
+        for (int b = 0; b < n && w < nu + 5; ++b) {
+            int uj = -1, lt = -1;
+            for (int j = 0; j < nu; ++j)
+                if (ub[j] == b) uj = j;
+            for (int t2 = 0; t2 < 5; ++t2)
+                if (lane_bits[t2] == b) lt = t2;
+            if (uj < 0 && lt < 0) continue;
+            a.wg[w] = 1u << b;
+            a.ws[w] = uj >= 0 ? (1u << (nu - 1 - uj)) * 33u : (1u << lt);
+            ++w;
+        }
+        if (w != nu + 5 || a.wg[0] != 1u || a.wg[4] != 16u) return set_error(QGB_EINVAL, "staged trajectory geometry");
+    }
     a.p_dep = k > 0 ? p_dep : 0.0;
     a.seed0 = uint32_t(seed);
     a.seed1 = uint32_t(seed >> 32);

@@ -58,6 +58,14 @@ def circuit_ops(circ, n=None, build=False, nm=None):
     return seq
 
 
+def _gate_requires_grad(g):
+    """Whether a gate's matrix carries an autograd graph, without building a
+    parametrised gate's matrix that has not been read yet (its angles decide)."""
+    if getattr(g, "matrix_pending", lambda: False)():
+        return any(torch.is_tensor(a) and a.requires_grad for a in g.angles)
+    return torch.is_tensor(g.matrix) and g.matrix.requires_grad
+
+
 def gates_to_ops(seq, n):
     ops = []
     for g in seq:
@@ -135,8 +143,7 @@ class StatevectorSim:
         return self._exec
 
     def _needs_grad(self):
-        return torch.is_grad_enabled() and any(
-            torch.is_tensor(g.matrix) and g.matrix.requires_grad for g in self.circ.gate_list)
+        return torch.is_grad_enabled() and any(_gate_requires_grad(g) for g in self.circ.gate_list)
 
     def run(self, progress_bar=False, debug=0):
         """Apply the circuit to the initial state (``core/base_sim.py:30-53``)."""

@@ -165,3 +165,14 @@ def test_closed_form_rotations_for_complex64_adjoint():
     slow = _matrices(gates)
     for a, b in zip(fast, slow):
         assert a.shape == b.shape and torch.max(torch.abs(a - b.detach())).item() < 1e-9
+
+
+def test_gradient_check_reads_no_pending_matrix():
+    """The simulator decides whether a run needs the adjoint from the angles of
+    gates whose matrix is not built yet, without building it."""
+    from qaravan_gb300.gates import CNOT
+    from qaravan_gb300.statevector import _gate_requires_grad
+    th = torch.tensor([0.1, 0.2], dtype=torch.float64, requires_grad=True)
+    gates = [RY(0, th[0]), RZ(1, th[1].detach()), CNOT([0, 1], 2)]
+    assert [_gate_requires_grad(g) for g in gates] == [True, False, False]
+    assert gates[0].matrix_pending() and gates[1].matrix_pending()

@@ -70,12 +70,16 @@ def _replay(gates, n, t, seed, p_dep, gamma, plog, jlog):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("dtype", [torch.complex64, torch.complex128])
-def test_trajectory_replay_matches_oracle(dtype, cuda_ok):
+@pytest.mark.parametrize("dtype,n", [(torch.complex64, 6), (torch.complex128, 6), (torch.complex64, 10),
+                                     (torch.complex128, 10)])
+def test_trajectory_replay_matches_oracle(dtype, n, cuda_ok):
+    """Every trajectory replayed branch by branch through the oracle. At 10
+    qubits the unions of 2 to 4 bits that reach bits 0..4 take the warp-staged
+    access path (complex64)."""
     from qaravan_gb300 import workloads
     from qaravan_gb300.circuits import Circuit
     from qaravan_gb300.trajectories import TrajectorySim
-    n, T, seed, p, gamma = 6, 12, 77, 0.3, 0.35
+    T, seed, p, gamma = 12, 77, 0.3, 0.35
     gates = workloads.brickwork_gates(n, 3, 4)
     sim = TrajectorySim(Circuit(gates, n=n), T, p_dep=p, gamma=gamma, seed=seed, dtype=dtype, log=True)
     states = sim.run().cpu().numpy()
