@@ -308,9 +308,11 @@ def unitary_flags(ops, tol=1e-6):
         by_dim.setdefault(m.shape[0], []).append(i)
     for d, idx in by_dim.items():
         m = np.stack([np.asarray(ops[i].matrix, dtype=np.complex128) for i in idx])
-        err = np.abs(np.einsum("bji,bjk->bik", m.conj(), m) - np.eye(d)).max(axis=(1, 2))
-        for i, e in zip(idx, err):
-            flags[i] = bool(e < tol)
+        gram = np.matmul(m.conj().transpose(0, 2, 1), m)
+        gram[:, np.arange(d), np.arange(d)] -= 1
+        err = np.abs(gram).reshape(len(idx), -1).max(axis=1)
+        for i, e in zip(idx, err.tolist()):
+            flags[i] = e < tol
     return flags
 
 

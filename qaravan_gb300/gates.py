@@ -66,7 +66,11 @@ class Gate:
         return g
 
     def shallow_copy(self):
-        return Gate(self.name, self.indices, self.matrix, time=self.time)
+        # Gate(self.name, self.indices, self.matrix, time=self.time) without re-validating the indices
+        g = Gate.__new__(Gate)
+        g.name, g.indices, g.matrix, g.time = self.name, [int(i) for i in self.indices], self.matrix, self.time
+        g.span = len(g.indices)
+        return g
 
 
 def embed_operator(num_sites, active_sites, local_ops, local_dim=2, dense=False, factor=False):
