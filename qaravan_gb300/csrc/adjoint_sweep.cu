@@ -65,7 +65,9 @@ constexpr int kAdjMaxRun = 4;  // consecutive ops on the same sites handled in o
 // A run of R consecutive ops on the same K sites (R <= kAdjMaxRun): per group
 // of partner amplitudes, one load and one store of the staged tiles; for each
 // op of the run in order, the derivative (if wanted) at the op's output, then
-// U^dagger on both. threads tid = 0..nthr-1 of the CTA.
+// U^dagger on both (diagonal ones by one product per amplitude). A single op
+// without derivative whose U^dagger permutes (CNOT, SWAP, X) is a copy from the
+// permuted tile offsets. threads tid = 0..nthr-1 of the CTA.
 template <typename T, int K, int R>
 __device__ __forceinline__ void adj_tile_run(cplx<T>* __restrict__ pt, cplx<T>* __restrict__ lt, int m,
                                              const AdjSweepArgs& a, int op0, const cplx<T>* __restrict__ ush,
@@ -105,10 +107,74 @@ __device__ __forceinline__ void adj_tile_run(cplx<T>* __restrict__ pt, cplx<T>* 
             gc[q][r] = a.gcol[op0 + q][r];
         }
     }
+    // U^dagger diagonal (e.g. RZ, CZ): two complex products per row instead of a row of the matrix
+    bool diag[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+        bool d = true;
+#pragma unroll
+        for (int r = 0; r < D; ++r)
+#pragma unroll
+            for (int c = 0; c < D; ++c)
+                if (r != c) d = d && ud[q][r * D + c].x == T(0) && ud[q][r * D + c].y == T(0);
+        diag[q] = d;
+    }
+    const uint32_t groups = 1u << (m - K);
+    if constexpr (R == 1) {
+        // a single op without derivative whose U^dagger is a permutation with unit entries
+        // (CNOT, SWAP, X): out[r] = in[col(r)], read straight from the permuted tile offsets
+        if (!want[0]) {
+            int col[D];
+            bool perm = true;
+#pragma unroll
+            for (int r = 0; r < D; ++r) {
+                int nz = 0;
+                col[r] = 0;
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    const C u = ud[0][r * D + c];
+                    if (u.x != T(0) || u.y != T(0)) {
+                        ++nz;
+                        col[r] = c;
+                        perm = perm && u.x == T(1) && u.y == T(0);
+                    }
+                }
+                perm = perm && nz == 1;
+            }
+            if (perm) {
+                uint32_t poff[D];
+#pragma unroll
+                for (int r = 0; r < D; ++r) {
+                    uint32_t o = 0;
+#pragma unroll
+                    for (int j = 0; j < K; ++j) o |= uint32_t((col[r] >> (K - 1 - j)) & 1) << pos[j];
+                    poff[r] = swz<T>(o);
+                }
+                for (uint32_t g = tid; g < groups; g += nthr) {
+                    uint32_t base = g;
+#pragma unroll
+                    for (int j = 0; j < K; ++j)
+                        base = ((base >> srt[j]) << (srt[j] + 1)) | (base & ((1u << srt[j]) - 1));
+                    const uint32_t sb = swz<T>(base);
+                    C p[D], l[D];
+#pragma unroll
+                    for (int r = 0; r < D; ++r) {
+                        p[r] = pt[sb ^ poff[r]];
+                        l[r] = lt[sb ^ poff[r]];
+                    }
+#pragma unroll
+                    for (int r = 0; r < D; ++r) {
+                        pt[sb ^ soff[r]] = p[r];
+                        lt[sb ^ soff[r]] = l[r];
+                    }
+                }
+                return;
+            }
+        }
+    }
     T s[R];
 #pragma unroll
     for (int q = 0; q < R; ++q) s[q] = T(0);
-    const uint32_t groups = 1u << (m - K);
     for (uint32_t g = tid; g < groups; g += nthr) {
         uint32_t base = g;
 #pragma unroll
@@ -134,22 +200,33 @@ __device__ __forceinline__ void adj_tile_run(cplx<T>* __restrict__ pt, cplx<T>* 
                     s[q] += l[r].x * w.y - l[r].y * w.x;  // Im(conj(l) w)
                 }
             }
-            C pn[D], ln[D];
+            if (diag[q]) {
 #pragma unroll
-            for (int r = 0; r < D; ++r) {
-                C x = mk<T>(0, 0), y = mk<T>(0, 0);
-#pragma unroll
-                for (int c = 0; c < D; ++c) {
-                    cfma(x, ud[q][r * D + c], p[c]);
-                    cfma(y, ud[q][r * D + c], l[c]);
+                for (int r = 0; r < D; ++r) {
+                    C x = mk<T>(0, 0), y = mk<T>(0, 0);
+                    cfma(x, ud[q][r * D + r], p[r]);
+                    cfma(y, ud[q][r * D + r], l[r]);
+                    p[r] = x;
+                    l[r] = y;
                 }
-                pn[r] = x;
-                ln[r] = y;
-            }
+            } else {
+                C pn[D], ln[D];
 #pragma unroll
-            for (int r = 0; r < D; ++r) {
-                p[r] = pn[r];
-                l[r] = ln[r];
+                for (int r = 0; r < D; ++r) {
+                    C x = mk<T>(0, 0), y = mk<T>(0, 0);
+#pragma unroll
+                    for (int c = 0; c < D; ++c) {
+                        cfma(x, ud[q][r * D + c], p[c]);
+                        cfma(y, ud[q][r * D + c], l[c]);
+                    }
+                    pn[r] = x;
+                    ln[r] = y;
+                }
+#pragma unroll
+                for (int r = 0; r < D; ++r) {
+                    p[r] = pn[r];
+                    l[r] = ln[r];
+                }
             }
         }
 #pragma unroll
