@@ -424,9 +424,14 @@ def section_trajectories(n=20, ntraj=1024, steps=40):
     mean, _ = sim.mean_expectations(z_terms(n))
     m = mean.cpu().numpy()
     ng = len(sim.gates)
+    # every gate reads and writes every trajectory's state once
+    alg = ng * 2 * ntraj * 2 ** n * 8
+    peak, peak_kind = _peaks()
     return {"qubits": n, "trajectories": ntraj, "gates": ng, "ms_per_run": round(ms, 2),
             "trajectories_per_s": round(ntraj / (ms / 1e3), 1),
             "trajectory_gates_per_s": round(ntraj * ng / (ms / 1e3), 1), "launches_per_run": sim.launches,
+            "algorithmic_tb": round(alg / 1e12, 2), "hbm_frac": round(alg / (ms / 1e3) / 1e9 / peak, 3),
+            "hbm_frac_of": f"hbm_gbs of {peak_kind}",
             "mean_z_first": float(m[0]), "mean_zz_first": float(m[n])}
 
 
@@ -443,11 +448,17 @@ def section_dm_batch(count=256, seed=7):
     compile_s = time.perf_counter() - t0
     ms = _event_ms(lambda: batch.run(graph=True), 1, 1)
     res = batch.results()
+    # algorithmic HBM bytes of the stream-parallel circuits: every pass reads and writes vec(rho)
+    passes = sum(ex.plan.n_sweeps for _, _, ex, _, _, _ in batch.large)
+    alg = sum(ex.plan.n_sweeps * 2 * 4 ** s.num_sites * 8 for _, s, ex, _, _, _ in batch.large)
+    peak, peak_kind = _peaks()
     out = {"circuits": count, "small_batched": len(batch.small), "stream_parallel": len(batch.large),
            "compile_s": round(compile_s, 2), "ms_per_batch": round(ms, 1),
            "circuits_per_s": round(count / (ms / 1e3), 2),
            "max_trace_error": float(max(abs(r["trace"] - 1) for r in res)),
-           "state_gb": round(sum(4 ** n * 8 for n, _, _ in specs) / 1e9, 1)}
+           "state_gb": round(sum(4 ** n * 8 for n, _, _ in specs) / 1e9, 1),
+           "large_passes": passes, "large_algorithmic_tb": round(alg / 1e12, 2),
+           "hbm_frac": round(alg / (ms / 1e3) / 1e9 / peak, 3), "hbm_frac_of": f"hbm_gbs of {peak_kind}"}
     del batch, sims
     torch.cuda.empty_cache()
     return out
