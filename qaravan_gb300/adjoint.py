@@ -257,6 +257,24 @@ def _rotation_angle(g):
     return a
 
 
+def _stack_angles(angles):
+    """All rotation angles as one float64 host vector for autograd. When every
+    angle is a one-element view of the same contiguous tensor (``th[l, q, k]``,
+    as a parameter tensor is usually indexed), one gather from that tensor
+    replaces a stack of per-angle selects, so the backward is one scatter rather
+    than one autograd node per angle; the values and gradients are the same."""
+    if not angles:
+        return torch.zeros(0, dtype=torch.float64)
+    base = angles[0]._base
+    if (base is not None and base.is_contiguous()
+            and all(a._base is base and a.numel() == 1 and a.dtype == base.dtype for a in angles)):
+        idx = torch.tensor([a.storage_offset() - base.storage_offset() for a in angles], dtype=torch.long,
+                           device=base.device)
+        out = base.reshape(-1).index_select(0, idx)
+        return (out.cpu() if out.is_cuda else out).to(torch.float64)
+    return torch.stack([(a.cpu() if a.is_cuda else a).reshape(()).to(torch.float64) for a in angles])
+
+
 class _Inputs:
     """How the gates enter autograd. A rotation gate exp(-i theta P) built from
     a torch angle contributes its angle (all such angles stacked into one
@@ -272,11 +290,10 @@ class _Inputs:
             a = _rotation_angle(g)
             if a is not None:
                 self.rot.append(i)
-                angles.append(a.reshape(()).to(torch.float64))
+                angles.append(a)
         rs = set(self.rot)
         self.other = [i for i in range(len(gates)) if i not in rs]
-        self.angles = (torch.stack([a.cpu() if a.is_cuda else a for a in angles]) if angles
-                       else torch.zeros(0, dtype=torch.float64))
+        self.angles = _stack_angles(angles)
         self.kinds = np.array([_KIND[gates[i].name] for i in self.rot], dtype=np.int64)
 
     def args(self):

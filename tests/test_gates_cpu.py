@@ -176,3 +176,26 @@ def test_gradient_check_reads_no_pending_matrix():
     gates = [RY(0, th[0]), RZ(1, th[1].detach()), CNOT([0, 1], 2)]
     assert [_gate_requires_grad(g) for g in gates] == [True, False, False]
     assert gates[0].matrix_pending() and gates[1].matrix_pending()
+
+
+def test_stacked_angles_gather_from_one_parameter_tensor():
+    """The adjoint's angle vector: one gather when every angle is an element view
+    of the same tensor (also through a transposed view), a stack otherwise; the
+    same values and the same gradient either way."""
+    from qaravan_gb300.adjoint import _stack_angles
+    th = torch.randn(5, 4, 2, dtype=torch.float64, requires_grad=True)
+    views = [th[l, q, k] for l in range(5) for q in range(4) for k in range(2)][::-1]
+    w = torch.randn(len(views), dtype=torch.float64)
+    a = _stack_angles(views)
+    assert a.grad_fn is not None and "IndexSelect" in type(a.grad_fn).__name__
+    (a * w).sum().backward()
+    g = th.grad.clone()
+    th.grad = None
+    b = torch.stack([v.reshape(()) for v in views])
+    (b * w).sum().backward()
+    assert torch.equal(a.detach(), b.detach()) and torch.equal(g, th.grad)
+    tt = th.transpose(0, 2)
+    assert torch.equal(_stack_angles([tt[1, 3, 4], tt[0, 2, 1]]).detach(), torch.stack([th[4, 3, 1], th[1, 2, 0]]).detach())
+    other = torch.tensor([0.5, 0.25], dtype=torch.float64, requires_grad=True)
+    mixed = _stack_angles([th[0, 0, 0], other[1], other * 2][:2])
+    assert "Stack" in type(mixed.grad_fn).__name__ and mixed[1].item() == 0.25
