@@ -460,6 +460,12 @@ class BatchedAnsatz:
         self._kinds = torch.tensor(kinds, dtype=torch.int32, device=self.device)
         self._pidx = torch.tensor(pidx, dtype=torch.int32, device=self.device)
         self._fixed = fixed
+        # one gate-matrix row per gate: the fixed gates' matrices in place, rotations
+        # left for qgb_param_matrices; copied to every parameter set in one step
+        tmpl = np.zeros((len(gates), 16), dtype=np.complex128)
+        for i, m in fixed:
+            tmpl[i, :m.size] = m.reshape(-1)
+        self._template = torch.from_numpy(tmpl).to(self.dtype).to(self.device)
         by_param = [[] for _ in range(self.nparams)]
         for g, (k, p) in enumerate(zip(kinds, pidx)):
             if k:
@@ -505,9 +511,7 @@ class BatchedAnsatz:
 
     def _matrices(self, params, P):
         G = len(self.gates)
-        mats = torch.zeros(P, G, 16, dtype=self.dtype, device=self.device)
-        for i, m in self._fixed:
-            mats[:, i, :m.size] = torch.as_tensor(m.reshape(-1)).to(self.dtype).to(self.device)
+        mats = self._template.unsqueeze(0).expand(P, G, 16).contiguous()
         _lib.check(_lib.lib().qgb_param_matrices(self._kinds.data_ptr(), self._pidx.data_ptr(), G, params.data_ptr(),
                                                  self.nparams, P, mats.data_ptr(), self.code, 16, 16 * G,
                                                  _lib.stream_ptr(self.device)), "param_matrices")
