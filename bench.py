@@ -285,7 +285,7 @@ def section_adjoint(n=24, layers=40, base_layers=4):
         torch.cuda.synchronize()
         return time.perf_counter() - t0, float(e.item()), th.grad.numpy().copy()
 
-    adjoint_run(2)
+    adjoint_run(layers)  # warm-up: plans and caches of this circuit structure, as a training loop has them
     torch.cuda.reset_peak_memory_stats()
     base = torch.cuda.memory_allocated()
     t_full, e_full, _ = adjoint_run(layers)
@@ -316,7 +316,8 @@ def section_adjoint(n=24, layers=40, base_layers=4):
                         .pauli_sum_expectation(terms))
         shift_err = max(shift_err, abs((e_pm[0] - e_pm[1]) - g128[idx]))
     out["c128_grad_max_abs_err_vs_parameter_shift"] = float(shift_err)
-    # the reference's torch path at a depth that fits, same depth for the adjoint
+    # the reference's torch path at a depth that fits, same depth for the adjoint (both warmed up)
+    adjoint_run(base_layers)
     t_adj_b, e_adj_b, g_adj_b = adjoint_run(base_layers)
     params = workloads.hea_params(n, base_layers, 1)
     e_w, _ = _torch_reference_energy(n, 1, params[:1], terms, "cuda")  # warm-up of the torch path

@@ -80,35 +80,59 @@ __global__ void __launch_bounds__(kRedThreads) pauli_group_kernel(const cplx<T>*
     const int nblk = gridDim.x;
     Acc<T, NT> acc;
     const uint64_t stride = uint64_t(nblk) * blockDim.x;
+    // grid-stride loops unrolled so that each thread has several independent loads in flight
     if (g.xmask == 0) {
+        constexpr int U = 4;
         const uint64_t len = uint64_t(1) << n;
-        for (uint64_t x = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; x < len; x += stride) {
-            const cplx<T> a = s[x];
-            const T p = a.x * a.x + a.y * a.y;
+        for (uint64_t x0 = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; x0 < len; x0 += U * stride) {
+            cplx<T> a[U];
 #pragma unroll
-            for (int j = 0; j < NT; ++j)
-                if (j < g.nterms) acc.add(j, (__popcll(x & g.zmask[j]) & 1) ? -p : p);
-            acc.step();
+            for (int u = 0; u < U; ++u) a[u] = x0 + u * stride < len ? s[x0 + u * stride] : mk<T>(T(0), T(0));
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint64_t x = x0 + u * stride;
+                if (x >= len) break;
+                const T p = a[u].x * a[u].x + a[u].y * a[u].y;
+#pragma unroll
+                for (int j = 0; j < NT; ++j)
+                    if (j < g.nterms) acc.add(j, (__popcll(x & g.zmask[j]) & 1) ? -p : p);
+                acc.step();
+            }
         }
     } else {
         // visit each pair {x, x ^ xmask} once: x has a zero at the top bit of xmask
+        constexpr int U = 2;
         const int top = 63 - __clzll(g.xmask);
         const uint64_t half = uint64_t(1) << (n - 1);
-        for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < half; i += stride) {
-            const uint64_t x = ((i >> top) << (top + 1)) | (i & ((uint64_t(1) << top) - 1));
-            const uint64_t y = x ^ g.xmask;
-            const cplx<T> a = s[x], c = s[y];
-            // v = conj(psi[y]) psi[x] contributes at x; conj(v) contributes at y
-            const T vr = c.x * a.x + c.y * a.y;
-            const T vi = c.x * a.y - c.y * a.x;
+        for (uint64_t i0 = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i0 < half; i0 += U * stride) {
+            cplx<T> a[U], c[U];
+            uint64_t xs[U];
 #pragma unroll
-            for (int j = 0; j < NT; ++j)
-                if (j < g.nterms) {
-                    const T tx = re_iny<T>(vr, vi, g.ny[j]);
-                    const T ty = re_iny<T>(vr, -vi, g.ny[j]);
-                    acc.add(j, ((__popcll(x & g.zmask[j]) & 1) ? -tx : tx) + ((__popcll(y & g.zmask[j]) & 1) ? -ty : ty));
+            for (int u = 0; u < U; ++u) {
+                const uint64_t i = i0 + u * stride;
+                xs[u] = ((i >> top) << (top + 1)) | (i & ((uint64_t(1) << top) - 1));
+                a[u] = c[u] = mk<T>(T(0), T(0));
+                if (i < half) {
+                    a[u] = s[xs[u]];
+                    c[u] = s[xs[u] ^ g.xmask];
                 }
-            acc.step();
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (i0 + u * stride >= half) break;
+                const uint64_t x = xs[u], y = x ^ g.xmask;
+                // v = conj(psi[y]) psi[x] contributes at x; conj(v) contributes at y
+                const T vr = c[u].x * a[u].x + c[u].y * a[u].y;
+                const T vi = c[u].x * a[u].y - c[u].y * a[u].x;
+#pragma unroll
+                for (int j = 0; j < NT; ++j)
+                    if (j < g.nterms) {
+                        const T tx = re_iny<T>(vr, vi, g.ny[j]);
+                        const T ty = re_iny<T>(vr, -vi, g.ny[j]);
+                        acc.add(j, ((__popcll(x & g.zmask[j]) & 1) ? -tx : tx) + ((__popcll(y & g.zmask[j]) & 1) ? -ty : ty));
+                    }
+                acc.step();
+            }
         }
     }
     acc.flush();
@@ -139,10 +163,17 @@ __global__ void __launch_bounds__(kRedThreads) norm2_kernel(const cplx<T>* __res
     const cplx<T>* s = sv + int64_t(blockIdx.y) * sv_stride;
     const uint64_t len = uint64_t(1) << n, stride = uint64_t(gridDim.x) * blockDim.x;
     Acc<T, 1> acc;
-    for (uint64_t x = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; x < len; x += stride) {
-        const cplx<T> a = s[x];
-        acc.add(0, a.x * a.x + a.y * a.y);
-        acc.step();
+    constexpr int U = 4;  // independent loads in flight per thread
+    for (uint64_t x0 = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; x0 < len; x0 += U * stride) {
+        cplx<T> a[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) a[u] = x0 + u * stride < len ? s[x0 + u * stride] : mk<T>(T(0), T(0));
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (x0 + u * stride >= len) break;
+            acc.add(0, a[u].x * a[u].x + a[u].y * a[u].y);
+            acc.step();
+        }
     }
     acc.flush();
     block_reduce_store<1>(acc.d, partials + int64_t(blockIdx.y) * gridDim.x + blockIdx.x, gridDim.x);
@@ -157,11 +188,23 @@ __global__ void __launch_bounds__(kRedThreads) inner_kernel(const cplx<T>* __res
     const cplx<T>* y = bv + b * stride_ab;
     const uint64_t len = uint64_t(1) << n, stride = uint64_t(gridDim.x) * blockDim.x;
     Acc<T, 2> acc;
-    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < len; i += stride) {
-        const cplx<T> u = x[i], v = y[i];
-        acc.add(0, u.x * v.x + u.y * v.y);
-        acc.add(1, u.x * v.y - u.y * v.x);
-        acc.step();
+    constexpr int U = 2;  // independent loads in flight per thread
+    for (uint64_t i0 = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i0 < len; i0 += U * stride) {
+        cplx<T> us[U], vs[U];
+#pragma unroll
+        for (int k = 0; k < U; ++k) {
+            const uint64_t i = i0 + k * stride;
+            us[k] = i < len ? x[i] : mk<T>(T(0), T(0));
+            vs[k] = i < len ? y[i] : mk<T>(T(0), T(0));
+        }
+#pragma unroll
+        for (int k = 0; k < U; ++k) {
+            if (i0 + k * stride >= len) break;
+            const cplx<T> u = us[k], v = vs[k];
+            acc.add(0, u.x * v.x + u.y * v.y);
+            acc.add(1, u.x * v.y - u.y * v.x);
+            acc.step();
+        }
     }
     acc.flush();
     block_reduce_store<2>(acc.d, partials + (b * 2) * gridDim.x + blockIdx.x, gridDim.x);
