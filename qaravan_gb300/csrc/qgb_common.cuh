@@ -61,14 +61,15 @@ template <> __device__ __forceinline__ uint32_t swz<float>(uint32_t e) { return 
 template <> __device__ __forceinline__ uint32_t swz<double>(uint32_t e) { return e ^ ((e >> 3) & 7u); }
 
 // Per-thread accumulators. complex128 states sum in float64 throughout. For
-// complex64 states the products and the running sums are float32 over chunks
-// of kChunk grid-stride iterations, each chunk then folded into a float64 sum:
-// the FP64 pipe of this part runs at a small fraction of its FP32 rate, and
-// float64 arithmetic on every element (conversions included) made these
-// kernels compute-bound far below HBM speed. A float32 chunk sum of kChunk
-// terms carries a relative error of at most kChunk * 2^-24 of the sum of the
-// magnitudes (well inside complex64 tolerances); the order stays fixed, so
-// results remain bitwise reproducible.
+// complex64 states the products and the running sums are float32 in two
+// levels -- chunks of kChunk grid-stride iterations, kChunk chunks summed into
+// a second float32 sum -- which is then folded into a float64 sum: the FP64
+// pipe of this part runs at a small fraction of its FP32 rate, and float64
+// arithmetic on every element (conversions included), or even once per chunk,
+// kept these kernels bound by that pipe far below HBM speed. Each level of
+// kChunk float32 terms carries a relative error of at most kChunk * 2^-24 of
+// the sum of the magnitudes (well inside complex64 tolerances); the order stays
+// fixed, so results remain bitwise reproducible.
 constexpr int kChunk = 16;
 
 template <typename T, int NV>
@@ -86,26 +87,39 @@ struct Acc {
 template <int NV>
 struct Acc<float, NV> {
     double d[NV];
-    float f[NV];
-    int cnt;
-    __device__ __forceinline__ Acc() : cnt(0) {
+    float f[NV], g[NV];
+    int cnt, cnt2;
+    __device__ __forceinline__ Acc() : cnt(0), cnt2(0) {
 #pragma unroll
         for (int j = 0; j < NV; ++j) {
             d[j] = 0.0;
-            f[j] = 0.0f;
+            f[j] = g[j] = 0.0f;
         }
     }
     __device__ __forceinline__ void add(int j, float v) { f[j] += v; }
-    __device__ __forceinline__ void flush() {
+    // the chunk into the second level
+    __device__ __forceinline__ void chunk() {
 #pragma unroll
         for (int j = 0; j < NV; ++j) {
-            d[j] += double(f[j]);
+            g[j] += f[j];
             f[j] = 0.0f;
         }
         cnt = 0;
     }
+    __device__ __forceinline__ void flush() {
+        chunk();
+#pragma unroll
+        for (int j = 0; j < NV; ++j) {
+            d[j] += double(g[j]);
+            g[j] = 0.0f;
+        }
+        cnt2 = 0;
+    }
     __device__ __forceinline__ void step() {
-        if (++cnt == kChunk) flush();
+        if (++cnt == kChunk) {
+            if (++cnt2 == kChunk) flush();
+            else chunk();
+        }
     }
 };
 

@@ -71,7 +71,12 @@ __device__ __forceinline__ R re_iny(R re, R im, int ny) {
 
 // One pass over the vector for all terms sharing one X mask.
 // partials[(b * nslots + slot) * nblk + blk]
-template <typename T, int NT>
+__device__ __forceinline__ int popc_any(uint32_t v) { return __popc(v); }
+__device__ __forceinline__ int popc_any(uint64_t v) { return __popcll(v); }
+
+// I: the index type, 32-bit for vectors of up to 2^31 entries (cheaper loop and
+// mask arithmetic than 64-bit), else 64-bit.
+template <typename T, int NT, typename I>
 __global__ void __launch_bounds__(kRedThreads) pauli_group_kernel(const cplx<T>* __restrict__ sv, int n, int64_t sv_stride,
                                                                   const __grid_constant__ PauliGroup g, int nslots,
                                                                   double* __restrict__ partials) {
@@ -79,23 +84,26 @@ __global__ void __launch_bounds__(kRedThreads) pauli_group_kernel(const cplx<T>*
     const cplx<T>* s = sv + b * sv_stride;
     const int nblk = gridDim.x;
     Acc<T, NT> acc;
-    const uint64_t stride = uint64_t(nblk) * blockDim.x;
+    const I stride = I(nblk) * blockDim.x;
+    I zm[NT];
+#pragma unroll
+    for (int j = 0; j < NT; ++j) zm[j] = I(g.zmask[j]);
     // grid-stride loops unrolled so that each thread has several independent loads in flight
     if (g.xmask == 0) {
         constexpr int U = 4;
-        const uint64_t len = uint64_t(1) << n;
-        for (uint64_t x0 = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; x0 < len; x0 += U * stride) {
+        const I len = I(1) << n;
+        for (I x0 = I(blockIdx.x) * blockDim.x + threadIdx.x; x0 < len; x0 += U * stride) {
             cplx<T> a[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) a[u] = x0 + u * stride < len ? s[x0 + u * stride] : mk<T>(T(0), T(0));
 #pragma unroll
             for (int u = 0; u < U; ++u) {
-                const uint64_t x = x0 + u * stride;
+                const I x = x0 + u * stride;
                 if (x >= len) break;
                 const T p = a[u].x * a[u].x + a[u].y * a[u].y;
 #pragma unroll
                 for (int j = 0; j < NT; ++j)
-                    if (j < g.nterms) acc.add(j, (__popcll(x & g.zmask[j]) & 1) ? -p : p);
+                    if (j < g.nterms) acc.add(j, (popc_any(I(x & zm[j])) & 1) ? -p : p);
                 acc.step();
             }
         }
@@ -103,24 +111,25 @@ __global__ void __launch_bounds__(kRedThreads) pauli_group_kernel(const cplx<T>*
         // visit each pair {x, x ^ xmask} once: x has a zero at the top bit of xmask
         constexpr int U = 2;
         const int top = 63 - __clzll(g.xmask);
-        const uint64_t half = uint64_t(1) << (n - 1);
-        for (uint64_t i0 = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i0 < half; i0 += U * stride) {
+        const I xm = I(g.xmask);
+        const I half = I(1) << (n - 1);
+        for (I i0 = I(blockIdx.x) * blockDim.x + threadIdx.x; i0 < half; i0 += U * stride) {
             cplx<T> a[U], c[U];
-            uint64_t xs[U];
+            I xs[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
-                const uint64_t i = i0 + u * stride;
-                xs[u] = ((i >> top) << (top + 1)) | (i & ((uint64_t(1) << top) - 1));
+                const I i = i0 + u * stride;
+                xs[u] = ((i >> top) << (top + 1)) | (i & ((I(1) << top) - 1));
                 a[u] = c[u] = mk<T>(T(0), T(0));
                 if (i < half) {
                     a[u] = s[xs[u]];
-                    c[u] = s[xs[u] ^ g.xmask];
+                    c[u] = s[xs[u] ^ xm];
                 }
             }
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 if (i0 + u * stride >= half) break;
-                const uint64_t x = xs[u], y = x ^ g.xmask;
+                const I x = xs[u], y = x ^ xm;
                 // v = conj(psi[y]) psi[x] contributes at x; conj(v) contributes at y
                 const T vr = c[u].x * a[u].x + c[u].y * a[u].y;
                 const T vi = c[u].x * a[u].y - c[u].y * a[u].x;
@@ -129,7 +138,7 @@ __global__ void __launch_bounds__(kRedThreads) pauli_group_kernel(const cplx<T>*
                     if (j < g.nterms) {
                         const T tx = re_iny<T>(vr, vi, g.ny[j]);
                         const T ty = re_iny<T>(vr, -vi, g.ny[j]);
-                        acc.add(j, ((__popcll(x & g.zmask[j]) & 1) ? -tx : tx) + ((__popcll(y & g.zmask[j]) & 1) ? -ty : ty));
+                        acc.add(j, ((popc_any(I(x & zm[j])) & 1) ? -tx : tx) + ((popc_any(I(y & zm[j])) & 1) ? -ty : ty));
                     }
                 acc.step();
             }
@@ -595,8 +604,12 @@ void launch_group(const void* sv, int n, int64_t stride, const PauliGroup& g, in
     dim3 grid(red_blocks(nbits), unsigned(batch));
     if (dm)
         dm_pauli_kernel<T, NT><<<grid, kRedThreads, 0, st>>>((const cplx<T>*)sv, n, stride, g, nslots, partials);
+    else if (n <= 31)
+        pauli_group_kernel<T, NT, uint32_t><<<grid, kRedThreads, 0, st>>>((const cplx<T>*)sv, n, stride, g, nslots,
+                                                                          partials);
     else
-        pauli_group_kernel<T, NT><<<grid, kRedThreads, 0, st>>>((const cplx<T>*)sv, n, stride, g, nslots, partials);
+        pauli_group_kernel<T, NT, uint64_t><<<grid, kRedThreads, 0, st>>>((const cplx<T>*)sv, n, stride, g, nslots,
+                                                                          partials);
 }
 
 template <typename T>
