@@ -22,8 +22,9 @@ class Circuit:
     def __init__(self, gate_list, n=None, local_dim=2, meas_sites=None, requires_decomp=False):
         self.gate_list = list(gate_list)
         if len(self.gate_list) != 0:
-            sites = np.concatenate([g.indices for g in self.gate_list])
-            self.num_sites = int(max(sites) + 1) if n is None else n
+            if n is None:
+                n = int(max(max(g.indices) for g in self.gate_list) + 1)
+            self.num_sites = n
             self.local_dim = self.gate_list[0].get_local_dim()
         else:
             self.num_sites = n

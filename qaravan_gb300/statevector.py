@@ -68,14 +68,18 @@ def _gate_requires_grad(g):
 
 def gates_to_ops(seq, n):
     ops = []
+    top = n - 1
     for g in seq:
-        if g.name == "ID" and getattr(g, "nm", None) is not None:
+        name = g.name
+        if name == "ID" and getattr(g, "nm", None) is not None:
             continue  # identity on a statevector (ID.matrix = eye)
-        if np.shape(g.matrix)[0] != 2 ** len(g.indices):
+        m = g.matrix
+        m = m if type(m) is np.ndarray and m.dtype == np.complex128 else _to_np(m)
+        idx = g.indices
+        if m.shape[0] != 1 << len(idx):
             raise NotImplementedError("qaravan_gb300 supports qubits only (local_dim 2)")
-        bits = [n - 1 - int(q) for q in g.indices]
-        ops.append(Op(bits, _to_np(g.matrix)))
-        if g.name == "Reset" and getattr(g, "normalize", True):
+        ops.append(Op([top - int(q) for q in idx], m))
+        if name == "Reset" and getattr(g, "normalize", True):
             ops.append(None)
     return ops
 
