@@ -221,18 +221,3 @@ def test_msp_via_environments_cost_is_the_final_overlap():
             m = np.asarray(g.matrix)
             assert np.max(np.abs(m @ m.conj().T - np.eye(2))) < 1e-12
 
-
-def test_unitary_embedding_keeps_the_given_columns():
-    """The deprecated embedding: the given input columns map to their outputs,
-    the other columns are an orthonormal basis of the null space of (out^T in)^T."""
-    from qaravan_gb300.applications import unitary_embedding
-    rng = np.random.default_rng(4)
-    outs = []
-    for _ in range(2):
-        v = rng.normal(size=8) + 1j * rng.normal(size=8)
-        outs.append(v / np.linalg.norm(v))
-    a = unitary_embedding(["010", "111"], outs)
-    assert np.max(np.abs(a[:, 2] - outs[0])) < 1e-15 and np.max(np.abs(a[:, 7] - outs[1])) < 1e-15
-    rest = a[:, [0, 1, 3, 4, 5, 6]]
-    assert np.max(np.abs(rest.conj().T @ rest - np.eye(6))) < 1e-12
-    assert np.max(np.abs(a[:, [2, 7]].T @ rest)) < 1e-12
