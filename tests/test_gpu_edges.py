@@ -84,3 +84,35 @@ def test_smallest_tensor_core_state_matches_oracle():
     sv = _sv(Circuit(gates, n=n), torch.complex64, mode="fused", fusion_width=6, init_state=init)
     assert np.max(np.abs(sv - ref.run_sv(gates, n, init_state=init))) < 1e-5
     assert abs(np.linalg.norm(sv) - 1) < 1e-6
+
+
+def test_noise_free_trajectories_equal_the_statevector():
+    """With no noise every trajectory is the ideal state: 64 trajectories of the
+    20-qubit TFI Trotter circuit against StatevectorSim (complex64), and each
+    trajectory's norm stays 1 with amplitude damping alone."""
+    from qaravan_gb300 import workloads
+    from qaravan_gb300.trajectories import TrajectorySim
+    n = 20
+    circ = workloads.tfi_trotter_circuit(n, 0.05, 2)
+    ideal = _sv(circ, torch.complex64)
+    states = TrajectorySim(circ, 64, p_dep=0.0, gamma=0.0, seed=5).run()
+    err = (states.to(torch.complex128).cpu() - torch.from_numpy(ideal)).abs().max().item()
+    assert err < 1e-5
+    damped = TrajectorySim(circ, 64, p_dep=0.0, gamma=0.05, seed=5).run()
+    norms = torch.linalg.vector_norm(damped.to(torch.complex128), dim=1).cpu().numpy()
+    assert np.max(np.abs(norms - 1)) < 1e-5
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+def test_unitary_density_matrix_is_the_pure_state(dtype):
+    """A noise-free density-matrix run equals |psi><psi| of the statevector run
+    of the same circuit (10 qubits, brickwork)."""
+    from qaravan_gb300 import DensityMatrixSim, workloads
+    from qaravan_gb300.circuits import Circuit
+    n = 10
+    gates = workloads.brickwork_gates(n, 4, 17)
+    psi = _sv(Circuit(gates, n=n), dtype)
+    dm = DensityMatrixSim(Circuit(gates, n=n), dtype=dtype)
+    dm.run()
+    rho = dm.get_density_matrix().reshape(2 ** n, 2 ** n).to(torch.complex128).cpu().numpy()
+    assert np.max(np.abs(rho - np.outer(psi, psi.conj()))) < TOL[dtype]
