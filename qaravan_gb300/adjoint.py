@@ -272,7 +272,12 @@ def _stack_angles(angles):
                            device=base.device)
         out = base.reshape(-1).index_select(0, idx)
         return (out.cpu() if out.is_cuda else out).to(torch.float64)
-    return torch.stack([(a.cpu() if a.is_cuda else a).reshape(()).to(torch.float64) for a in angles])
+    vals = [a.reshape(()).to(torch.float64) for a in angles]
+    try:
+        out = torch.stack(vals)  # one copy to the host when the angles share a device
+    except RuntimeError:
+        return torch.stack([v.cpu() for v in vals])
+    return out.cpu() if out.is_cuda else out
 
 
 class _Inputs:
@@ -385,7 +390,11 @@ def _matrices(gates, closed_form=False):
             if kind is not None and getattr(g, "matrix_pending", lambda: False)() and _rotation_angle(g) is not None:
                 by_kind.setdefault(kind, []).append(i)
         for kind, idx in by_kind.items():
-            th = torch.stack([gates[i].angle_values()[0].reshape(()).to(torch.float64).cpu() for i in idx])
+            vals = [gates[i].angle_values()[0].reshape(()).to(torch.float64) for i in idx]
+            try:
+                th = torch.stack(vals).cpu()  # one copy when the angles share a device
+            except RuntimeError:
+                th = torch.stack([v.cpu() for v in vals])
             gen = _GEN_T[kind]
             eye = torch.eye(gen.shape[0], dtype=torch.complex128)
             m = torch.cos(th)[:, None, None] * eye - 1j * torch.sin(th)[:, None, None] * gen
