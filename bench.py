@@ -125,35 +125,76 @@ def workload_gates(n=N_QUBITS, depth=DEPTH, seed=SEED):
     return workloads.brickwork_gates(n, depth, seed)
 
 
-def _mixed_sample(gates, n, count):
-    """Alternate SU(2) and SU(4) gates of the first depth unit (the circuit's 1:1 mix)."""
-    ones = [g for g in gates[:2 * n] if len(g.indices) == 1]
-    twos = [g for g in gates[:2 * n] if len(g.indices) == 2]
-    out = []
-    for a, b in zip(ones, twos):
-        out += [a, b]
-    return out[:count]
+def depth_unit(gates, n):
+    """The circuit's first depth unit: SU(2) on every site, then SU(4) on the even
+    and odd nearest-neighbour pairs (n + n - 1 gates, 55 at 28 qubits). Every
+    depth unit of the brickwork has this shape, so its time extrapolates to the
+    whole circuit by the gate count."""
+    return gates[:2 * n - 1]
 
 
-def cpu_baseline(gates, n, budget_s=12.0, min_gates=2, max_gates=8):
-    """Reference algorithm (oracle op_action, complex128) on a bounded sample of the circuit's gates."""
+def _cpu_threads():
     import torch
-    from oracle import ref
     threads = os.cpu_count() or 1
     torch.set_num_threads(threads)
-    state = ref.initial_sv(n)
-    sample = _mixed_sample(gates, n, max_gates)
-    done, t0 = 0, time.perf_counter()
-    for g in sample:
-        state = ref.op_action(g.matrix, g.indices, state)
-        done += 1
-        if done >= min_gates and time.perf_counter() - t0 > budget_s:
-            break
+    return threads
+
+
+def cpu_depth_unit_c64(gates, n, reps=1):
+    """The reference's torch backend on the host cores (complex64; op_action =
+    permute + tensordot on torch CPU tensors, restated in oracle/): seconds per
+    gate over `reps` passes of the circuit's first depth unit."""
+    import torch
+    from oracle import ref
+    unit = depth_unit(gates, n)
+    mats = [torch.tensor(np.asarray(g.matrix), dtype=torch.complex64) for g in unit]
+    state = torch.zeros([2] * n, dtype=torch.complex64)
+    state.view(-1)[0] = 1
+    state = ref.op_action_torch(mats[0], unit[0].indices, state)  # warm-up (allocator, BLAS threads)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        for m, g in zip(mats, unit):
+            state = ref.op_action_torch(m, g.indices, state)
     dt = time.perf_counter() - t0
     del state
-    return {"value": done / dt, "unit": "gates/s", "cores": threads, "kind": "port",
-            "sample": f"{done} gates alternating SU(2)/SU(4) from the first depth unit of the {n}-qubit circuit, "
-                      f"complex128 tensordot+transpose (reference op_action via oracle/), {dt:.1f} s"}
+    return dt / (reps * len(unit)), len(unit)
+
+
+def cpu_baseline(gates, n, numpy_gates=4):
+    """The reference's CPU path on the host cores, all threads: one full depth unit
+    (55 gates at 28 qubits) through its torch backend in complex64 -- the
+    benchmark's own dtype -- extrapolated to the circuit by the gate count;
+    beside it the numpy complex128 path on a few gates of that unit, and the
+    12-qubit depth-20 complex128 circuit run whole (median of 5)."""
+    from oracle import ref
+    threads = _cpu_threads()
+    s_per_gate, ngates = cpu_depth_unit_c64(gates, n)
+    out = {"value": round(1.0 / s_per_gate, 4), "unit": "gates/s", "cores": threads, "kind": "port",
+           "sample": f"one full depth unit ({ngates} gates: {n} SU(2) + {n - 1} SU(4)) of the {n}-qubit brickwork, "
+                     f"complex64, the reference torch backend's op_action (permute + tensordot on CPU tensors, "
+                     f"restated in oracle/), {ngates * s_per_gate:.1f} s; the {len(gates)}-gate circuit "
+                     f"extrapolates to {len(gates) * s_per_gate:.0f} s"}
+    # numpy complex128 (the reference's default backend) on the first gates of the same unit
+    unit = depth_unit(gates, n)
+    state = ref.initial_sv(n)
+    t0 = time.perf_counter()
+    for g in unit[:numpy_gates]:
+        state = ref.op_action(g.matrix, g.indices, state)
+    dt = time.perf_counter() - t0
+    del state
+    out["numpy_c128"] = {"gates_per_s": round(numpy_gates / dt, 4),
+                         "sample": f"first {numpy_gates} gates of the same depth unit, numpy complex128"}
+    # configuration 1: 12 qubits, depth 20, complex128, the whole circuit (median of 5 runs)
+    from qaravan_gb300 import workloads
+    g12 = workloads.brickwork_gates(12, 20, 12)
+    times = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        ref.run_sv(g12, 12)
+        times.append(time.perf_counter() - t0)
+    out["config1_12q_depth20_c128"] = {"gates": len(g12), "median_s": round(statistics.median(times), 5),
+                                       "gates_per_s": round(len(g12) / statistics.median(times), 1)}
+    return out
 
 
 def _event_ms(fn, warmup=1, steps=1):
@@ -216,6 +257,69 @@ def section_variants(n, gates):
     return out
 
 
+def _torch_backend_apply(m, idx, s):
+    """The reference torch backend's op_action (tensorQ/statevector_sim.py:124-140:
+    the operator's input legs contracted with the state's legs `idx` by one
+    tensordot, the output legs moved back into place), restated on torch
+    tensors of the state's device."""
+    import torch
+    n, k = s.ndim, len(idx)
+    t = torch.tensordot(m.reshape([2] * 2 * k), s, dims=(list(range(k, 2 * k)), list(idx)))
+    order = list(idx) + [a for a in range(n) if a not in idx]
+    return t.permute(*[order.index(a) for a in range(n)])
+
+
+def section_torch_backend_gpu(gates, n):
+    """The reference's torch backend on this GPU (StatevectorSim(backend="torch",
+    device="cuda"): per gate a complex64 cast and copy of the matrix to the
+    device and one permute + tensordot, tensorQ/statevector_sim.py:19-29,50-52,
+    124-140), restated here: the circuit's first depth unit at 28 qubits, and
+    one brick layer (25 SU(4) gates) at 26 qubits, the reference's own GPU
+    benchmark (examples/gpu_acceleration.ipynb, 4.5 s on a T4)."""
+    import torch
+    out = {}
+    for name, nq, gl in (("depth_unit_28q", n, depth_unit(gates, n)),
+                         ("brick_layer_26q", 26, [g for g in workload_gates(26, 1)[26:] if len(g.indices) == 2])):
+        host = [np.asarray(g.matrix, dtype=np.complex128) for g in gl]
+
+        def run():
+            st = torch.zeros([2] * nq, dtype=torch.complex64, device="cuda")
+            st.view(-1)[0] = 1
+            for m, g in zip(host, gl):
+                st = _torch_backend_apply(torch.tensor(m).to("cuda", torch.complex64), g.indices, st)
+            return st
+        ms = _event_ms(run, 1, 1)
+        out[name] = {"qubits": nq, "gates": len(gl), "ms": round(ms, 2),
+                     "gates_per_s": round(len(gl) / (ms / 1e3), 1)}
+        torch.cuda.empty_cache()
+    return out
+
+
+def section_config1(seed=12):
+    """The 12-qubit depth-20 brickwork (460 gates) on the GPU through
+    StatevectorSim, complex128 (its parity configuration) and complex64,
+    each a whole run (compile cached, state initialisation included)."""
+    import torch
+    from qaravan_gb300 import StatevectorSim, workloads
+    from qaravan_gb300.circuits import Circuit
+    gl = workloads.brickwork_gates(12, 20, seed)
+    out = {"gates": len(gl)}
+    for name, dtype in (("c128", torch.complex128), ("c64", torch.complex64)):
+        circ = Circuit(gl, n=12)
+        ex = StatevectorSim(circ, dtype=dtype).compile()
+        st = torch.empty(2 ** 12, dtype=dtype, device="cuda")
+        from qaravan_gb300 import _lib
+        code = _lib.dtype_code(dtype)
+
+        def step():
+            _lib.check(_lib.lib().qgb_init_basis(st.data_ptr(), code, 12, 0, 1, 0, _lib.stream_ptr()), "init")
+            ex.run(st)
+        ms = _event_ms(step, 3, 20)
+        out[name] = {"ms": round(ms, 4), "gates_per_s": round(len(gl) / (ms / 1e3), 1),
+                     "hbm_passes": ex.plan.n_sweeps}
+    return out
+
+
 def _torch_reference_energy(n, layers, params, terms, device):
     """The reference's torch-backend path on this GPU, for the autograd comparison:
     gate matrices by torch.linalg.matrix_exp (core/param_gates.py:51-80), cast to
@@ -230,14 +334,7 @@ def _torch_reference_energy(n, layers, params, terms, device):
     st = torch.zeros([2] * n, dtype=torch.complex64, device=device)
     st.view(-1)[0] = 1
 
-    def apply(m, idx, s):
-        k = len(idx)
-        t = torch.tensordot(m.reshape([2] * 2 * k), s, dims=(list(range(k, 2 * k)), list(idx)))
-        rest = [a for a in range(n) if a not in idx]
-        order = list(idx) + rest
-        inv = [order.index(a) for a in range(n)]
-        return t.permute(*inv)
-
+    apply = _torch_backend_apply
     for l in range(layers):
         for q in range(n):
             st = apply(torch.linalg.matrix_exp(-1j * th[l, q, 0] * Y).to(device, torch.complex64), [q], st)
@@ -460,6 +557,28 @@ def section_dm_batch(count=256, seed=7):
            "state_gb": round(sum(4 ** n * 8 for n, _, _ in specs) / 1e9, 1),
            "large_passes": passes, "large_algorithmic_tb": round(alg / 1e12, 2),
            "hbm_frac": round(alg / (ms / 1e3) / 1e9 / peak, 3), "hbm_frac_of": f"hbm_gbs of {peak_kind}"}
+    # accuracy against the same circuits in complex128 (CUDA-core sweeps, pinned to the
+    # oracle at 1e-12): ten circuits of up to 10 qubits, two of 12 and one of 13
+    pick, want = [], {10: 10, 12: 2, 13: 1}
+    for i, (n, d, sd) in enumerate(specs):
+        key = 10 if n <= 10 else n
+        if want.get(key, 0) > 0:
+            pick.append(i)
+            want[key] -= 1
+    perr, zerr, rerr = 0.0, 0.0, 0.0
+    for i in pick:
+        n, d, sd = specs[i]
+        s128 = DensityMatrixSim(workloads.noisy_brickwork_circuit(n, d, sd, p=1e-3), dtype=torch.complex128)
+        s128.run()
+        z = s128.pauli_expectations([(1.0, 'i' * q + 'z' + 'i' * (n - q - 1)) for q in range(n)]).cpu().numpy()
+        perr = max(perr, abs(res[i]["purity"] - s128.purity()))
+        zerr = max(zerr, float(np.abs(res[i]["z"] - z).max()))
+        rho = batch.density_matrix(i).to(torch.complex128)
+        rerr = max(rerr, float((rho - s128.get_density_matrix()).abs().max().item()))
+        del s128, rho
+        torch.cuda.empty_cache()
+    out["vs_complex128"] = {"circuits": [specs[i][:2] for i in pick], "max_purity_error": perr,
+                            "max_z_error": zerr, "max_abs_entry_error": rerr}
     del batch, sims
     torch.cuda.empty_cache()
     return out
@@ -595,7 +714,23 @@ def gpu_arm(args):
         e2e = {"value": round(world * gates_per_step * args.e2e_steps / dt, 2), "unit": "gates/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 8,
                "note": "StatevectorSim(host circuit).run() incl. compile + pinned H2D of fused matrices, "
-                       "then pauli_expectation('zi...i').item()", "check_value": r}
+                       "then pauli_expectation('zi...i').item(); the fusion plan of the circuit's structure "
+                       "is cached after the first run (cold_compile: the first run of a new structure)",
+               "check_value": r}
+        # the same call with every plan and table cache emptied: a circuit structure seen for the first time
+        from qaravan_gb300 import compiler, engine
+        compiler._PLAN_CACHE.clear()
+        engine._LAYOUT_CACHE.clear()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s2 = StatevectorSim(Circuit(gates, n=n), dtype=dtype, mode=args.mode, fusion_width=args.width,
+                            tile_bits=args.tile, low_bits=args.low)
+        s2.run()
+        s2.pauli_expectation("z" + "i" * (n - 1))
+        torch.cuda.synchronize()
+        cold = time.perf_counter() - t0
+        del s2
+        e2e["cold_compile"] = {"s": round(cold, 4), "gates_per_s": round(gates_per_step / cold, 2)}
 
     if rank != 0:
         return
@@ -616,9 +751,12 @@ def gpu_arm(args):
     del state, ex, sim
     torch.cuda.empty_cache()
     sections = {}
-    wanted = args.sections.split(",") if args.sections != "all" else ["variants", "adjoint", "adjoint_batch",
-                                                                       "trajectories", "dm_batch"]
-    for name, fn in [("variants", lambda: section_variants(n, gates)), ("adjoint", section_adjoint),
+    all_sections = ["variants", "torch_backend_gpu", "config1", "adjoint", "adjoint_batch", "trajectories",
+                    "dm_batch"]
+    wanted = args.sections.split(",") if args.sections != "all" else all_sections
+    for name, fn in [("variants", lambda: section_variants(n, gates)),
+                     ("torch_backend_gpu", lambda: section_torch_backend_gpu(gates, n)),
+                     ("config1", section_config1), ("adjoint", section_adjoint),
                      ("adjoint_batch", section_adjoint_batch),
                      ("trajectories", section_trajectories), ("dm_batch", section_dm_batch)]:
         if name in wanted:
@@ -627,18 +765,16 @@ def gpu_arm(args):
             except Exception as e:  # secondary sections never suppress the headline line
                 sections[name] = {"error": f"{type(e).__name__}: {str(e)[:300]}"}
             torch.cuda.empty_cache()
-    cpu = None if args.no_cpu else cpu_baseline(gates, n, budget_s=args.cpu_budget)
+    cpu = None if args.no_cpu else cpu_baseline(gates, n)
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": "gates/s", "n_gates": gates_per_step,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "c64" if dtype == torch.complex64 else "c128", "data": "synthetic (seeded Haar brickwork)",
-        "config": {"workload": f"{n}-qubit open-chain Haar brickwork, depth {args.depth} "
-                               f"({gates_per_step} gates), {'complex64' if dtype == torch.complex64 else 'complex128'}",
-                   "qubits": n, "depth": args.depth, "seed": SEED, "mode": args.mode, "fusion_width": args.width,
-                   "tile_bits": args.tile, "hbm_passes_per_step": passes, "flops_per_amp_per_step": flops_per_amp,
-                   "l2": "state (2^n x itemsize) larger than L2; no flush needed",
-                   "parallelism": f"replicas x{world}"},
+        "config": workload_config(n, args.depth, "complex64" if dtype == torch.complex64 else "complex128"),
+        "execution": {"mode": args.mode, "fusion_width": args.width, "tile_bits": args.tile,
+                      "hbm_passes_per_step": passes, "flops_per_amp_per_step": flops_per_amp,
+                      "parallelism": f"replicas x{world}"},
         "hbm_gbs_effective": round(passes * alg_bytes / (ms_step / 1e3) / 1e9, 1),
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks.summary(),
         "gpu_launches": launches, "accuracy": accuracy, "sections": sections,
@@ -646,41 +782,107 @@ def gpu_arm(args):
     print(json.dumps(out), flush=True)
 
 
+def workload_config(n, depth, dtype_name):
+    """The benchmark configuration, identical in both arms."""
+    return {"workload": f"{n}-qubit open-chain Haar brickwork, depth {depth} "
+                        f"({depth * (2 * n - 1)} gates), {dtype_name}",
+            "qubits": n, "depth": depth, "seed": SEED, "dtype": dtype_name,
+            "l2": "state (2^n x itemsize) larger than L2; no flush needed"}
+
+
 def reference_arm(args):
-    """The reference's CPU algorithm (complex128 op_action via tensordot), all host threads."""
+    """The reference's CPU path (its torch backend's op_action on the host cores,
+    complex64, all threads) on the benchmark's circuit: each step applies the
+    next ceil(55 / steps) gates of the circuit's first depth unit, so the timed
+    steps together cover the whole 55-gate unit (every depth unit has its shape)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    import torch
+    from oracle import ref
     n = args.qubits
     gates = workload_gates(n, args.depth)
-    from oracle import ref
-    import torch
-    threads = os.cpu_count() or 1
-    torch.set_num_threads(threads)
-    sample = _mixed_sample(gates, n, args.ref_gates)
-    state = ref.initial_sv(n)
-    for g in sample[:1] * args.warmup:
-        state = ref.op_action(g.matrix, g.indices, state)
-    times = []
+    threads = _cpu_threads()
+    unit = depth_unit(gates, n)
+    mats = [torch.tensor(np.asarray(g.matrix), dtype=torch.complex64) for g in unit]
+    per_step = -(-len(unit) // max(args.steps, 1))
+    state = torch.zeros([2] * n, dtype=torch.complex64)
+    state.view(-1)[0] = 1
+    for i in range(args.warmup):
+        state = ref.op_action_torch(mats[i % len(unit)], unit[i % len(unit)].indices, state)
+    times, applied, pos = [], 0, 0
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        for g in sample:
-            state = ref.op_action(g.matrix, g.indices, state)
+        for _ in range(per_step):
+            state = ref.op_action_torch(mats[pos], unit[pos].indices, state)
+            pos = (pos + 1) % len(unit)
         times.append(time.perf_counter() - t0)
+        applied += per_step
     total = sum(times)
-    value = args.steps * len(sample) / total
+    value = applied / total
     cpu = {"value": round(value, 4), "unit": "gates/s", "cores": threads, "kind": "port",
-           "sample": f"{len(sample)} gates (alternating SU(2), SU(4)) of the {n}-qubit brickwork per step, complex128, "
-                     f"reference op_action restated in oracle/"}
+           "sample": f"{applied} gates ({per_step} per step) of the first depth unit ({len(unit)} gates: {n} SU(2) + "
+                     f"{n - 1} SU(4)) of the {n}-qubit brickwork, complex64, the reference torch backend's op_action "
+                     f"(permute + tensordot on CPU tensors, restated in oracle/); the {len(gates)}-gate circuit "
+                     f"extrapolates to {len(gates) / value:.0f} s"}
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "gates/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 1),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
-        "data": "synthetic (seeded Haar brickwork)",
-        "config": {"workload": f"{n}-qubit open-chain Haar brickwork, depth {args.depth}", "qubits": n,
-                   "depth": args.depth, "seed": SEED},
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+        "data": "synthetic (seeded Haar brickwork)", "config": workload_config(n, args.depth, "complex64"),
         "cpu_baseline": cpu, "e2e": {"value": round(value, 4), "unit": "gates/s", "h2d_bytes_per_step": 0,
                                      "d2h_bytes_per_step": 0}}), flush=True)
+
+
+def run_case(args):
+    """Small committed workloads for profiler captures (one run each, no CUDA
+    graph, so that a profiler sees every launch):
+      adjoint_batch [qubits layers sets]: one batched energy-and-gradient
+        evaluation of the hardware-efficient ansatz (default 18 4 64);
+      trajectory_gates [qubits trajectories steps]: the noisy TFI trajectories
+        gate by gate with CUDA events around every gate (default 20 1024 2);
+      dm_batch [circuits seed]: the uneven noisy density-matrix batch (default 32 7)."""
+    import torch
+    from qaravan_gb300 import build as qbuild
+    qbuild.build()
+    from qaravan_gb300 import workloads
+    vals = [int(v) for v in args.case_args.split(",") if v.strip()] if args.case_args else []
+    if args.case == "adjoint_batch":
+        from qaravan_gb300.adjoint import BatchedAnsatz
+        from qaravan_gb300.hamiltonians import TFI
+        n, layers, sets = (vals + [18, 4, 64][len(vals):])[:3]
+        ba = BatchedAnsatz.hea(n, layers)
+        x = torch.tensor(np.stack([workloads.hea_params(n, layers, s).reshape(-1) for s in range(sets)]),
+                         device="cuda")
+        E, _ = ba.energy_and_grad(x, TFI(n, 1, 1).pauli_sum())
+        torch.cuda.synchronize()
+        print("energy[0]", float(E[0]), "reverse passes", len(ba._rev), "ops per pass", [s.n_ops for s in ba._rev])
+    elif args.case == "trajectory_gates":
+        from qaravan_gb300.trajectories import TrajectorySim
+        n, T, steps = (vals + [20, 1024, 2][len(vals):])[:3]
+        sim = TrajectorySim(workloads.tfi_trotter_circuit(n, 0.05, steps), T, p_dep=1e-3, gamma=5e-4, seed=2026,
+                            mode="per_gate")
+        sim.run()
+        rows = sim.time_gates()
+        alg = 2 * T * 2 ** n * 8
+        total = sum(ms for *_, ms in rows)
+        print(f"{n} qubits, {T} trajectories, {len(rows)} gates: {total / len(rows):.3f} ms/gate, "
+              f"{alg / 1e9:.2f} GB algorithmic per gate")
+    elif args.case == "dm_batch":
+        from qaravan_gb300 import DensityMatrixSim
+        from qaravan_gb300.batch import DensityMatrixBatch
+        count, seed = (vals + [32, 7][len(vals):])[:2]
+        specs = workloads.uneven_dm_specs(count, seed)
+        sims = [DensityMatrixSim(workloads.noisy_brickwork_circuit(n, d, s, p=1e-3), dtype=torch.complex64)
+                for n, d, s in specs]
+        batch = DensityMatrixBatch(sims, dtype=torch.complex64)
+        batch.run()
+        torch.cuda.synchronize()
+        res = batch.results()
+        print(f"{count} circuits: {len(batch.small)} in the batched launch, {len(batch.large)} stream-parallel; "
+              f"max trace error {max(abs(r['trace'] - 1) for r in res):.2e}")
+    else:
+        raise SystemExit(f"unknown case {args.case!r}")
 
 
 def main():
@@ -700,12 +902,15 @@ def main():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-accuracy", action="store_true", help="skip the complex128 comparison of the final state")
-    p.add_argument("--cpu-budget", type=float, default=12.0)
-    p.add_argument("--ref-gates", type=int, default=2)
     p.add_argument("--sections", default="all",
-                   help="comma list of variants,adjoint,adjoint_batch,trajectories,dm_batch; 'none' for the headline only")
+                   help="comma list of variants,torch_backend_gpu,config1,adjoint,adjoint_batch,trajectories,"
+                        "dm_batch; 'none' for the headline only")
+    p.add_argument("--case", default=None, help="run one profiling workload instead (see run_case)")
+    p.add_argument("--case-args", default="", help="comma-separated integers for --case")
     args = p.parse_args()
-    if args.impl == "reference":
+    if args.case:
+        run_case(args)
+    elif args.impl == "reference":
         reference_arm(args)
     else:
         gpu_arm(args)

@@ -90,6 +90,15 @@ const char* qgb_last_error(void);
 /* Reads and clears the device status word set by bounded waits; returns
  * QGB_OK or QGB_ETIMEOUT. Synchronises `stream`. */
 int qgb_check_status(void* stream);
+/* Health check of the failure path (no counterpart in the reference, which
+ * has no device code): one warp runs the library's bounded wait -- the helper
+ * every kernel uses for its mbarrier and flag waits -- on a wait that cannot
+ * finish, with limit_ns (at most 10 s): mode 0 an mbarrier that nobody
+ * arrives on, mode 1 the device int at `flag` reaching 1 (nothing sets it),
+ * mode 2 an mbarrier whose arrival comes first (completes). A wait that gives
+ * up records its code in the status word, so the next qgb_check_status
+ * returns QGB_ETIMEOUT, and the kernel returns; the context stays usable. */
+int qgb_wait_probe(int mode, unsigned long long limit_ns, const int* flag, void* stream);
 
 /* ---- statevector ------------------------------------------------------ */
 
@@ -126,6 +135,30 @@ int qgb_op_action_unitary(void* sv, int dtype, int n, const int* indices, int k,
 int qgb_op_action_unitary_chain(void* sv, int dtype, int n, const int* indices, int k, const void* op,
                                 int64_t op_stride, int64_t batch, int64_t sv_stride, double* chain, int link,
                                 void* stream);
+
+/* qgb_op_action for one vector (batch 1) with the operator multiplied by the
+ * float64 factor *factor, read on the device when the pass runs (so that a
+ * factor computed by an earlier kernel on the stream can scale it without a
+ * host round trip). On the tensor-core path the factor is folded into the
+ * matrix; elsewhere a second pass multiplies the result. With
+ * qgb_dm_trace_factor it forms the trace chain of complex64 density matrices
+ * (a CPTP map keeps Tr rho; the tensor cores' round-toward-zero accumulation
+ * shrinks it by ~1e-7 per pass). Replaces, like qgb_op_action, the
+ * reference's per-op superoperator application DensityMatrixSim.apply_gate
+ * (tensorQ/density_matrix_sim.py:38-42), which needs no such control. */
+int qgb_op_action_scaled(void* sv, int dtype, int n, const int* indices, int k, const void* op,
+                         const double* factor, void* stream);
+
+/* Trace of one density matrix of n sites (vec(rho), 4^n entries), summed in
+ * float64 in a fixed order by one CTA, into `chain` (3 doubles of device
+ * memory): start != 0 sets chain[0] = Tr rho (the chain's reference) and
+ * chain[1] = 1; otherwise chain[1] = chain[0] / Tr rho, the factor that the
+ * next qgb_op_action_scaled applies. chain[2] = the trace measured. Callers
+ * measure only where the ops applied so far form whole channels (both halves
+ * of every unitary), where the trace equals the reference in exact
+ * arithmetic. Counterpart of DensityMatrixSim.normalize_state's trace
+ * (tensorQ/density_matrix_sim.py:85-89), without the division. */
+int qgb_dm_trace_factor(const void* rho, int dtype, int n, double* chain, int start, void* stream);
 
 /* A fused pass (several gates per read+write of the state), planned by the
  * host compiler from a Circuit's gate list (core/base_sim.py:30-53 loop). */
@@ -175,14 +208,17 @@ int qgb_pauli_expectation(const void* sv, int dtype, int n, const char* paulis, 
  * application owns all device memory through its own pool and forbids
  * cudaMalloc/cudaFree beside it, GPUs whose memory is already fully reserved
  * so that even a small allocation would fail. Instead of a caller buffer it
- * uses one fixed 1 MiB device array inside the library (held on every device
- * the library is used on until the process exits), so it accepts at most 64
- * terms and at most 131072 / blocks(n) terms in total (blocks(n) =
- * min(1216, max(1, 2^n / 4096))), and returns QGB_EINVAL beyond that. The
- * first call on a device looks up the array's address (cudaGetSymbolAddress,
- * that device current) -- make it before any stream capture. Calls share the
- * array: calls that overlap on the GPU race. Results equal
- * qgb_pauli_expectation's (out: nterms float64, device). */
+ * uses one fixed 1 MiB device array inside the library, so it accepts at most
+ * 64 terms and returns QGB_EINVAL beyond that. CUDA loads the library's device
+ * code lazily: the array is reserved on a device when the first call there
+ * (or the first call of any other reduction entry point) loads that code, and
+ * held until the process exits -- make one warm-up call before reserving the
+ * rest of the device's memory and before any stream capture, or set
+ * CUDA_MODULE_LOADING=EAGER. Every call looks the array's address up again
+ * (cudaGetSymbolAddress, the caller's device current), so it stays right
+ * after a cudaDeviceReset. Calls share the array: calls that overlap on the
+ * GPU race. Results equal qgb_pauli_expectation's (out: nterms float64,
+ * device). */
 int qgb_pauli_expectation_noalloc(const void* sv, int dtype, int n, const char* paulis, const double* coeff,
                                   int nterms, double* out, void* stream);
 

@@ -62,9 +62,12 @@ SIGNATURES = {
     "qgb_abi_version": (C.c_int, []),
     "qgb_last_error": (C.c_char_p, []),
     "qgb_check_status": (C.c_int, [_vp]),
+    "qgb_wait_probe": (C.c_int, [_i, C.c_ulonglong, _vp, _vp]),
     "qgb_op_action": (C.c_int, [_vp, _i, _i, _ip, _i, _vp, _i64, _i64, _i64, _vp]),
     "qgb_op_action_unitary": (C.c_int, [_vp, _i, _i, _ip, _i, _vp, _i64, _i64, _i64, _vp]),
     "qgb_op_action_unitary_chain": (C.c_int, [_vp, _i, _i, _ip, _i, _vp, _i64, _i64, _i64, _vp, _i, _vp]),
+    "qgb_op_action_scaled": (C.c_int, [_vp, _i, _i, _ip, _i, _vp, _vp, _vp]),
+    "qgb_dm_trace_factor": (C.c_int, [_vp, _i, _i, _vp, _i, _vp]),
     "qgb_apply_sweep": (C.c_int, [_vp, _i, _i, C.POINTER(Sweep), _vp, _i64, _i64, _i64, _vp]),
     "qgb_set_sweep_impl": (C.c_int, [_i]),
     "qgb_init_basis": (C.c_int, [_vp, _i, _i, _u64, _i64, _i64, _vp]),

@@ -585,25 +585,3 @@ class BatchedAnsatz:
         _lib.check(L.qgb_param_grads(self._csr_ptr.data_ptr(), self._csr_gate.data_ptr(), self.nparams, P,
                                      gvals.data_ptr(), 2.0, grad.data_ptr(), st), "param_grads")
         return E, grad
-
-
-def _main(argv=None):
-    """``python -m qaravan_gb300.adjoint [qubits] [layers] [parameter sets]``: one
-    batched energy-and-gradient evaluation of the hardware-efficient ansatz
-    (complex64) on the TFI energy, for seeded parameter sets
-    (``workloads.hea_params`` with seeds 0, 1, ...); prints the first energy and
-    the reverse tile passes' op counts."""
-    import sys
-    from . import workloads
-    from .hamiltonians import TFI
-    args = [int(a) for a in (sys.argv[1:] if argv is None else argv)]
-    n, layers, sets = (args + [18, 4, 64][len(args):])[:3]
-    ba = BatchedAnsatz.hea(n, layers)
-    x = torch.tensor(np.stack([workloads.hea_params(n, layers, s).reshape(-1) for s in range(sets)]), device="cuda")
-    E, _ = ba.energy_and_grad(x, TFI(n, 1, 1).pauli_sum())
-    torch.cuda.synchronize()
-    print("energy[0]", float(E[0]), "reverse passes", len(ba._rev), "ops per pass", [s.n_ops for s in ba._rev])
-
-
-if __name__ == "__main__":
-    _main()

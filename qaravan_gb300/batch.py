@@ -197,29 +197,3 @@ class DensityMatrixBatch:
             if item[0] == i:
                 return item[3].reshape(d, d)
         raise KeyError(i)
-
-
-def _main(argv=None):
-    """``python -m qaravan_gb300.batch [circuits] [seed]``: the uneven noisy
-    density-matrix workload (6-14 qubits, depth 10-40, depolarising 1e-3 after
-    each two-qubit gate; ``workloads.uneven_dm_specs``), run once without a CUDA
-    graph so that a profiler sees every launch; prints the split between the
-    batched launch and the stream-parallel circuits and the largest trace error."""
-    import sys
-    from . import workloads
-    from .density_matrix import DensityMatrixSim
-    args = [int(a) for a in (sys.argv[1:] if argv is None else argv)]
-    count, seed = (args + [32, 7][len(args):])[:2]
-    specs = workloads.uneven_dm_specs(count, seed)
-    sims = [DensityMatrixSim(workloads.noisy_brickwork_circuit(n, d, s, p=1e-3), dtype=torch.complex64)
-            for n, d, s in specs]
-    batch = DensityMatrixBatch(sims, dtype=torch.complex64)
-    batch.run()
-    torch.cuda.synchronize()
-    res = batch.results()
-    print(f"{count} circuits: {len(batch.small)} in the batched launch, {len(batch.large)} stream-parallel; "
-          f"max trace error {max(abs(r['trace'] - 1) for r in res):.2e}")
-
-
-if __name__ == "__main__":
-    _main()

@@ -41,6 +41,7 @@ class Op:
     matrix: np.ndarray  # complex128, 2^k x 2^k
     kind: str = "unitary"  # "unitary" | "nonunitary" | "channel" | "pauli_mix"
     terms: list = None  # "pauli_mix": [(coeff, Pauli string over the vector's bits, char j <-> bit nbits-1-j)]
+    pair: int = None  # density matrices: id shared by the ket and bra halves of one gate (None otherwise)
 
 
 @dataclass
@@ -48,6 +49,7 @@ class DenseStep:
     bits: list
     mat: int  # index into the plan's matrix list
     unitary: bool = False  # the block is unitary (every op in it is): its launch may restore group norms
+    whole: bool = False  # density matrices: the ops applied up to this step form whole channels (no half gate)
 
 
 @dataclass
@@ -85,6 +87,7 @@ class Plan:
     matrices: list = field(default_factory=list)  # complex128 arrays (host-composed), or Recipe objects
     n_gates: int = 0  # original op count
     op_matrices: list = field(default_factory=list)  # raw op matrices the recipes refer to
+    trace_kept: bool = False  # density matrices: every op keeps the trace, or a renormalisation follows it
 
     def add_matrix(self, m):
         if isinstance(m, Recipe):
@@ -316,6 +319,58 @@ def unitary_flags(ops, tol=1e-6):
     return flags
 
 
+def trace_preserving(op):
+    """Whether an op on vec(rho) keeps Tr rho for every rho: a half of a unitary
+    gate (unitary on its bits; the other half is its conjugate) or a channel
+    superoperator on 2k bits (bra bits first) whose rows with equal bra and ket
+    index sum to the trace functional."""
+    m = np.asarray(op.matrix, dtype=np.complex128)
+    if op.pair is not None:
+        return unitary_flags([op])[0]
+    if op.kind != "channel":
+        return False
+    k2 = len(op.bits)
+    k = k2 // 2
+    d = 2 ** k
+    diag = [(a << k) | a for a in range(d)]
+    t = m[diag, :].sum(axis=0)
+    want = np.zeros(4 ** k, dtype=np.complex128)
+    want[diag] = 1.0
+    return bool(np.abs(t - want).max() < 1e-9)
+
+
+def whole_cuts(seg, groups):
+    """For each group of segment op indices (in application order): whether the
+    ops applied up to and including it leave no gate with only one of its
+    halves (ket or bra) applied. At such a cut the ops applied so far are whole
+    channels, which keep the trace."""
+    open_pairs: set = set()
+    out = []
+    for g in groups:
+        for i in g:
+            p = seg[i].pair
+            if p is not None:
+                open_pairs ^= {p}
+        out.append(not open_pairs)
+    return out
+
+
+def _pair_offsets(ops):
+    """Offset from each op to the other half of its pair (0 when unpaired): the
+    pairing structure, independent of the ids."""
+    first: dict = {}
+    out = [0] * len(ops)
+    for i, o in enumerate(ops):
+        if o is None or o.pair is None:
+            continue
+        if o.pair in first:
+            j = first.pop(o.pair)
+            out[i], out[j] = j - i, i - j
+        else:
+            first[o.pair] = i
+    return out
+
+
 # Plans whose block matrices are all device-composed (Recipe) depend on the op
 # matrices only through the unitarity flags: such a plan is kept per structure
 # (op bits, flags, options) and reused with new op matrices, so a circuit run
@@ -330,7 +385,8 @@ def _cached_plan(key, ops):
     if tpl is None:
         return None
     _PLAN_CACHE[key] = tpl  # most recently used last
-    plan = Plan(nbits=tpl.nbits, steps=tpl.steps, matrices=tpl.matrices, n_gates=tpl.n_gates)
+    plan = Plan(nbits=tpl.nbits, steps=tpl.steps, matrices=tpl.matrices, n_gates=tpl.n_gates,
+                trace_kept=tpl.trace_kept)
     plan.op_matrices = [np.ascontiguousarray(o.matrix, dtype=np.complex128) for o in ops if o is not None]
     return plan
 
@@ -354,15 +410,33 @@ def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, 
     :class:`Recipe` objects for the executor to compose on the GPU.
     """
     tile_bits = min(tile_bits, 14 if itemsize <= 8 else 13)
+    # density matrices: does every op keep the trace, or is it followed by a renormalisation?
+    dm = any(o is not None and (o.pair is not None or o.kind == "channel") for o in ops)
+    trace_kept = False
+    tp_flags = ()
+    if dm:
+        trace_kept = True
+        pending_loss = False
+        tp_list = []
+        for o in ops:
+            if o is None:
+                pending_loss = False
+                continue
+            tp = o.kind == "pauli_mix" or trace_preserving(o)
+            tp_list.append(tp)
+            pending_loss |= not tp
+        trace_kept = not pending_loss
+        tp_flags = tuple(tp_list)
     key = None
     if device_fusion and mode != "gate" and ops and not any(o is not None and o.kind == "pauli_mix" for o in ops):
         flags = unitary_flags([o for o in ops if o is not None])
         key = (nbits, mode, width, tile_bits, low_bits, max_sweep_k, itemsize,
-               tuple(None if o is None else tuple(o.bits) for o in ops), tuple(flags))
+               tuple(None if o is None else tuple(o.bits) for o in ops), tuple(flags), tuple(_pair_offsets(ops)),
+               tp_flags)
         plan = _cached_plan(key, ops)
         if plan is not None:
             return plan
-    plan = Plan(nbits=nbits, n_gates=sum(1 for o in ops if o is not None))
+    plan = Plan(nbits=nbits, n_gates=sum(1 for o in ops if o is not None), trace_kept=trace_kept)
     segments, cur = [], []
     for o in ops:
         if o is None or o.kind == "pauli_mix":
@@ -383,8 +457,8 @@ def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, 
             continue
         uflags = unitary_flags(seg)
         if mode == "gate":
-            for o, u in zip(seg, uflags):
-                plan.steps.append(DenseStep(list(o.bits), plan.add_matrix(o.matrix), u))
+            for o, u, w_ in zip(seg, uflags, whole_cuts(seg, [[i] for i in range(len(seg))])):
+                plan.steps.append(DenseStep(list(o.bits), plan.add_matrix(o.matrix), u, w_))
             continue
         w = max(width, max(len(o.bits) for o in seg))
         if device_fusion:
@@ -394,13 +468,15 @@ def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, 
             blocks = [Block(b.bits, Recipe(list(b.bits), [(base + i, list(seg[i].bits)) for i in b.ops]), b.n_ops)
                       for b in sym]
             bflags = [all(uflags[i] for i in b.ops) for b in sym]
+            wflags = whole_cuts(seg, [b.ops for b in sym])
         else:
             blocks = fuse(seg, w)
             bflags = [bool(np.abs(b.matrix.conj().T @ b.matrix - np.eye(b.matrix.shape[0])).max() < 1e-6)
                       for b in blocks]
+            wflags = [all(o.pair is None for o in seg)] * len(blocks)  # membership unknown here
         if mode == "fused" or w > max_sweep_k or tile_bits <= 0:
-            for b, u in zip(blocks, bflags):
-                plan.steps.append(DenseStep(list(b.bits), plan.add_matrix(b.matrix), u))
+            for b, u, w_ in zip(blocks, bflags, wflags):
+                plan.steps.append(DenseStep(list(b.bits), plan.add_matrix(b.matrix), u, w_))
             continue
         for L, high, taken in plan_sweeps(blocks, nbits, tile_bits, low_bits):
             tpos = {b: b for b in range(L)}

@@ -235,7 +235,7 @@ namespace qgb_host {
 // j is out_bits[j] (same set of bits) to `batch` vectors of 2^nbits entries.
 int apply_dense_bits(void* sv, int dtype, int nbits, const int* in_bits, const int* out_bits, int k,
                      const void* op, int64_t op_stride, int64_t batch, int64_t sv_stride, cudaStream_t st,
-                     int unitary = 0, double* chain = nullptr, int link = 0) {
+                     int unitary = 0, double* chain = nullptr, int link = 0, const double* scale = nullptr) {
     if (!sv || !op) return set_error(QGB_EINVAL, "null state or operator pointer");
     if (dtype != QGB_C64 && dtype != QGB_C128) return set_error(QGB_EINVAL, "dtype %d unknown", dtype);
     if (k < 1 || k > QGB_MAX_K) return set_error(QGB_EINVAL, "gate width k=%d not in [1, %d]", k, QGB_MAX_K);
@@ -285,11 +285,14 @@ int apply_dense_bits(void* sv, int dtype, int nbits, const int* in_bits, const i
         unitary = 1;
     }
     if (dtype == QGB_C64) {
-        const int rc =
-            try_dense_tc(sv, op, nbits, a.sorted, in_bits, out_bits, k, op_stride, batch, sv_stride, unitary, st);
+        const int rc = try_dense_tc(sv, op, nbits, a.sorted, in_bits, out_bits, k, op_stride, batch, sv_stride,
+                                    unitary, st, nullptr, 0, scale);
         if (rc != QGB_EDECLINE) return rc;
     }
-    return dtype == QGB_C64 ? dispatch_dense<float>(sv, op, a, st) : dispatch_dense<double>(sv, op, a, st);
+    const int rc = dtype == QGB_C64 ? dispatch_dense<float>(sv, op, a, st) : dispatch_dense<double>(sv, op, a, st);
+    if (rc || !scale) return rc;
+    // the CUDA-core kernels take no factor: one more pass multiplies the result by it
+    return qgb_scale(sv, dtype, nbits, scale, 1, 0, st);
 }
 
 }  // namespace qgb_host
@@ -329,6 +332,21 @@ extern "C" int qgb_op_action_unitary_chain(void* sv, int dtype, int n, const int
         return set_error(QGB_EINVAL, "norm chain buffer missing or not 8-byte aligned");
     if (link < 0) return set_error(QGB_EINVAL, "negative chain link %d", link);
     return op_action(sv, dtype, n, indices, k, op, op_stride, batch, sv_stride, stream, 2, chain, link);
+}
+
+extern "C" int qgb_op_action_scaled(void* sv, int dtype, int n, const int* indices, int k, const void* op,
+                                    const double* factor, void* stream) {
+    if (!factor || (reinterpret_cast<uintptr_t>(factor) % sizeof(double)))
+        return set_error(QGB_EINVAL, "factor missing or not 8-byte aligned");
+    if (n < 1 || n > QGB_MAX_QUBITS) return set_error(QGB_EINVAL, "n=%d not in [1, %d]", n, QGB_MAX_QUBITS);
+    if (!indices) return set_error(QGB_EINVAL, "null indices");
+    if (k < 1 || k > QGB_MAX_K) return set_error(QGB_EINVAL, "gate width k=%d not in [1, %d]", k, QGB_MAX_K);
+    int bits[QGB_MAX_K];
+    for (int j = 0; j < k; ++j) {
+        if (indices[j] < 0 || indices[j] >= n) return set_error(QGB_EINVAL, "site %d out of range for n=%d", indices[j], n);
+        bits[j] = n - 1 - indices[j];
+    }
+    return apply_dense_bits(sv, dtype, n, bits, bits, k, op, 0, 1, 0, (cudaStream_t)stream, 0, nullptr, 0, factor);
 }
 
 extern "C" int qgb_dm_apply_superop(void* rho, int dtype, int n, const int* indices, int k, const void* superop,

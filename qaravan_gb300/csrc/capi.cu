@@ -8,6 +8,34 @@
 
 namespace qgb {
 __device__ int g_status = 0;
+
+// The library's bounded waits, made to run out on purpose: one warp waits on
+// a shared-memory mbarrier (mode 0: it expects one arrival that nobody makes;
+// mode 2: lane 0 arrives first, so the wait completes) or on a global flag
+// that nothing sets (mode 1), with the given limit; a wait that gives up
+// records its code in the status word (3: mbarrier, 4: flag) and the kernel
+// returns. Nothing else is touched and nothing stays in flight.
+__global__ void wait_probe_kernel(int mode, unsigned long long limit_ns, const int* flag) {
+    __shared__ __align__(8) uint64_t bar;
+    const uint32_t b = uint32_t(__cvta_generic_to_shared(&bar));
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncwarp();
+    if (mode == 1) {
+        if (threadIdx.x == 0 && !flag_wait_bounded(flag, 1, limit_ns)) atomicExch(&g_status, 4);
+        return;
+    }
+    if (mode == 2 && threadIdx.x == 0) {
+        uint64_t state;
+        asm volatile("mbarrier.arrive.shared::cta.b64 %0, [%1];" : "=l"(state) : "r"(b) : "memory");
+        (void)state;
+    }
+    __syncwarp();
+    const bool ok = mbar_wait_parity_bounded(b, 0, limit_ns);
+    if (!ok && threadIdx.x == 0) atomicExch(&g_status, 3);
+}
 }
 
 namespace {
@@ -48,6 +76,15 @@ int sm_count() {
 extern "C" int qgb_abi_version(void) { return QGB_ABI_VERSION; }
 
 extern "C" const char* qgb_last_error(void) { return g_last_error; }
+
+extern "C" int qgb_wait_probe(int mode, unsigned long long limit_ns, const int* flag, void* stream) {
+    if (mode < 0 || mode > 2) return qgb_host::set_error(QGB_EINVAL, "wait probe mode %d unknown (0, 1, 2)", mode);
+    if (mode == 1 && (!flag || (reinterpret_cast<uintptr_t>(flag) % sizeof(int))))
+        return qgb_host::set_error(QGB_EINVAL, "wait probe flag missing or misaligned");
+    if (limit_ns > 10000000000ull) return qgb_host::set_error(QGB_EINVAL, "wait probe limit above 10 s");
+    qgb::wait_probe_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(mode, limit_ns, flag);
+    return qgb_host::check_launch("wait probe");
+}
 
 extern "C" int qgb_check_status(void* stream) {
     cudaStream_t st = (cudaStream_t)stream;

@@ -84,6 +84,7 @@ struct TcArgs {
     uint64_t tiles;                      // tiles_per_state * batch
     int64_t sv_stride;
     double* chain;                       // norm chain (3 slots of {reference, output} squared norms) or null
+    const double* scale;                 // MODE 0: device factor f, the op applied is f * M (null: 1)
     int c_prev, c_cur, c_next;           // slots of the previous epoch, this epoch, the next epoch (-1: none)
     int c_head, c_tail;                  // this pass opens its epoch (corrects) / closes it (measures its output)
 };
@@ -113,24 +114,8 @@ template <int K> struct TcGeom {
 
 __device__ __forceinline__ uint32_t tc_smem_u32(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
 
-__device__ __forceinline__ unsigned long long tc_global_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
 __device__ __forceinline__ bool tc_wait_bounded(uint32_t bar, uint32_t parity) {
-    const unsigned long long t0 = tc_global_ns();
-    while (true) {
-        uint32_t done;
-        asm volatile(
-            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3; selp.u32 %0, 1, 0, p; }"
-            : "=r"(done)
-            : "r"(bar), "r"(parity), "r"(20000)
-            : "memory");
-        if (done) return true;
-        if (tc_global_ns() - t0 > kTcWaitNs) return false;
-    }
+    return mbar_wait_parity_bounded(bar, parity, kTcWaitNs);
 }
 
 // Byte offset of fp16 element (n, k) of a B operand with R rows (N) in the
@@ -342,6 +327,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
     // scaled by 1 + gcorr = sqrt(ref / out_prev)
     bool chain_start = false;
     float gcorr = 0.f;
+    if constexpr (MODE == 0) {
+        // a factor f ~ 1 (the trace chain of density matrices): folded into W as w + w (f - 1)
+        if (a.scale) gcorr = float(*a.scale - 1.0);
+    }
     if constexpr (MODE == 2) {
         if (a.c_head) {
             double chain_ref = 0.0;
@@ -383,8 +372,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
         const int i = p / D, j = p - (p / D) * D;
         const float2 m = op[a.perm_out[i] * D + a.perm_in[j]];
         float w[4] = {m.x * wscale, -m.y * wscale, m.y * wscale, m.x * wscale};  // (2i,2j) (2i,2j+1) (2i+1,2j) (2i+1,2j+1)
-        if constexpr (MODE == 2) {
-            // the chain's correction 1 + g (|g| ~ 1e-7) goes into W: w + w g in one rounding; the
+        if (MODE != 1 && gcorr != 0.f) {
+            // a chain's correction 1 + g (|g| ~ 1e-7) goes into W: w + w g in one rounding; the
             // hi/lo split then carries it like any other matrix value
 #pragma unroll
             for (int e = 0; e < 4; ++e) w[e] = fmaf(w[e], gcorr, w[e]);
@@ -837,8 +826,9 @@ int set_dense_impl(int mode) {
 // CUDA-core kernel instead.
 int try_dense_tc(void* sv, const void* op, int nbits, const int* sorted, const int* in_bits, const int* out_bits,
                  int k, int64_t op_stride, int64_t batch, int64_t sv_stride, int unitary, cudaStream_t st,
-                 double* chain, int link) {
+                 double* chain, int link, const double* scale) {
     const int mode = dense_impl();
+    if (scale && unitary != 0) return QGB_EDECLINE;  // a factor goes with plain (MODE 0) passes only
     if (unitary == 2 && (batch > 1 || !chain)) return QGB_EDECLINE;  // the chain follows one state
     if (mode == 0 || k < 4 || k > 6 || (k == 4 && mode < 2)) return QGB_EDECLINE;
     if (nbits < 13) return QGB_EDECLINE;              // fewer than one 8192-amplitude tile
@@ -909,6 +899,7 @@ int try_dense_tc(void* sv, const void* op, int nbits, const int* sorted, const i
     a.tiles_per_state = uint64_t(1) << (nbits - 13);  // 8192 amplitudes per tile
     a.tiles = a.tiles_per_state * uint64_t(batch);
     a.sv_stride = batch > 1 ? sv_stride : 0;
+    a.scale = scale;
     float2* s = static_cast<float2*>(sv);
     const float2* m = static_cast<const float2*>(op);
     if (unitary == 2) {

@@ -28,6 +28,43 @@ template <typename C> __device__ __forceinline__ void cfma(C& acc, const C& a, c
     acc.y = fma(a.y, b.x, acc.y);
 }
 
+// ---- bounded device waits --------------------------------------------------
+// Every wait in the library's kernels gives up after a time limit (read from
+// %globaltimer) instead of spinning forever: the caller then records a status
+// word that the host reads (qgb_check_status -> QGB_ETIMEOUT) and returns.
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Waits for phase `parity` of the shared-memory mbarrier at `bar`; false after limit_ns.
+__device__ __forceinline__ bool mbar_wait_parity_bounded(uint32_t bar, uint32_t parity,
+                                                         unsigned long long limit_ns) {
+    const unsigned long long t0 = global_ns();
+    while (true) {
+        uint32_t done;
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3; selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(bar), "r"(parity), "r"(20000)
+            : "memory");
+        if (done) return true;
+        if (global_ns() - t0 > limit_ns) return false;
+    }
+}
+
+// Waits until the global int at `flag` equals `want`; false after limit_ns.
+__device__ __forceinline__ bool flag_wait_bounded(const volatile int* flag, int want, unsigned long long limit_ns) {
+    const unsigned long long t0 = global_ns();
+    while (*flag != want) {
+        __nanosleep(1000);
+        if (global_ns() - t0 > limit_ns) return false;
+    }
+    return true;
+}
+
 // Insert a zero at each (ascending) bit position of `sorted_bits`.
 __device__ __forceinline__ uint64_t insert_zeros(uint64_t g, const int* sorted_bits, int k) {
 #pragma unroll 6
@@ -135,7 +172,7 @@ int sm_count();
 constexpr int QGB_EDECLINE = 1000;
 int try_dense_tc(void* sv, const void* op, int nbits, const int* sorted, const int* in_bits, const int* out_bits,
                  int k, int64_t op_stride, int64_t batch, int64_t sv_stride, int unitary, cudaStream_t st,
-                 double* chain = nullptr, int link = 0);
+                 double* chain = nullptr, int link = 0, const double* scale = nullptr);
 int tc_status_read_clear();
 int fuse_status_read_clear();
 }  // namespace qgb_host

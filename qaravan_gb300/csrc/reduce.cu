@@ -392,6 +392,40 @@ __global__ void __launch_bounds__(kRedThreads) dm_trace_kernel(const cplx<T>* __
     block_reduce_store<1>(acc.d, partials + int64_t(blockIdx.y) * gridDim.x + blockIdx.x, gridDim.x);
 }
 
+// Trace chain of a complex64 density matrix run on the tensor cores: the tensor
+// cores accumulate with round-toward-zero, so every pass shrinks vec(rho) by
+// ~1e-7 of its size, and a channel (unlike a unitary) keeps no vector norm that
+// could be restored. A channel sequence keeps the trace instead: one CTA sums
+// the 2^n diagonal entries (index x (2^n + 1)) in float64 in a fixed order and
+// writes chain[0] = that trace (start) or chain[1] = chain[0] / trace, the
+// factor the next plain tensor-core pass folds into its matrix; chain[2] keeps
+// the measured trace.
+template <typename T>
+__global__ void __launch_bounds__(1024) trace_factor_kernel(const cplx<T>* __restrict__ rho, int n,
+                                                            double* __restrict__ chain, int start) {
+    __shared__ double red[32];
+    const uint64_t dim = uint64_t(1) << n;
+    double s = 0.0;
+#pragma unroll 4
+    for (uint64_t x = threadIdx.x; x < dim; x += blockDim.x) s += double(rho[(x << n) | x].x);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < int(blockDim.x >> 5); ++w) t += red[w];
+        if (start) {
+            chain[0] = t;
+            chain[1] = 1.0;
+        } else {
+            const double ref = chain[0];
+            chain[1] = (ref > 0.0 && t > 0.0) ? ref / t : 1.0;
+        }
+        chain[2] = t;
+    }
+}
+
 // Adjoint reverse step for one gate U on K <= 2 sites, one pass over two vectors:
 //   phi <- U^dagger phi,  lam <- U^dagger lam, and, by GradMode,
 //   kGradNone:     nothing else;
@@ -835,6 +869,17 @@ extern "C" int qgb_dm_trace(const void* rho, int dtype, int n, int64_t batch, in
     return finish((const double*)scratch, red_blocks(2 * n), 1, batch, nullptr, out, st);
 }
 
+extern "C" int qgb_dm_trace_factor(const void* rho, int dtype, int n, double* chain, int start, void* stream) {
+    int rc = check_common(rho, dtype, 2 * n, 1, 0);
+    if (rc) return rc;
+    if (!chain || (reinterpret_cast<uintptr_t>(chain) % sizeof(double)))
+        return set_error(QGB_EINVAL, "chain buffer missing or not 8-byte aligned");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (dtype == QGB_C64) trace_factor_kernel<float><<<1, 1024, 0, st>>>((const float2*)rho, n, chain, start);
+    else trace_factor_kernel<double><<<1, 1024, 0, st>>>((const double2*)rho, n, chain, start);
+    return check_launch("dm trace factor");
+}
+
 extern "C" int qgb_pauli_apply(const void* sv, void* out, int dtype, int n, const char* paulis, const double* coeff,
                                int nterms, int64_t batch, int64_t sv_stride, void* stream) {
     int rc = check_common(sv, dtype, n, batch, sv_stride);
@@ -971,46 +1016,41 @@ extern "C" int qgb_adjoint_step(void* phi, void* lam, int dtype, int n, const in
 // allocation fails. qgb_pauli_expectation needs a caller-provided scratch
 // buffer for its per-block partial sums; this variant takes its partial sums
 // from one fixed array in device memory that is part of the library image
-// (1 MiB, allocated once when the library is loaded on a device and held until
-// the process exits), so a call allocates nothing -- neither device memory nor
-// host heap memory. The array's device address is looked up with
-// cudaGetSymbolAddress the first time the entry point runs on a device (with
-// that device current) and cached per device; make that first call before any
-// stream capture. Every partial-sum slot a call reads was written earlier in
-// the same call, so nothing needs clearing between calls; but all calls share
-// the one array, so two calls whose kernels overlap on the GPU (different
-// streams, or different host threads) race and give wrong results.
+// (1 MiB), so a call allocates nothing -- neither device memory nor host heap
+// memory. CUDA loads a library's device code lazily by default, so the array
+// is reserved on a device when this file's device code is first loaded there:
+// the first call on a device (or the first call of any other reduction entry
+// point) reserves it, and it is held until the process exits. A caller that
+// reserves all device memory for itself makes one warm-up call first (or sets
+// CUDA_MODULE_LOADING=EAGER); the first call on a device also belongs before
+// any stream capture. The array's device address is looked up with
+// cudaGetSymbolAddress on every call, with the caller's device current: the
+// lookup allocates nothing, and a fresh lookup stays right after the context
+// is torn down and recreated (cudaDeviceReset), when the module is loaded
+// again and the array may move. Every partial-sum slot a call reads was
+// written earlier in the same call, so nothing needs clearing between calls;
+// but all calls share the one array, so two calls whose kernels overlap on the
+// GPU (different streams, or different host threads) race and give wrong
+// results.
 namespace {
 
 constexpr size_t kNoAllocScratchDoubles = size_t(1) << 17;  // 1 MiB of float64 partial sums
 constexpr int kNoAllocMaxTerms = 64;
-constexpr int kNoAllocMaxDevices = 64;
+// red_blocks() never exceeds 1216 partial sums per term, so 64 terms always fit:
+// the term count is the only limit
+static_assert(size_t(kNoAllocMaxTerms) * 1216 <= kNoAllocScratchDoubles, "fixed scratch too small for 64 terms");
 
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
 
 void* noalloc_scratch_address(int* rc) {
-    static void* addr[kNoAllocMaxDevices] = {nullptr};
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) {
-        *rc = set_error(QGB_ECUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        *rc = set_error(QGB_ECUDA, "cudaGetSymbolAddress of the fixed scratch array: %s", cudaGetErrorString(e));
         return nullptr;
-    }
-    if (dev < 0 || dev >= kNoAllocMaxDevices) {
-        *rc = set_error(QGB_EINVAL, "device %d beyond the %d devices the scratch cache covers", dev, kNoAllocMaxDevices);
-        return nullptr;
-    }
-    if (!addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            *rc = set_error(QGB_ECUDA, "cudaGetSymbolAddress of the fixed scratch array: %s", cudaGetErrorString(e));
-            return nullptr;
-        }
-        addr[dev] = p;
     }
     *rc = QGB_OK;
-    return addr[dev];
+    return p;
 }
 
 }  // namespace
@@ -1024,10 +1064,6 @@ extern "C" int qgb_pauli_expectation_noalloc(const void* sv, int dtype, int n, c
     if (nterms < 1 || nterms > kNoAllocMaxTerms)
         return set_error(QGB_EINVAL, "%d terms requested; the allocation-free variant takes 1..%d (use "
                          "qgb_pauli_expectation for more)", nterms, kNoAllocMaxTerms);
-    const size_t need = size_t(red_blocks(n)) * size_t(nterms);
-    if (need > kNoAllocScratchDoubles)
-        return set_error(QGB_EINVAL, "%d terms on %d qubits need %zu partial sums; the fixed scratch holds %zu "
-                         "(use qgb_pauli_expectation with a caller buffer)", nterms, n, need, kNoAllocScratchDoubles);
     ParsedPauli ps[kNoAllocMaxTerms];  // parsed on the stack: no heap allocation
     for (int t = 0; t < nterms; ++t) {
         ParsedPauli p{0, 0, 0};

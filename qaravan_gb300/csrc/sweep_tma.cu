@@ -41,24 +41,8 @@ constexpr unsigned long long kWaitNs = 2000000000ull;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
 
-__device__ __forceinline__ unsigned long long global_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
 __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
-    const unsigned long long t0 = global_ns();
-    while (true) {
-        uint32_t done;
-        asm volatile(
-            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3; selp.u32 %0, 1, 0, p; }"
-            : "=r"(done)
-            : "r"(bar), "r"(parity), "r"(20000)
-            : "memory");
-        if (done) return true;
-        if (global_ns() - t0 > kWaitNs) return false;
-    }
+    return mbar_wait_parity_bounded(bar, parity, kWaitNs);
 }
 
 constexpr int kTmaMaxThreads = 32 + 512;  // producer warp + up to 16 compute warps

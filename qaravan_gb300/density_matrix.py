@@ -15,6 +15,8 @@ the operator's rows.
 """
 from __future__ import annotations
 
+import itertools
+
 import numpy as np
 import torch
 
@@ -22,6 +24,9 @@ from . import _lib
 from .compiler import Op, compile_ops
 from .engine import Executor, Scratch
 from .statevector import _to_np, circuit_ops, inner_product
+
+
+_PAIR_IDS = itertools.count()  # ties the ket and bra halves of one gate
 
 
 def _sorted_rows(mat, idx):
@@ -84,7 +89,8 @@ def dm_ops_for_gate(g, n):
         s = np.asarray(g.matrix, dtype=np.complex128).reshape(4 ** len(idx), 4 ** len(idx))
         return [Op(bra + ket, _sorted_rows(s, idx), kind="channel")]
     m = _sorted_rows(_to_np(g.matrix), idx)
-    return [Op(ket, m), Op(bra, np.conj(m))]
+    pair = next(_PAIR_IDS)
+    return [Op(ket, m, pair=pair), Op(bra, np.conj(m), pair=pair)]
 
 
 class DensityMatrixSim:

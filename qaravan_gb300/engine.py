@@ -32,6 +32,31 @@ _NORM_MODES = {"1": "chain", "chain": "chain", "row": "row", "0": "off", "off": 
 _NORM_RESTORE = _NORM_MODES.get(os.environ.get("QGB_NORM_RESTORE", "chain"), "chain")
 
 
+# Complex64 density matrices on the tensor cores keep their trace by a trace
+# chain: the trace is measured (qgb_dm_trace_factor) where the ops applied so
+# far are whole channels, at most every _TRACE_EPOCH tensor-core passes, and the
+# next tensor-core pass multiplies its matrix by reference / measured trace
+# (qgb_op_action_scaled). QGB_TRACE_CHAIN=0 or set_trace_chain(False) turns it off.
+_TRACE_EPOCH = 4
+_TRACE_CHAIN = os.environ.get("QGB_TRACE_CHAIN", "1") not in ("0", "off")
+
+
+def set_trace_chain(on=True):
+    """Process-wide trace chain of complex64 density matrices (default on)."""
+    global _TRACE_CHAIN
+    _TRACE_CHAIN = bool(on)
+
+
+def tc_eligible(code, nbits, k, batch=1):
+    """Whether the library runs a dense op of width k on a vector of nbits bits on
+    the tensor cores (its own rule: complex64, 4-6 bits -- 4 only in its default
+    mode --, at least one 8192-amplitude tile, one operator for the batch)."""
+    if code != _lib.QGB_C64 or nbits < 13 or not 4 <= k <= 6:
+        return False
+    impl = _lib.lib().qgb_get_dense_impl()
+    return impl >= 2 or (impl == 1 and k >= 5)
+
+
 def set_norm_restore(mode="chain"):
     """Process-wide norm control of unitary tensor-core blocks: "chain" (default),
     "row", or "off" (True / False mean "chain" / "off")."""
@@ -100,7 +125,8 @@ class Executor:
             if isinstance(s, DenseStep):
                 nb = plan.nbits
                 sites = [nb - 1 - b for b in s.bits]
-                self._steps.append(("dense", _lib.int_array(sites), len(sites), offs[s.mat], s.unitary))
+                self._steps.append(("dense", _lib.int_array(sites), len(sites), offs[s.mat], s.unitary, s.whole,
+                                    tc_eligible(self.code, nb, len(sites))))
             elif isinstance(s, SweepStep):
                 sw = _lib.Sweep()
                 sw.low_bits = s.low_bits
@@ -212,12 +238,38 @@ class Executor:
         mptr = mats.data_ptr()
         launches = 0
         link = 0  # position in the current norm chain of consecutive unitary blocks
+        # trace chain: one complex64 density matrix whose ops keep the trace
+        tchain = (_TRACE_CHAIN and self.normalize_kind == "dm" and self.code == _lib.QGB_C64 and batch == 1
+                  and mats is self.mats and self.plan.trace_kept
+                  and any(s[0] == "dense" and s[6] for s in self._steps))
+        if tchain:
+            if getattr(self, "_tchain", None) is None:
+                self._tchain = torch.zeros(4, dtype=torch.float64, device=self.device)
+            tptr = self._tchain.data_ptr()
+            _lib.check(L.qgb_dm_trace_factor(ptr, self.code, nb // 2, tptr, 1, st), "dm_trace_factor")
+            launches += 1
+            t_since, t_pending = 0, False  # tensor-core passes since the last measurement; a factor waits
         for s in self._steps:
             if events is not None and s[0] != "normalize":
                 e0 = torch.cuda.Event(enable_timing=True)
                 e0.record()
-            if s[0] == "dense":
-                _, sites, k, off, unitary = s
+            if s[0] == "dense" and tchain:
+                _, sites, k, off, unitary, whole, on_tc = s
+                if on_tc and t_pending:
+                    _lib.check(L.qgb_op_action_scaled(ptr, self.code, nb, sites, k, mptr + off * self.itemsize,
+                                                      tptr + 8, st), "op_action")
+                    t_pending = False
+                else:
+                    _lib.check(L.qgb_op_action(ptr, self.code, nb, sites, k, mptr + off * self.itemsize, 0, 1, 0,
+                                               st), "op_action")
+                launches += 1
+                t_since += int(on_tc)
+                if whole and t_since >= _TRACE_EPOCH:
+                    _lib.check(L.qgb_dm_trace_factor(ptr, self.code, nb // 2, tptr, 0, st), "dm_trace_factor")
+                    launches += 1
+                    t_since, t_pending = 0, True
+            elif s[0] == "dense":
+                _, sites, k, off, unitary = s[:5]
                 # per-vector matrices (mat_stride) need not be unitary: only the plan's own are flagged
                 mode = _NORM_RESTORE if (unitary and mats is self.mats) else "off"
                 if mode == "chain" and batch == 1:
@@ -254,6 +306,10 @@ class Executor:
             else:
                 launches += self.normalize(state, batch, stride)
                 link = 0
+                if tchain:  # the trace is 1 again: a new reference
+                    _lib.check(L.qgb_dm_trace_factor(ptr, self.code, nb // 2, tptr, 1, st), "dm_trace_factor")
+                    launches += 1
+                    t_since, t_pending = 0, False
             if events is not None and s[0] != "normalize":
                 e1 = torch.cuda.Event(enable_timing=True)
                 e1.record()

@@ -162,31 +162,3 @@ def z_terms(n):
     zs = [(1.0, 'i' * q + 'z' + 'i' * (n - q - 1)) for q in range(n)]
     zz = [(1.0, 'i' * q + 'zz' + 'i' * (n - q - 2)) for q in range(n - 1)]
     return zs + zz
-
-
-def _main(argv=None):
-    """``python -m qaravan_gb300.trajectories [qubits] [trajectories] [trotter steps]``:
-    per-gate device time of the noisy TFI trajectory workload (depolarising
-    1e-3 and amplitude damping 5e-4 after every gate), grouped by the width of
-    the gate's union with the pending sites and by whether it reaches bits 0..2."""
-    import sys
-    from . import workloads
-    args = [int(a) for a in (sys.argv[1:] if argv is None else argv)]
-    n, T, steps = (args + [20, 1024, 2][len(args):])[:3]
-    sim = TrajectorySim(workloads.tfi_trotter_circuit(n, 0.05, steps), T, p_dep=1e-3, gamma=5e-4, seed=2026)
-    sim.run()
-    rows = sim.time_gates()
-    alg = 2 * T * 2 ** n * np.dtype(np.complex64 if sim.dtype == torch.complex64 else np.complex128).itemsize
-    groups = {}
-    for _, k, lo, ms in rows:
-        groups.setdefault((k, "low" if lo < 3 else "high"), []).append(ms)
-    total = sum(ms for *_, ms in rows)
-    print(f"{n} qubits, {T} trajectories, {len(rows)} gates: {total / len(rows):.3f} ms/gate, "
-          f"{alg / 1e9:.2f} GB algorithmic per gate")
-    for key in sorted(groups):
-        v = groups[key]
-        print(f"union {key[0]} {key[1]}: {len(v)} gates, {np.mean(v):.3f} ms, {alg / np.mean(v) / 1e6:.0f} GB/s")
-
-
-if __name__ == "__main__":
-    _main()

@@ -4,10 +4,11 @@ buffer-taking one.
 qgb_pauli_expectation_noalloc exists for callers that may not allocate device
 memory (real-time loops that may not stall on the allocator, plugins inside an
 application that owns all device memory, fully reserved GPUs): it keeps its
-partial sums in a fixed device array inside the library instead of a caller
-buffer. This file is collected last so that, if it fails, a run that stops at
-the first failure has already run every other test; it also passes alone in a
-fresh process (it builds the library and makes its own states).
+partial sums in a fixed device array inside the library, which holds the
+partial sums of up to 64 terms, instead of a caller buffer. This file is
+collected last so that, if it fails, a run that stops at the first failure has
+already run every other test; it also passes alone in a fresh process (it
+builds the library and makes its own states).
 """
 import numpy as np
 import pytest
@@ -59,11 +60,86 @@ def test_noalloc_matches_buffered_entry_point_twice(cuda_ok, dtype, n):
         assert torch.max(torch.abs(out - ref)).item() < tol
 
 
+def _compare(L, sv, n, code, terms, tol, calls=2):
+    from qaravan_gb300 import _lib
+    st = _lib.stream_ptr()
+    strings = "".join(s for _, s in terms).encode()
+    coeff = _lib.double_array([c for c, _ in terms])
+    nt = len(terms)
+    ref = torch.empty(nt, dtype=torch.float64, device="cuda")
+    nbytes = L.qgb_reduce_scratch_bytes(n, nt, 1)
+    scratch = torch.empty(nbytes // 8 + 1, dtype=torch.float64, device="cuda")
+    _lib.check(L.qgb_pauli_expectation(sv.data_ptr(), code, n, strings, coeff, nt, 1, 0, ref.data_ptr(),
+                                       scratch.data_ptr(), nbytes, st), "pauli_expectation")
+    for _ in range(calls):
+        out = torch.full((nt,), float("nan"), dtype=torch.float64, device="cuda")
+        _lib.check(L.qgb_pauli_expectation_noalloc(sv.data_ptr(), code, n, strings, coeff, nt, out.data_ptr(), st),
+                   "pauli_expectation_noalloc")
+        torch.cuda.synchronize()
+        scale = max(1.0, torch.max(torch.abs(ref)).item())
+        assert torch.max(torch.abs(out - ref)).item() < tol * scale
+
+
+def test_noalloc_64_terms_with_one_x_mask_split_over_two_launches(cuda_ok):
+    # 40 consecutive terms share the X mask of 'x' on site 0: more than the 32 terms one
+    # launch takes, so that run is split in two; 64 terms is the entry point's maximum
+    from qaravan_gb300 import _lib, build
+    build.build()
+    L = _lib.lib()
+    n = 16
+    rng = np.random.default_rng(5)
+    sv = _state(n, torch.complex64, 77)
+    terms = [(float(rng.normal()), 'x' + ''.join(rng.choice(list('iz'), size=n - 1))) for _ in range(40)]
+    terms += [(float(rng.normal()), ''.join(rng.choice(list('ixyz'), size=n))) for _ in range(24)]
+    assert len(terms) == 64
+    _compare(L, sv, n, _lib.QGB_C64, terms, 1e-5)
+
+
+def test_noalloc_64_bit_indices_on_32_qubits(cuda_ok):
+    # 2^32 amplitudes (34 GB of complex64): the reduction kernels switch to 64-bit indices above 31 qubits
+    from qaravan_gb300 import _lib, build
+    build.build()
+    L = _lib.lib()
+    n = 32
+    sv = torch.empty(2 ** n, dtype=torch.complex64, device="cuda")
+    torch.view_as_real(sv).normal_(generator=torch.Generator(device="cuda").manual_seed(3))
+    terms = [(1.0, 'z' + 'i' * (n - 1)), (0.5, 'i' * (n - 1) + 'x'), (-0.25, 'y' + 'i' * (n - 2) + 'y'),
+             (2.0, 'x' * n)]
+    _compare(L, sv, n, _lib.QGB_C64, terms, 1e-5)
+    del sv
+    torch.cuda.empty_cache()
+
+
+def test_noalloc_second_call_leaves_free_device_memory_unchanged(cuda_ok):
+    # the first call loads the library's reduction code and reserves the fixed array;
+    # after it, calls reserve nothing
+    from qaravan_gb300 import _lib, build
+    build.build()
+    L = _lib.lib()
+    n = 20
+    sv = _state(n, torch.complex64, 9)
+    terms = _terms(n, 4)
+    strings = "".join(s for _, s in terms).encode()
+    coeff = _lib.double_array([c for c, _ in terms])
+    out = torch.empty(len(terms), dtype=torch.float64, device="cuda")
+    st = _lib.stream_ptr()
+    _lib.check(L.qgb_pauli_expectation_noalloc(sv.data_ptr(), _lib.QGB_C64, n, strings, coeff, len(terms),
+                                               out.data_ptr(), st), "pauli_expectation_noalloc")
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        _lib.check(L.qgb_pauli_expectation_noalloc(sv.data_ptr(), _lib.QGB_C64, n, strings, coeff, len(terms),
+                                                   out.data_ptr(), st), "pauli_expectation_noalloc")
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+
+
 def test_noalloc_rejects_sizes_beyond_its_fixed_scratch(cuda_ok):
     from qaravan_gb300 import _lib, build
     build.build()
     L = _lib.lib()
-    n = 24  # 1216 partial sums per term: at most 107 terms fit, and the entry point caps at 64
+    n = 24  # the entry point takes at most 64 terms
     sv = _state(n, torch.complex64, 1)
     out = torch.empty(80, dtype=torch.float64, device="cuda")
     strings = ("z" + "i" * (n - 1)).encode() * 80
