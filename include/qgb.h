@@ -85,6 +85,26 @@ typedef struct {
     double op_gen_val[QGB_SWEEP_MAX_OPS][4][2];
 } qgb_adjoint_sweep;
 
+/* One tile sweep of the persistent trajectory kernel: the tile is the low L
+ * flat bits times the H listed high bits (ascending, >= L); ops
+ * [op_begin, op_end) of the op table run on it, in order (at most 128). */
+typedef struct {
+    int32_t L, H;
+    int32_t high_bits[QGB_SWEEP_MAX_HIGH];
+    int32_t op_begin, op_end;
+} qgb_traj_sweep;
+
+/* One gate of a trajectory sweep: width k (1 or 2), its sites as tile
+ * positions in matrix order (pos[0] is the matrix's most significant bit),
+ * the gate's index in the circuit (the Philox event of its channels, and what
+ * the jump log records) and the element offset of its 2^k x 2^k matrix. */
+typedef struct {
+    int32_t k;
+    int32_t pos[2];
+    int32_t gate;
+    int64_t mat;
+} qgb_traj_op;
+
 int qgb_abi_version(void);
 const char* qgb_last_error(void);
 /* Reads and clears the device status word set by bounded waits; returns
@@ -369,6 +389,29 @@ int qgb_traj_step(void* sv, int dtype, int n, int64_t ntraj, int64_t stride, con
                   const void* gate, const int* prev_sites, int kprev, void* kraus, double p_dep, double gamma,
                   uint64_t seed, uint32_t event, double* partials, uint8_t* pauli_log, uint8_t* jump_log,
                   void* stream);
+
+/* Every trajectory of a noisy circuit in one persistent launch (replaces the
+ * reference's per-sample loop MonteCarloSim.circuit_sample /
+ * expectation_sample, tensorQ/monte_carlo_sim.py:14-35, extended to amplitude
+ * damping as in qgb_traj_step). Each CTA takes the next trajectory from a
+ * work counter and runs it through every sweep (tables `sweeps_dev` /
+ * `ops_dev` in device memory, `sweeps_host` the same sweeps in host memory
+ * for validation; matrices at `mats` in the state's dtype): after each gate,
+ * on each of its sites, depolarising p_dep (the Paulis qgb_traj_step draws
+ * for the same seed) then amplitude damping gamma, unravelled exactly by the
+ * no-jump norm (a sweep that contains a jump runs again from its input with
+ * the jump). Output: the normalised final states at sv + t * stride,
+ * jump_count[t] (device, may be NULL) and, when max_log > 0, the first max_log
+ * jumps of trajectory t as (gate, site) pairs at jump_log[(t * max_log + i) *
+ * 2]. scratch: qgb_traj_run_scratch_bytes(dtype, n, largest tile bits, ntraj)
+ * bytes of device memory (a work counter and one state per resident CTA). */
+int qgb_traj_run(void* sv, int dtype, int n, int64_t ntraj, int64_t stride, const qgb_traj_sweep* sweeps_host,
+                 const qgb_traj_sweep* sweeps_dev, int nsweeps, const qgb_traj_op* ops_dev, int nops,
+                 const void* mats, double p_dep, double gamma, uint64_t seed, int* jump_count, int* jump_log,
+                 int max_log, void* scratch, size_t scratch_bytes, void* stream);
+size_t qgb_traj_run_scratch_bytes(int dtype, int n, int tile_bits, int64_t ntraj);
+size_t qgb_traj_sweep_bytes(void);
+size_t qgb_traj_op_bytes(void);
 
 /* The Philox uniform the trajectory kernels draw (host-side, for replays). */
 void qgb_philox_uniform(uint32_t event, uint32_t traj, uint32_t stream, uint64_t seed, double* out);

@@ -106,6 +106,11 @@ SIGNATURES = {
     "qgb_traj_step": (C.c_int, [_vp, _i, _i, _i64, _i64, _ip, _i, _vp, _ip, _i, _vp, C.c_double, C.c_double,
                                 _u64, C.c_uint32, _vp, _vp, _vp, _vp]),
     "qgb_philox_uniform": (None, [C.c_uint32, C.c_uint32, C.c_uint32, _u64, C.POINTER(C.c_double)]),
+    "qgb_traj_run": (C.c_int, [_vp, _i, _i, _i64, _i64, _vp, _vp, _i, _vp, _i, _vp, C.c_double, C.c_double, _u64,
+                               _vp, _vp, _i, _vp, _sz, _vp]),
+    "qgb_traj_run_scratch_bytes": (C.c_size_t, [_i, _i, _i, _i64]),
+    "qgb_traj_sweep_bytes": (C.c_size_t, []),
+    "qgb_traj_op_bytes": (C.c_size_t, []),
     "qgb_dm_apply_superop": (C.c_int, [_vp, _i, _i, _ip, _i, _vp, _i64, _i64, _vp]),
     "qgb_dm_pauli_expectation": (C.c_int, [_vp, _i, _i, _cp, _dp, _i, _i64, _i64, _vp, _vp, _sz, _vp]),
     "qgb_dm_product_expectation": (C.c_int, [_vp, _i, _i, _dp, _i64, _i64, _vp, _vp, _sz, _vp]),

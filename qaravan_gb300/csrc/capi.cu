@@ -104,6 +104,9 @@ extern "C" int qgb_check_status(void* stream) {
     const int tc = qgb_host::tc_status_read_clear();
     if (tc < 0) return qgb_host::set_error(QGB_ECUDA, "tensor-core status read failed");
     if (tc != 0) return qgb_host::set_error(QGB_ETIMEOUT, "a tensor-core completion wait gave up (code %d)", tc);
+    const int tj = qgb_host::traj_status_read_clear();
+    if (tj < 0) return qgb_host::set_error(QGB_ECUDA, "trajectory status read failed");
+    if (tj != 0) return qgb_host::set_error(QGB_EINVAL, "more than 16 jumps in one sweep of a trajectory (code %d)", tj);
     const int fu = qgb_host::fuse_status_read_clear();
     if (fu < 0) return qgb_host::set_error(QGB_ECUDA, "fusion status read failed");
     if (fu != 0) return qgb_host::set_error(QGB_EINVAL, "a fusion table entry was out of bounds (code %d)", fu);

@@ -98,13 +98,19 @@ class StatevectorSim:
         if self.device.type != "cuda":
             raise _lib.QgbError("qaravan_gb300 runs on CUDA devices only")
         self.dtype = dtype
-        # auto: complex64 -> dense fused blocks, one HBM pass each: 6-qubit blocks on the tensor
-        # cores from 13 qubits up (half the passes of 4-qubit blocks at the same speed per pass,
-        # fastest measured on the 28-qubit brickwork), 4-qubit blocks on the CUDA cores below;
-        # complex128 -> 3-qubit blocks grouped into shared-memory tile sweeps (float64 arithmetic
-        # dominates, so fewer passes win)
+        # auto: the autotuner's choice for this size and dtype (a cached measurement, a
+        # measurement now with QGB_AUTOTUNE=1, else the defaults measured on GB300:
+        # complex64 -> dense fused blocks, one HBM pass each: 6-qubit blocks on the tensor
+        # cores from 13 qubits up (half the passes of 4-qubit blocks at the same speed per
+        # pass, fastest measured on the 28-qubit brickwork), 4-qubit blocks on the CUDA cores
+        # below; complex128 -> 3-qubit blocks grouped into shared-memory tile sweeps (float64
+        # arithmetic dominates, so fewer passes win))
         if mode == "auto":
-            mode = "fused" if dtype == torch.complex64 else "sweep"
+            from . import autotune
+            a_mode, a_width, a_tile = autotune.choose_sv(circ.num_sites, dtype)
+            mode = a_mode
+            fusion_width = a_width if fusion_width is None else fusion_width
+            tile_bits = a_tile if tile_bits is None else tile_bits
         if fusion_width is None:
             if dtype == torch.complex64:
                 fusion_width = 6 if circ.num_sites >= 13 and _lib.lib().qgb_get_dense_impl() >= 1 else 4
