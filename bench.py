@@ -211,6 +211,23 @@ def _event_ms(fn, warmup=1, steps=1):
     return a.elapsed_time(b) / steps
 
 
+def fma_peaks():
+    """Measured rate of the float32 and float64 FMA pipes (qgb_fma_probe: 8
+    independent FMA chains per thread, 8 CTAs of 256 threads per SM), TFLOP/s."""
+    import torch
+    from qaravan_gb300 import _lib
+    L = _lib.lib()
+    out = torch.empty(152 * 32, dtype=torch.float64, device="cuda")
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    res = {}
+    for name, prec, iters in (("fp32_tflops", 0, 200000), ("fp64_tflops", 1, 20000)):
+        def run():
+            _lib.check(L.qgb_fma_probe(prec, iters, 8, out.data_ptr(), _lib.stream_ptr()), "fma_probe")
+        ms = _event_ms(run, 1, 3)
+        res[name] = round(2 * 8 * iters * 256 * 8 * sms / (ms / 1e3) / 1e12, 2)
+    return res
+
+
 def section_variants(n, gates):
     """Unfused (one HBM pass per gate), fused dense blocks of width 2..6 on the
     CUDA cores and (4..6) on the tensor cores, shared-memory tile sweeps, and
@@ -248,6 +265,15 @@ def section_variants(n, gates):
             ms = _event_ms(step, 1, 1)
             out[name] = {"gates_per_s": round(len(gates) / (ms / 1e3), 1), "ms": round(ms, 2),
                          "hbm_passes": ex.plan.n_sweeps}
+            if dtype == torch.complex128:
+                from qaravan_gb300.compiler import plan_flops
+                flops = plan_flops(ex.plan)[1] * 2 ** n
+                out[name]["tflops"] = round(flops / (ms / 1e3) / 1e12, 3)
+                peaks = out.setdefault("fma_peaks", fma_peaks())
+                out[name]["roofline"] = {"bound": "fp64", "achieved": out[name]["tflops"],
+                                         "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
+                                         "frac": round(out[name]["tflops"] / peaks["fp64_tflops"], 3),
+                                         "peak_source": "qgb_fma_probe float64 FMA rate measured in this run"}
             del st, ex
         except Exception as e:  # a variant that does not fit is reported, not fatal
             out[name] = {"error": str(e)[:200]}
@@ -862,6 +888,8 @@ def run_case(args):
         evaluation of the hardware-efficient ansatz (default 18 4 64);
       trajectory_gates [qubits trajectories steps]: the noisy TFI trajectories
         gate by gate with CUDA events around every gate (default 20 1024 2);
+      trajectories [qubits trajectories steps tile_bits]: the same workload in
+        one persistent launch (default 18 256 2 13);
       dm_batch [circuits seed]: the uneven noisy density-matrix batch (default 32 7)."""
     import torch
     from qaravan_gb300 import build as qbuild
@@ -889,6 +917,14 @@ def run_case(args):
         total = sum(ms for *_, ms in rows)
         print(f"{n} qubits, {T} trajectories, {len(rows)} gates: {total / len(rows):.3f} ms/gate, "
               f"{alg / 1e9:.2f} GB algorithmic per gate")
+    elif args.case == "trajectories":
+        from qaravan_gb300.trajectories import TrajectorySim
+        n, T, steps, tile = (vals + [18, 256, 2, 13][len(vals):])[:4]
+        sim = TrajectorySim(workloads.tfi_trotter_circuit(n, 0.05, steps), T, p_dep=1e-3, gamma=5e-4, seed=2026,
+                            tile_bits=tile)
+        ms = _event_ms(sim.run, 1, 1)
+        print(f"{n} qubits, {T} trajectories, {len(sim.gates)} gates, {len(sim.sweep_plan)} sweeps of "
+              f"{tile}-bit tiles: {ms:.2f} ms, {int(sim.jump_count.sum().item())} jumps")
     elif args.case == "dm_batch":
         from qaravan_gb300 import DensityMatrixSim
         from qaravan_gb300.batch import DensityMatrixBatch

@@ -119,6 +119,13 @@ int qgb_check_status(void* stream);
  * up records its code in the status word, so the next qgb_check_status
  * returns QGB_ETIMEOUT, and the kernel returns; the context stays usable. */
 int qgb_wait_probe(int mode, unsigned long long limit_ns, const int* flag, void* stream);
+/* Peak rate of the fused multiply-add pipe (no counterpart in the reference):
+ * sm_count * blocks_per_sm CTAs of 256 threads each run 8 independent chains
+ * of `iters` FMAs in float32 (precision 0) or float64 (precision 1);
+ * 2 * 8 * iters * 256 * CTAs flops, no memory traffic. Time it with events on
+ * `stream`; `out` is a device buffer of at least one value per CTA that is
+ * never written in practice. The complex128 kernels' roofline is this rate. */
+int qgb_fma_probe(int precision, int iters, int blocks_per_sm, void* out, void* stream);
 
 /* ---- statevector ------------------------------------------------------ */
 
@@ -395,8 +402,9 @@ int qgb_traj_step(void* sv, int dtype, int n, int64_t ntraj, int64_t stride, con
  * expectation_sample, tensorQ/monte_carlo_sim.py:14-35, extended to amplitude
  * damping as in qgb_traj_step). Each CTA takes the next trajectory from a
  * work counter and runs it through every sweep (tables `sweeps_dev` /
- * `ops_dev` in device memory, `sweeps_host` the same sweeps in host memory
- * for validation; matrices at `mats` in the state's dtype): after each gate,
+ * `ops_dev` in device memory, `sweeps_host` / `ops_host` the same tables in
+ * host memory, checked before the launch; `mat_elems` matrices' elements at
+ * `mats` in the state's dtype): after each gate,
  * on each of its sites, depolarising p_dep (the Paulis qgb_traj_step draws
  * for the same seed) then amplitude damping gamma, unravelled exactly by the
  * no-jump norm (a sweep that contains a jump runs again from its input with
@@ -406,9 +414,10 @@ int qgb_traj_step(void* sv, int dtype, int n, int64_t ntraj, int64_t stride, con
  * 2]. scratch: qgb_traj_run_scratch_bytes(dtype, n, largest tile bits, ntraj)
  * bytes of device memory (a work counter and one state per resident CTA). */
 int qgb_traj_run(void* sv, int dtype, int n, int64_t ntraj, int64_t stride, const qgb_traj_sweep* sweeps_host,
-                 const qgb_traj_sweep* sweeps_dev, int nsweeps, const qgb_traj_op* ops_dev, int nops,
-                 const void* mats, double p_dep, double gamma, uint64_t seed, int* jump_count, int* jump_log,
-                 int max_log, void* scratch, size_t scratch_bytes, void* stream);
+                 const qgb_traj_sweep* sweeps_dev, int nsweeps, const qgb_traj_op* ops_host,
+                 const qgb_traj_op* ops_dev, int nops, const void* mats, int64_t mat_elems, double p_dep,
+                 double gamma, uint64_t seed, int* jump_count, int* jump_log, int max_log, void* scratch,
+                 size_t scratch_bytes, void* stream);
 size_t qgb_traj_run_scratch_bytes(int dtype, int n, int tile_bits, int64_t ntraj);
 size_t qgb_traj_sweep_bytes(void);
 size_t qgb_traj_op_bytes(void);

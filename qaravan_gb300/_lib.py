@@ -63,6 +63,7 @@ SIGNATURES = {
     "qgb_last_error": (C.c_char_p, []),
     "qgb_check_status": (C.c_int, [_vp]),
     "qgb_wait_probe": (C.c_int, [_i, C.c_ulonglong, _vp, _vp]),
+    "qgb_fma_probe": (C.c_int, [_i, _i, _i, _vp, _vp]),
     "qgb_op_action": (C.c_int, [_vp, _i, _i, _ip, _i, _vp, _i64, _i64, _i64, _vp]),
     "qgb_op_action_unitary": (C.c_int, [_vp, _i, _i, _ip, _i, _vp, _i64, _i64, _i64, _vp]),
     "qgb_op_action_unitary_chain": (C.c_int, [_vp, _i, _i, _ip, _i, _vp, _i64, _i64, _i64, _vp, _i, _vp]),
@@ -106,8 +107,8 @@ SIGNATURES = {
     "qgb_traj_step": (C.c_int, [_vp, _i, _i, _i64, _i64, _ip, _i, _vp, _ip, _i, _vp, C.c_double, C.c_double,
                                 _u64, C.c_uint32, _vp, _vp, _vp, _vp]),
     "qgb_philox_uniform": (None, [C.c_uint32, C.c_uint32, C.c_uint32, _u64, C.POINTER(C.c_double)]),
-    "qgb_traj_run": (C.c_int, [_vp, _i, _i, _i64, _i64, _vp, _vp, _i, _vp, _i, _vp, C.c_double, C.c_double, _u64,
-                               _vp, _vp, _i, _vp, _sz, _vp]),
+    "qgb_traj_run": (C.c_int, [_vp, _i, _i, _i64, _i64, _vp, _vp, _i, _vp, _vp, _i, _vp, _i64, C.c_double,
+                               C.c_double, _u64, _vp, _vp, _i, _vp, _sz, _vp]),
     "qgb_traj_run_scratch_bytes": (C.c_size_t, [_i, _i, _i, _i64]),
     "qgb_traj_sweep_bytes": (C.c_size_t, []),
     "qgb_traj_op_bytes": (C.c_size_t, []),

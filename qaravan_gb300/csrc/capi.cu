@@ -86,6 +86,37 @@ extern "C" int qgb_wait_probe(int mode, unsigned long long limit_ns, const int* 
     return qgb_host::check_launch("wait probe");
 }
 
+namespace qgb {
+// Peak rate of the FMA pipe of one precision: 8 independent chains of fused
+// multiply-adds per thread (so the pipe, not the dependency latency, bounds
+// it); the sum is stored only under a condition that never holds, which keeps
+// the chains alive without memory traffic.
+template <typename T>
+__global__ void __launch_bounds__(256) fma_probe_kernel(T* out, int iters, T a, T b) {
+    T x[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) x[j] = T(threadIdx.x + j) * T(1e-3);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) x[j] = fma(x[j], a, b);
+    }
+    T s = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s += x[j];
+    if (s == T(-1.2345e-7)) out[blockIdx.x] = s;
+}
+}  // namespace qgb
+
+extern "C" int qgb_fma_probe(int precision, int iters, int blocks_per_sm, void* out, void* stream) {
+    if ((precision != 0 && precision != 1) || iters < 1 || blocks_per_sm < 1 || blocks_per_sm > 32 || !out)
+        return qgb_host::set_error(QGB_EINVAL, "fma probe arguments invalid");
+    const unsigned grid = unsigned(qgb_host::sm_count() * blocks_per_sm);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (precision == 0) qgb::fma_probe_kernel<float><<<grid, 256, 0, st>>>((float*)out, iters, 0.9999999f, 1e-7f);
+    else qgb::fma_probe_kernel<double><<<grid, 256, 0, st>>>((double*)out, iters, 0.9999999999, 1e-12);
+    return qgb_host::check_launch("fma probe");
+}
+
 extern "C" int qgb_check_status(void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     cudaError_t e = cudaStreamSynchronize(st);

@@ -413,8 +413,8 @@ int traj_grid(int mmax, int hmax, int64_t ntraj, int* nbuf_out, size_t* smem_out
     return set_error(QGB_EINVAL, "trajectory tile of 2^%d amplitudes does not fit in shared memory", mmax);
 }
 
-int traj_check_tables(int n, const TrajSweepDesc* sweeps, int nsweeps, int nops_total, int* mmax, int* hmax,
-                      int dtype) {
+int traj_check_tables(int n, const TrajSweepDesc* sweeps, int nsweeps, const TrajOpDesc* ops, int nops_total,
+                      int64_t mat_elems, int* mmax, int* hmax, int dtype) {
     *mmax = 1;
     *hmax = 0;
     const int lmin = dtype == QGB_C64 ? 1 : 0;
@@ -434,6 +434,15 @@ int traj_check_tables(int n, const TrajSweepDesc* sweeps, int nsweeps, int nops_
             return set_error(QGB_EINVAL, "sweep %d: op range [%d, %d) invalid", s, sw.op_begin, sw.op_end);
         if (m > *mmax) *mmax = m;
         if (sw.H > *hmax) *hmax = sw.H;
+        for (int i = sw.op_begin; i < sw.op_end; ++i) {
+            const TrajOpDesc& op = ops[i];
+            if (op.k < 1 || op.k > 2 || op.k > m) return set_error(QGB_EINVAL, "op %d: width %d invalid", i, op.k);
+            for (int j = 0; j < op.k; ++j)
+                if (op.pos[j] < 0 || op.pos[j] >= m) return set_error(QGB_EINVAL, "op %d: tile position out of range", i);
+            if (op.k == 2 && op.pos[0] == op.pos[1]) return set_error(QGB_EINVAL, "op %d: repeated tile position", i);
+            if (op.gate < 0 || op.mat < 0 || op.mat + (int64_t(1) << (2 * op.k)) > mat_elems)
+                return set_error(QGB_EINVAL, "op %d: gate index or matrix offset out of range", i);
+        }
     }
     return QGB_OK;
 }
@@ -457,10 +466,11 @@ extern "C" size_t qgb_traj_run_scratch_bytes(int dtype, int n, int tile_bits, in
 }
 
 extern "C" int qgb_traj_run(void* sv, int dtype, int n, int64_t ntraj, int64_t stride, const qgb_traj_sweep* sweeps_host,
-                            const qgb_traj_sweep* sweeps_dev, int nsweeps, const qgb_traj_op* ops_dev, int nops,
-                            const void* mats, double p_dep, double gamma, uint64_t seed, int* jump_count,
+                            const qgb_traj_sweep* sweeps_dev, int nsweeps, const qgb_traj_op* ops_host,
+                            const qgb_traj_op* ops_dev, int nops, const void* mats, int64_t mat_elems, double p_dep, double gamma, uint64_t seed, int* jump_count,
                             int* jump_log, int max_log, void* scratch, size_t scratch_bytes, void* stream) {
-    if (!sv || !sweeps_host || !sweeps_dev || !ops_dev || !mats || !scratch) return set_error(QGB_EINVAL, "null pointer");
+    if (!sv || !sweeps_host || !sweeps_dev || !ops_host || !ops_dev || !mats || !scratch)
+        return set_error(QGB_EINVAL, "null pointer");
     if (dtype != QGB_C64 && dtype != QGB_C128) return set_error(QGB_EINVAL, "dtype %d unknown", dtype);
     if (n < 1 || n > 30) return set_error(QGB_EINVAL, "n=%d invalid (trajectories of 1 to 30 qubits)", n);
     if (ntraj < 1 || ntraj > (int64_t(1) << 30)) return set_error(QGB_EINVAL, "ntraj %lld out of range", (long long)ntraj);
@@ -474,7 +484,8 @@ extern "C" int qgb_traj_run(void* sv, int dtype, int n, int64_t ntraj, int64_t s
         return set_error(QGB_EINVAL, "state, stride and scratch must be 16-byte aligned");
     if (reinterpret_cast<uintptr_t>(mats) % isz) return set_error(QGB_EINVAL, "matrix buffer misaligned");
     int mmax = 1, hmax = 0;
-    int rc = traj_check_tables(n, reinterpret_cast<const TrajSweepDesc*>(sweeps_host), nsweeps, nops, &mmax, &hmax, dtype);
+    int rc = traj_check_tables(n, reinterpret_cast<const TrajSweepDesc*>(sweeps_host), nsweeps,
+                               reinterpret_cast<const TrajOpDesc*>(ops_host), nops, mat_elems, &mmax, &hmax, dtype);
     if (rc) return rc;
     int nbuf = 0;
     size_t smem = 0;

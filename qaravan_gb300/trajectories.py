@@ -187,6 +187,7 @@ class TrajectorySim:
         self.sweep_plan = plan
         self._sweeps_host = np.ascontiguousarray(sw)
         self._sweeps_dev = torch.from_numpy(sw.view(np.uint8).copy()).to(self.device)
+        self._ops_host = np.ascontiguousarray(ops)
         self._ops_dev = torch.from_numpy(ops.view(np.uint8).copy()).to(self.device)
         self._nops = o
         code = _lib.dtype_code(self.dtype)
@@ -232,8 +233,8 @@ class TrajectorySim:
         jl = self.jump_events.data_ptr() if self.jump_events is not None else None
         _lib.check(L.qgb_traj_run(self.state.data_ptr(), code, self.n, self.ntraj, 2 ** self.n,
                                   self._sweeps_host.ctypes.data, self._sweeps_dev.data_ptr(),
-                                  len(self.sweep_plan), self._ops_dev.data_ptr(), self._nops, self.mats.data_ptr(),
-                                  self.p_dep, self.gamma, self.seed, self.jump_count.data_ptr(), jl, self.max_log,
+                                  len(self.sweep_plan), self._ops_host.ctypes.data, self._ops_dev.data_ptr(),
+                                  self._nops, self.mats.data_ptr(), self.mats.numel(), self.p_dep, self.gamma, self.seed, self.jump_count.data_ptr(), jl, self.max_log,
                                   self._scratch.data_ptr(), self._scratch_bytes, st), "traj_run")
 
     @property
