@@ -97,12 +97,22 @@ typedef struct {
 /* One gate of a trajectory sweep: width k (1 or 2), its sites as tile
  * positions in matrix order (pos[0] is the matrix's most significant bit),
  * the gate's index in the circuit (the Philox event of its channels, and what
- * the jump log records) and the element offset of its 2^k x 2^k matrix. */
+ * the jump log records) and the element offset of its 2^k x 2^k matrix;
+ * flags bit 0: the matrix is diagonal. Consecutive ops form runs over R tile
+ * bits (R = min(4, tile bits) for complex64, min(3, tile bits) for
+ * complex128) applied to groups of 2^R amplitudes in registers: the first op
+ * of a run holds the run's length in `run` and the tile positions of its R
+ * local bits in run_pos (local bit i <-> run_pos[i]); the others hold run = 0.
+ * lpos: each site's local bit in its run (run_pos[lpos[j]] == pos[j]). */
 typedef struct {
     int32_t k;
     int32_t pos[2];
     int32_t gate;
     int64_t mat;
+    int32_t flags;
+    int32_t run;
+    int32_t run_pos[4];
+    int32_t lpos[2];
 } qgb_traj_op;
 
 int qgb_abi_version(void);

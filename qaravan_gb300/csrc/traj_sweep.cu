@@ -67,15 +67,83 @@ template <typename T> __device__ __forceinline__ uint32_t tswz(uint32_t e);
 template <> __device__ __forceinline__ uint32_t tswz<float>(uint32_t e) { return swz<float>(e); }
 template <> __device__ __forceinline__ uint32_t tswz<double>(uint32_t e) { return swz<double>(e); }
 
-// Amplitude damping of the site at matrix bit `bit` of a group of D amplitudes
-// in registers: W += weight of the |1> components; then K0 (mode 1) or the
-// jump sc * K1 (mode 2).
-template <int D, typename C, typename T>
-__device__ __forceinline__ void traj_damp(C (&v)[D], int bit, int mode, T s0, T sj, float& w) {
+// ---- ops on a register group ------------------------------------------------
+// A run of consecutive ops whose sites lie within R tile bits is applied to
+// groups of 2^R amplitudes held in registers: local index bit P <-> the run's
+// tile position run_pos[P]. Positions are runtime values; each (width,
+// positions) case is its own fully unrolled instance, chosen by a switch, so
+// the group never leaves registers.
+
+template <typename C> __device__ __forceinline__ C cmul(const C& a, const C& b) {
+    C r;
+    r.x = a.x * b.x - a.y * b.y;
+    r.y = a.x * b.y + a.y * b.x;
+    return r;
+}
+
+template <int R, int P, typename C>
+__device__ __forceinline__ void reg_op1(C (&v)[1 << R], const C* __restrict__ m, bool diag) {
+    constexpr int D = 1 << R, bit = 1 << P;
+    const C m00 = m[0], m01 = m[1], m10 = m[2], m11 = m[3];
+    if (diag) {
+#pragma unroll
+        for (int c = 0; c < D; ++c) v[c] = cmul(v[c], (c & bit) ? m11 : m00);
+        return;
+    }
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+        if (c & bit) continue;
+        const C a = v[c], b = v[c | bit];
+        C x = cmul(m00, a), y = cmul(m10, a);
+        cfma(x, m01, b);
+        cfma(y, m11, b);
+        v[c] = x;
+        v[c | bit] = y;
+    }
+}
+
+// matrix index bit 1 (most significant) <-> local position P0 (the op's first site), bit 0 <-> P1
+template <int R, int P0, int P1, typename C>
+__device__ __forceinline__ void reg_op2(C (&v)[1 << R], const C* __restrict__ m, bool diag) {
+    constexpr int D = 1 << R, b0 = 1 << P0, b1 = 1 << P1;
+    if (diag) {
+        const C d0 = m[0], d1 = m[5], d2 = m[10], d3 = m[15];
+#pragma unroll
+        for (int c = 0; c < D; ++c) v[c] = cmul(v[c], (c & b0) ? ((c & b1) ? d3 : d2) : ((c & b1) ? d1 : d0));
+        return;
+    }
+    C mm[16];
+#pragma unroll
+    for (int e = 0; e < 16; ++e) mm[e] = m[e];
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+        if ((c & b0) || (c & b1)) continue;
+        const C x[4] = {v[c], v[c | b1], v[c | b0], v[c | b0 | b1]};
+        C y[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            y[r] = cmul(mm[4 * r], x[0]);
+#pragma unroll
+            for (int k = 1; k < 4; ++k) cfma(y[r], mm[4 * r + k], x[k]);
+        }
+        v[c] = y[0];
+        v[c | b1] = y[1];
+        v[c | b0] = y[2];
+        v[c | b0 | b1] = y[3];
+    }
+}
+
+// Amplitude damping of the site at local position P: w += weight of its |1>
+// components; then K0 (mode 1: |1> components times s0) or the jump (mode 2:
+// the |1> components times sj move to |0>, |1> cleared).
+template <int R, int P, typename C, typename T>
+__device__ __forceinline__ void reg_damp(C (&v)[1 << R], int mode, T s0, T sj, T& w) {
+    constexpr int D = 1 << R, bit = 1 << P;
 #pragma unroll
     for (int c = 0; c < D; ++c) {
         if (!(c & bit)) continue;
-        w += float(v[c].x) * float(v[c].x) + float(v[c].y) * float(v[c].y);
+        w = fma(v[c].x, v[c].x, w);
+        w = fma(v[c].y, v[c].y, w);
         if (mode == 1) {
             v[c].x *= s0;
             v[c].y *= s0;
@@ -88,96 +156,169 @@ __device__ __forceinline__ void traj_damp(C (&v)[D], int bit, int mode, T s0, T 
     }
 }
 
-// One op (gate with the sampled Paulis folded into its rows, then amplitude
-// damping of each site) on every group of a staged tile.
-template <typename T, int K>
-__device__ __forceinline__ void traj_tile_op(cplx<T>* __restrict__ tile, int m, const TrajOpDesc& op,
-                                             const cplx<T>* __restrict__ mat, T prescale, const uint8_t* pk,
-                                             const int* dmode, const T* djump, T s0, double* chw, int tid,
-                                             int nthr) {
-    using C = cplx<T>;
-    constexpr int D = 1 << K;
-    C M[D * D];
-#pragma unroll
-    for (int i = 0; i < D * D; ++i) {
-        const C e = __ldg(&mat[i]);
-        M[i] = mk<T>(e.x * prescale, e.y * prescale);
+template <int R, typename C>
+__device__ __forceinline__ void reg_apply1(C (&v)[1 << R], int P, const C* m, bool diag) {
+    switch (P) {
+        case 0: reg_op1<R, 0>(v, m, diag); break;
+        case 1: if constexpr (R > 1) reg_op1<R, 1>(v, m, diag); break;
+        case 2: if constexpr (R > 2) reg_op1<R, 2>(v, m, diag); break;
+        case 3: if constexpr (R > 3) reg_op1<R, 3>(v, m, diag); break;
     }
-    // Paulis after the gate: rows r and r ^ bit of site j (X swaps, Y swaps with -i / i, Z negates the |1> row)
+}
+
+template <int R, int CODE, typename C>
+__device__ __forceinline__ void reg_apply2_case(C (&v)[1 << R], const C* m, bool diag) {
+    constexpr int P0 = CODE / 4, P1 = CODE % 4;
+    if constexpr (P0 < R && P1 < R && P0 != P1) reg_op2<R, P0, P1>(v, m, diag);
+}
+
+template <int R, typename C>
+__device__ __forceinline__ void reg_apply2(C (&v)[1 << R], int P0, int P1, const C* m, bool diag) {
+    switch (P0 * 4 + P1) {
+        case 1: reg_apply2_case<R, 1>(v, m, diag); break;
+        case 2: reg_apply2_case<R, 2>(v, m, diag); break;
+        case 3: reg_apply2_case<R, 3>(v, m, diag); break;
+        case 4: reg_apply2_case<R, 4>(v, m, diag); break;
+        case 6: reg_apply2_case<R, 6>(v, m, diag); break;
+        case 7: reg_apply2_case<R, 7>(v, m, diag); break;
+        case 8: reg_apply2_case<R, 8>(v, m, diag); break;
+        case 9: reg_apply2_case<R, 9>(v, m, diag); break;
+        case 11: reg_apply2_case<R, 11>(v, m, diag); break;
+        case 12: reg_apply2_case<R, 12>(v, m, diag); break;
+        case 13: reg_apply2_case<R, 13>(v, m, diag); break;
+        case 14: reg_apply2_case<R, 14>(v, m, diag); break;
+    }
+}
+
+template <int R, typename C, typename T>
+__device__ __forceinline__ void reg_damp_at(C (&v)[1 << R], int P, int mode, T s0, T sj, T& w) {
+    switch (P) {
+        case 0: reg_damp<R, 0>(v, mode, s0, sj, w); break;
+        case 1: if constexpr (R > 1) reg_damp<R, 1>(v, mode, s0, sj, w); break;
+        case 2: if constexpr (R > 2) reg_damp<R, 2>(v, mode, s0, sj, w); break;
+        case 3: if constexpr (R > 3) reg_damp<R, 3>(v, mode, s0, sj, w); break;
+    }
+}
+
+// Per-sweep, per-trajectory state in dynamic shared memory.
+template <typename T> struct TrajSweepSmem {
+    cplx<T>* msh;     // [op][16]: the op's matrix with its sampled Paulis folded in (first op: times the prescale)
+    double* chw_w;    // [warp][2 * kTrajMaxOps]: per-warp weights of |1> before each damping, summed in order
+    T* djump;         // [op][2]: jump factor sqrt(gamma) / sqrt(gamma W) where a jump is replayed
+    uint8_t* dmode;   // [op][2]: 0 none, 1 K0, 2 jump
+    uint8_t* dflag;   // [op]: the folded matrix is diagonal
+};
+
+// Every run of a sweep on one staged tile; G groups of 2^R amplitudes per
+// thread at a time, a barrier after each run.
+template <typename T, int R, int G>
+__device__ __forceinline__ void traj_tile_runs(cplx<T>* __restrict__ tile, int m, const TrajOpDesc* __restrict__ ops,
+                                               int nops, const TrajSweepSmem<T>& sm, bool damp, T s0, int tid,
+                                               int nthr) {
+    using C = cplx<T>;
+    constexpr int D = 1 << R;
+    const int warp = tid >> 5, lane = tid & 31;
+    double* myw = sm.chw_w + size_t(warp) * (2 * kTrajMaxOps);
+    for (int i0 = 0; i0 < nops;) {
+        const int nr = ops[i0].run;
+        int rp[R], srt[R];
 #pragma unroll
-    for (int j = 0; j < K; ++j) {
-        const int p = pk[j];
-        if (p == 0) continue;
-        const int bit = 1 << (K - 1 - j);
+        for (int j = 0; j < R; ++j) rp[j] = srt[j] = ops[i0].run_pos[j];
 #pragma unroll
-        for (int r = 0; r < D; ++r) {
-            if (r & bit) continue;
+        for (int x = 1; x < R; ++x)
 #pragma unroll
-            for (int c = 0; c < D; ++c) {
-                const C lo = M[r * D + c], hi = M[(r | bit) * D + c];
-                if (p == 1) {
-                    M[r * D + c] = hi;
-                    M[(r | bit) * D + c] = lo;
-                } else if (p == 2) {
-                    M[r * D + c] = mk<T>(hi.y, -hi.x);
-                    M[(r | bit) * D + c] = mk<T>(-lo.y, lo.x);
-                } else {
-                    M[(r | bit) * D + c] = mk<T>(-hi.x, -hi.y);
+            for (int y = x; y > 0; --y)
+                if (srt[y - 1] > srt[y]) {
+                    const int t = srt[y];
+                    srt[y] = srt[y - 1];
+                    srt[y - 1] = t;
+                }
+        uint32_t soff[D];
+#pragma unroll
+        for (int l = 0; l < D; ++l) {
+            uint32_t o = 0;
+#pragma unroll
+            for (int j = 0; j < R; ++j) o |= uint32_t((l >> j) & 1) << rp[j];
+            soff[l] = tswz<T>(o);
+        }
+        const uint32_t groups = 1u << (m - R);
+        for (uint32_t gb = 0; gb < groups; gb += uint32_t(G * nthr)) {
+            C v[G][D];
+            uint32_t sb[G];
+            bool ok[G];
+#pragma unroll
+            for (int gi = 0; gi < G; ++gi) {
+                const uint32_t g = gb + uint32_t(gi * nthr + tid);
+                ok[gi] = g < groups;
+                uint32_t base = ok[gi] ? g : 0u;
+#pragma unroll
+                for (int j = 0; j < R; ++j)
+                    base = ((base >> srt[j]) << (srt[j] + 1)) | (base & ((1u << srt[j]) - 1));
+                sb[gi] = tswz<T>(base);
+#pragma unroll
+                for (int l = 0; l < D; ++l) v[gi][l] = ok[gi] ? tile[sb[gi] ^ soff[l]] : mk<T>(T(0), T(0));
+            }
+            for (int q = 0; q < nr; ++q) {
+                const int i = i0 + q;
+                const int k = ops[i].k, p0 = ops[i].lpos[0], p1 = ops[i].lpos[1];
+                const C* mm = sm.msh + size_t(i) * 16;
+                const bool dg = sm.dflag[i] != 0;
+                T w0 = T(0), w1 = T(0);  // the state's precision: the jump and renormalisation factors come from these
+#pragma unroll
+                for (int gi = 0; gi < G; ++gi) {
+                    if (k == 1) reg_apply1<R>(v[gi], p0, mm, dg);
+                    else reg_apply2<R>(v[gi], p0, p1, mm, dg);
+                }
+                if (damp) {
+                    const int d0 = sm.dmode[2 * i], d1 = sm.dmode[2 * i + 1];
+                    const T j0 = sm.djump[2 * i], j1 = sm.djump[2 * i + 1];
+#pragma unroll
+                    for (int gi = 0; gi < G; ++gi) {
+                        reg_damp_at<R>(v[gi], p0, d0, s0, j0, w0);
+                        if (k == 2) reg_damp_at<R>(v[gi], p1, d1, s0, j1, w1);
+                    }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) {
+                        w0 += __shfl_xor_sync(0xffffffffu, w0, o);
+                        w1 += __shfl_xor_sync(0xffffffffu, w1, o);
+                    }
+                    if (lane == 0) {
+                        myw[2 * i] += double(w0);
+                        myw[2 * i + 1] += double(w1);
+                    }
                 }
             }
+#pragma unroll
+            for (int gi = 0; gi < G; ++gi)
+                if (ok[gi])
+#pragma unroll
+                    for (int l = 0; l < D; ++l) tile[sb[gi] ^ soff[l]] = v[gi][l];
         }
+        __syncthreads();
+        i0 += nr;
     }
-    int pos[K], srt[K];
-#pragma unroll
-    for (int j = 0; j < K; ++j) pos[j] = srt[j] = op.pos[j];
-    if (K == 2 && srt[0] > srt[1]) {
-        const int x = srt[0];
-        srt[0] = srt[1];
-        srt[1] = x;
+}
+
+template <typename T, int RMAX>
+__device__ __forceinline__ void traj_tile_dispatch(cplx<T>* tile, int m, const TrajOpDesc* ops, int nops,
+                                                   const TrajSweepSmem<T>& sm, bool damp, T s0, int tid, int nthr) {
+    const int R = m < RMAX ? m : RMAX;
+    switch (R) {
+        case 1: traj_tile_runs<T, 1, 2>(tile, m, ops, nops, sm, damp, s0, tid, nthr); break;
+        case 2: traj_tile_runs<T, 2, 2>(tile, m, ops, nops, sm, damp, s0, tid, nthr); break;
+        case 3: traj_tile_runs<T, 3, 2>(tile, m, ops, nops, sm, damp, s0, tid, nthr); break;
+        default: if constexpr (RMAX >= 4) traj_tile_runs<T, 4, 2>(tile, m, ops, nops, sm, damp, s0, tid, nthr); break;
     }
-    uint32_t soff[D];
-#pragma unroll
-    for (int c = 0; c < D; ++c) {
-        uint32_t o = 0;
-#pragma unroll
-        for (int j = 0; j < K; ++j) o |= uint32_t((c >> (K - 1 - j)) & 1) << pos[j];
-        soff[c] = tswz<T>(o);
-    }
-    float w[K];
-#pragma unroll
-    for (int j = 0; j < K; ++j) w[j] = 0.f;
-    const uint32_t groups = 1u << (m - K);
-    for (uint32_t g = tid; g < groups; g += nthr) {
-        uint32_t base = g;
-#pragma unroll
-        for (int j = 0; j < K; ++j) base = ((base >> srt[j]) << (srt[j] + 1)) | (base & ((1u << srt[j]) - 1));
-        const uint32_t sb = tswz<T>(base);
-        C v[D], o[D];
-#pragma unroll
-        for (int c = 0; c < D; ++c) v[c] = tile[sb ^ soff[c]];
-#pragma unroll
-        for (int r = 0; r < D; ++r) {
-            C acc = mk<T>(0, 0);
-#pragma unroll
-            for (int c = 0; c < D; ++c) cfma(acc, M[r * D + c], v[c]);
-            o[r] = acc;
-        }
-#pragma unroll
-        for (int j = 0; j < K; ++j)
-            if (dmode[j]) traj_damp<D>(o, 1 << (K - 1 - j), dmode[j], s0, djump[j], w[j]);
-#pragma unroll
-        for (int c = 0; c < D; ++c) tile[sb ^ soff[c]] = o[c];
-    }
-    if (chw) {
-        // the sites' weights: warp sums, one shared-memory atomic per warp and site
-#pragma unroll
-        for (int j = 0; j < K; ++j) {
-            float x = w[j];
-#pragma unroll
-            for (int s = 16; s > 0; s >>= 1) x += __shfl_down_sync(0xffffffffu, x, s);
-            if ((tid & 31) == 0 && dmode[j]) atomicAdd(&chw[j], double(x));
-        }
-    }
+}
+
+template <typename T> constexpr int traj_rmax() { return sizeof(T) == 4 ? 4 : 3; }
+
+// dynamic shared memory: tile buffers | high-bit offsets | folded matrices | per-warp weights | jump factors |
+// damping modes | diagonal flags
+template <typename T> __host__ __device__ constexpr size_t traj_aux_bytes() {
+    return sizeof(uint32_t) * (size_t(1) << QGB_SWEEP_MAX_HIGH) + sizeof(cplx<T>) * kTrajMaxOps * 16 +
+           sizeof(double) * (kTrajThreads / 32) * 2 * kTrajMaxOps + sizeof(T) * 2 * kTrajMaxOps + 2 * kTrajMaxOps +
+           kTrajMaxOps;
 }
 
 template <typename T>
@@ -192,18 +333,24 @@ __global__ void __launch_bounds__(kTrajThreads) traj_run_kernel(cplx<T>* __restr
     extern __shared__ __align__(16) unsigned char traj_smem[];
     C* bufs = reinterpret_cast<C*>(traj_smem);
     uint32_t* hoff = reinterpret_cast<uint32_t*>(bufs + (size_t(a.nbuf) << a.mmax));
-    __shared__ double chw[2 * kTrajMaxOps];        // per (op, site) of the sweep: weight of |1> before damping
-    __shared__ uint8_t pk[kTrajMaxOps][2];          // sampled Paulis
+    TrajSweepSmem<T> sm;
+    sm.msh = reinterpret_cast<C*>(hoff + (size_t(1) << QGB_SWEEP_MAX_HIGH));
+    sm.chw_w = reinterpret_cast<double*>(sm.msh + kTrajMaxOps * 16);
+    sm.djump = reinterpret_cast<T*>(sm.chw_w + (kTrajThreads / 32) * 2 * kTrajMaxOps);
+    sm.dmode = reinterpret_cast<uint8_t*>(sm.djump + 2 * kTrajMaxOps);
+    sm.dflag = sm.dmode + 2 * kTrajMaxOps;
+    __shared__ double chw[2 * kTrajMaxOps];  // per (op, site): weight of |1> before damping, summed over the tiles
+    __shared__ uint8_t pk[kTrajMaxOps][2];   // sampled Paulis
     __shared__ int jop[kTrajMaxJumps], jsite[kTrajMaxJumps];
     __shared__ double jscale[kTrajMaxJumps];
     __shared__ int s_traj, s_njump, s_replay;
     __shared__ double s_r, s_prescale;
     __shared__ int s_jumps_total;
-    const int tid = threadIdx.x, nthr = blockDim.x;
+    const int tid = threadIdx.x, nthr = blockDim.x, nwarps = blockDim.x >> 5;
     const uint64_t dim = uint64_t(1) << a.n;
     C* scratch = pingpong + uint64_t(blockIdx.x) * dim;
     const T s0 = T(sqrt(1.0 - a.gamma));
-    const T sqg = T(sqrt(a.gamma));
+    const bool damp = a.gamma > 0;
     constexpr uint32_t per16 = 16 / sizeof(C);
     while (true) {
         if (tid == 0) {
@@ -221,6 +368,7 @@ __global__ void __launch_bounds__(kTrajThreads) traj_run_kernel(cplx<T>* __restr
         for (int s = 0; s < a.nsweeps; ++s) {
             const TrajSweepDesc sw = sweeps[s];
             const int L = sw.L, H = sw.H, m = L + H, nops = sw.op_end - sw.op_begin;
+            const TrajOpDesc* sops = ops + sw.op_begin;
             const uint32_t lmask = (1u << L) - 1u;
             // tile-index -> global offset of the high bits; the outer bits enumerate tiles
             for (uint32_t h = tid; h < (1u << H); h += nthr) {
@@ -239,15 +387,51 @@ __global__ void __launch_bounds__(kTrajThreads) traj_run_kernel(cplx<T>* __restr
             // the Paulis of the sweep's channels (state independent, the gate-by-gate kernel's counters)
             for (int c = tid; c < 2 * nops; c += nthr) {
                 const int i = c >> 1, j = c & 1;
-                const TrajOpDesc& op = ops[sw.op_begin + i];
                 int p = 0;
-                if (a.p_dep > 0 && j < op.k) {
-                    const double u = Philox::uniform(uint32_t(op.gate), uint32_t(t), 2u * j, a.seed0, a.seed1);
+                if (a.p_dep > 0 && j < sops[i].k) {
+                    const double u = Philox::uniform(uint32_t(sops[i].gate), uint32_t(t), 2u * j, a.seed0, a.seed1);
                     if (u >= 1.0 - a.p_dep) p = 1 + min(2, int((u - (1.0 - a.p_dep)) / (a.p_dep / 3.0)));
                 }
                 pk[i][j] = uint8_t(p);
             }
             if (tid == 0) s_njump = 0;
+            __syncthreads();
+            // each op's matrix with its Paulis folded into the rows (X swaps, Y swaps with -i / i, Z negates
+            // the |1> row of its site); the first op of the sweep also carries the prescale 1 / sqrt(N_end)
+            for (int i = tid; i < nops; i += nthr) {
+                const TrajOpDesc& op = sops[i];
+                const int D = 1 << op.k;
+                C M[16];
+                const T ps = i == 0 ? T(s_prescale) : T(1);
+                for (int e = 0; e < D * D; ++e) {
+                    const C x = mats[op.mat + e];
+                    M[e] = mk<T>(x.x * ps, x.y * ps);
+                }
+                bool diag = (op.flags & 1) != 0;
+                for (int j = 0; j < op.k; ++j) {
+                    const int pj = pk[i][j];
+                    if (pj == 0) continue;
+                    if (pj != 3) diag = false;
+                    const int bit = 1 << (op.k - 1 - j);
+                    for (int r = 0; r < D; ++r) {
+                        if (r & bit) continue;
+                        for (int c = 0; c < D; ++c) {
+                            const C lo = M[r * D + c], hi = M[(r | bit) * D + c];
+                            if (pj == 1) {
+                                M[r * D + c] = hi;
+                                M[(r | bit) * D + c] = lo;
+                            } else if (pj == 2) {
+                                M[r * D + c] = mk<T>(hi.y, -hi.x);
+                                M[(r | bit) * D + c] = mk<T>(-lo.y, lo.x);
+                            } else {
+                                M[(r | bit) * D + c] = mk<T>(-hi.x, -hi.y);
+                            }
+                        }
+                    }
+                }
+                for (int e = 0; e < D * D; ++e) sm.msh[size_t(i) * 16 + e] = M[e];
+                sm.dflag[i] = diag ? 1 : 0;
+            }
             const uint64_t tiles = uint64_t(1) << (a.n - m);
             auto base_of = [&](uint64_t w) -> uint32_t {
                 uint32_t b = 0;
@@ -268,10 +452,20 @@ __global__ void __launch_bounds__(kTrajThreads) traj_run_kernel(cplx<T>* __restr
                 asm volatile("cp.async.commit_group;" ::: "memory");
             };
             for (int pass = 0; pass <= kTrajMaxJumps; ++pass) {
-                for (int c = tid; c < 2 * nops; c += nthr) chw[c] = 0.0;
+                // damping of every (op, site): K0, or the replayed jumps of this sweep
+                for (int c = tid; c < 2 * nops; c += nthr) {
+                    sm.dmode[c] = damp ? 1 : 0;
+                    sm.djump[c] = T(0);
+                }
+                for (int c = tid; c < nwarps * 2 * nops; c += nthr)
+                    sm.chw_w[size_t(c / (2 * nops)) * (2 * kTrajMaxOps) + (c % (2 * nops))] = 0.0;
                 __syncthreads();
-                const T pre = T(s_prescale);
-                const int njump = s_njump;
+                if (tid == 0)
+                    for (int q = 0; q < s_njump; ++q) {
+                        sm.dmode[2 * jop[q] + jsite[q]] = 2;
+                        sm.djump[2 * jop[q] + jsite[q]] = T(sqrt(a.gamma) * jscale[q]);
+                    }
+                __syncthreads();
                 load(0, bufs);
                 for (uint64_t w = 0; w < tiles; ++w) {
                     C* cur = bufs + (size_t(a.nbuf == 2 ? (w & 1) : 0) << m);
@@ -282,24 +476,7 @@ __global__ void __launch_bounds__(kTrajThreads) traj_run_kernel(cplx<T>* __restr
                         asm volatile("cp.async.wait_group 0;" ::: "memory");
                     }
                     __syncthreads();
-                    int jn = 0;  // next recorded jump of this pass
-                    for (int i = 0; i < nops; ++i) {
-                        const TrajOpDesc op = ops[sw.op_begin + i];
-                        int dm[2] = {a.gamma > 0 ? 1 : 0, a.gamma > 0 ? 1 : 0};
-                        T dj[2] = {T(0), T(0)};
-                        while (jn < njump && jop[jn] == i) {
-                            dm[jsite[jn]] = 2;
-                            dj[jsite[jn]] = T(double(sqg) * jscale[jn]);
-                            ++jn;
-                        }
-                        const T ps = i == 0 ? pre : T(1);
-                        double* cw = a.gamma > 0 ? &chw[2 * i] : nullptr;
-                        if (op.k == 1)
-                            traj_tile_op<T, 1>(cur, m, op, mats + op.mat, ps, pk[i], dm, dj, s0, cw, tid, nthr);
-                        else
-                            traj_tile_op<T, 2>(cur, m, op, mats + op.mat, ps, pk[i], dm, dj, s0, cw, tid, nthr);
-                        __syncthreads();
-                    }
+                    traj_tile_dispatch<T, traj_rmax<T>()>(cur, m, sops, nops, sm, damp, s0, tid, nthr);
                     const uint32_t base = base_of(w);
                     for (uint32_t e = per16 * tid; e < (1u << m); e += per16 * nthr)
                         *reinterpret_cast<float4*>(dst + (base + hoff[e >> L] + (e & lmask))) =
@@ -307,11 +484,18 @@ __global__ void __launch_bounds__(kTrajThreads) traj_run_kernel(cplx<T>* __restr
                     __syncthreads();  // the buffer is free for the copy issued two tiles later
                     if (a.nbuf == 1 && w + 1 < tiles) load(w + 1, bufs);
                 }
+                // the weights, summed over the warps in a fixed order
+                for (int c = tid; c < 2 * nops; c += nthr) {
+                    double x = 0.0;
+                    for (int wp = 0; wp < nwarps; ++wp) x += sm.chw_w[size_t(wp) * (2 * kTrajMaxOps) + c];
+                    chw[c] = x;
+                }
+                __syncthreads();
                 // the sweep's channels in order: where does the no-jump norm fall below the threshold?
                 if (tid == 0) {
                     s_replay = 0;
                     double N = 1.0;
-                    if (a.gamma > 0) {
+                    if (damp) {
                         // channels up to the last jump recorded in this sweep are decided; after it the
                         // replay renormalised the state, so the walk restarts there with N = 1
                         int i0 = 0, j0 = 0;
@@ -320,7 +504,7 @@ __global__ void __launch_bounds__(kTrajThreads) traj_run_kernel(cplx<T>* __restr
                             j0 = jsite[s_njump - 1] + 1;
                         }
                         for (int i = i0; i < nops && !s_replay; ++i) {
-                            const int k = ops[sw.op_begin + i].k;
+                            const int k = sops[i].k;
                             for (int j = (i == i0 ? j0 : 0); j < k; ++j) {
                                 const double Wc = chw[2 * i + j];
                                 const double Nn = N - a.gamma * Wc;
@@ -336,7 +520,7 @@ __global__ void __launch_bounds__(kTrajThreads) traj_run_kernel(cplx<T>* __restr
                                     ++s_njump;
                                     const int idx = s_jumps_total++;
                                     if (idx < a.max_log && jump_log) {
-                                        jump_log[(t * a.max_log + idx) * 2] = ops[sw.op_begin + i].gate;
+                                        jump_log[(t * a.max_log + idx) * 2] = sops[i].gate;
                                         jump_log[(t * a.max_log + idx) * 2 + 1] = j;
                                     }
                                     s_r = Philox::uniform4(uint32_t(idx + 1), uint32_t(t), 0u, 2u, a.seed0, a.seed1);
@@ -361,10 +545,9 @@ __global__ void __launch_bounds__(kTrajThreads) traj_run_kernel(cplx<T>* __restr
         // the normalised state into the trajectory's slot
         {
             const T sc = T(s_prescale);
-            const C* from = src ? src : nullptr;
-            if (from) {
+            if (src) {
                 for (uint64_t e = tid; e < dim; e += nthr) {
-                    const C v = from[e];
+                    const C v = src[e];
                     own[e] = mk<T>(v.x * sc, v.y * sc);
                 }
             } else {
@@ -385,7 +568,8 @@ namespace {
 
 template <typename T>
 size_t traj_smem_bytes(int mmax, int hmax, int nbuf) {
-    return sizeof(cplx<T>) * (size_t(nbuf) << mmax) + sizeof(uint32_t) * (size_t(1) << hmax);
+    (void)hmax;
+    return sizeof(cplx<T>) * (size_t(nbuf) << mmax) + traj_aux_bytes<T>();
 }
 
 template <typename T>
@@ -434,11 +618,32 @@ int traj_check_tables(int n, const TrajSweepDesc* sweeps, int nsweeps, const Tra
             return set_error(QGB_EINVAL, "sweep %d: op range [%d, %d) invalid", s, sw.op_begin, sw.op_end);
         if (m > *mmax) *mmax = m;
         if (sw.H > *hmax) *hmax = sw.H;
+        const int R = m < (dtype == QGB_C64 ? 4 : 3) ? m : (dtype == QGB_C64 ? 4 : 3);
+        int run_left = 0;
+        const int32_t* rpos = nullptr;
         for (int i = sw.op_begin; i < sw.op_end; ++i) {
             const TrajOpDesc& op = ops[i];
+            if (run_left == 0) {
+                if (op.run < 1 || i + op.run > sw.op_end)
+                    return set_error(QGB_EINVAL, "op %d: run length %d invalid in its sweep", i, op.run);
+                uint32_t seen = 0;
+                for (int j = 0; j < R; ++j) {
+                    const int p = op.run_pos[j];
+                    if (p < 0 || p >= m || ((seen >> p) & 1u)) return set_error(QGB_EINVAL, "op %d: run positions invalid", i);
+                    seen |= 1u << p;
+                }
+                run_left = op.run;
+                rpos = op.run_pos;
+            } else if (op.run != 0) {
+                return set_error(QGB_EINVAL, "op %d opens a run inside another run", i);
+            }
+            --run_left;
             if (op.k < 1 || op.k > 2 || op.k > m) return set_error(QGB_EINVAL, "op %d: width %d invalid", i, op.k);
-            for (int j = 0; j < op.k; ++j)
+            for (int j = 0; j < op.k; ++j) {
                 if (op.pos[j] < 0 || op.pos[j] >= m) return set_error(QGB_EINVAL, "op %d: tile position out of range", i);
+                if (op.lpos[j] < 0 || op.lpos[j] >= R || rpos[op.lpos[j]] != op.pos[j])
+                    return set_error(QGB_EINVAL, "op %d: local position does not match its run", i);
+            }
             if (op.k == 2 && op.pos[0] == op.pos[1]) return set_error(QGB_EINVAL, "op %d: repeated tile position", i);
             if (op.gate < 0 || op.mat < 0 || op.mat + (int64_t(1) << (2 * op.k)) > mat_elems)
                 return set_error(QGB_EINVAL, "op %d: gate index or matrix offset out of range", i);

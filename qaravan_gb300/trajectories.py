@@ -44,7 +44,8 @@ from .statevector import _to_np, circuit_ops, pauli_expectations
 
 TRAJ_SWEEP = np.dtype([("L", "<i4"), ("H", "<i4"), ("high_bits", "<i4", (10,)), ("op_begin", "<i4"),
                        ("op_end", "<i4")])
-TRAJ_OP = np.dtype([("k", "<i4"), ("pos", "<i4", (2,)), ("gate", "<i4"), ("mat", "<i8")])
+TRAJ_OP = np.dtype([("k", "<i4"), ("pos", "<i4", (2,)), ("gate", "<i4"), ("mat", "<i8"), ("flags", "<i4"),
+                    ("run", "<i4"), ("run_pos", "<i4", (4,)), ("lpos", "<i4", (2,))])
 TRAJ_MAX_OPS = 128
 
 
@@ -102,6 +103,34 @@ def plan_traj_sweeps(gate_bits, nbits, tile_bits, low_min, max_ops=TRAJ_MAX_OPS,
         done = set(taken)
         remaining = [g for g in remaining if g not in done]
     return sweeps
+
+
+class _TileOp:
+    def __init__(self, bits):
+        self.bits = list(bits)
+
+
+def plan_runs(tile_pos, m, rmax):
+    """Group a sweep's gates (their tile positions, in order) into runs over
+    ``R = min(rmax, m)`` tile bits that the kernel applies to register-resident
+    groups of 2^R amplitudes: the fusion rule of the compiler (a gate joins the
+    latest run it depends on while the union stays within R bits; earlier runs
+    it covers and that nothing in between touches are absorbed), so gates move
+    only past gates on other bits. Returns ``[(run bits padded to R, [gate
+    positions in the list, application order])]``."""
+    from .compiler import fuse_symbolic
+    R = min(rmax, m)
+    blocks = fuse_symbolic([_TileOp(p) for p in tile_pos], R)
+    runs = []
+    for b in blocks:
+        bits = sorted(b.bits)
+        for x in range(m):  # pad with unused tile bits: every run spans exactly R bits
+            if len(bits) >= R:
+                break
+            if x not in bits:
+                bits.append(x)
+        runs.append((bits, list(b.ops)))
+    return runs
 
 
 class TrajectorySim:
@@ -169,21 +198,35 @@ class TrajectorySim:
         plan = plan_traj_sweeps(bits, n, self.tile_bits, low_min) if self.gates else []
         sw = np.zeros(len(plan), dtype=TRAJ_SWEEP)
         ops = np.zeros(max(len(self.gates), 1), dtype=TRAJ_OP)
+        rmax = 4 if isz == 8 else 3
+        diag = [bool(np.all(np.asarray(_to_np(g.matrix)) == np.diag(np.diag(_to_np(g.matrix))))) for g in self.gates]
         o = 0
         for s_i, (Lb, high, taken) in enumerate(plan):
             tpos = {b: b for b in range(Lb)}
             for h, b in enumerate(high):
                 tpos[b] = Lb + h
+            m = Lb + len(high)
             sw[s_i]["L"], sw[s_i]["H"] = Lb, len(high)
             sw[s_i]["high_bits"][:len(high)] = high
             sw[s_i]["op_begin"] = o
-            for gi in taken:
-                ops[o]["k"] = len(bits[gi])
-                ops[o]["pos"][:len(bits[gi])] = [tpos[b] for b in bits[gi]]
-                ops[o]["gate"] = gi
-                ops[o]["mat"] = self.offs[gi]
-                o += 1
+            order = []
+            for rbits, members in plan_runs([[tpos[b] for b in bits[gi]] for gi in taken], m, rmax):
+                for q, mi in enumerate(members):
+                    gi = taken[mi]
+                    p = [tpos[b] for b in bits[gi]]
+                    ops[o]["k"] = len(p)
+                    ops[o]["pos"][:len(p)] = p
+                    ops[o]["gate"] = gi
+                    ops[o]["mat"] = self.offs[gi]
+                    ops[o]["flags"] = 1 if diag[gi] else 0
+                    if q == 0:
+                        ops[o]["run"] = len(members)
+                        ops[o]["run_pos"][:len(rbits)] = rbits
+                    ops[o]["lpos"][:len(p)] = [rbits.index(x) for x in p]
+                    order.append(gi)
+                    o += 1
             sw[s_i]["op_end"] = o
+            plan[s_i] = (Lb, high, order)  # the gates in the order the kernel applies them
         self.sweep_plan = plan
         self._sweeps_host = np.ascontiguousarray(sw)
         self._sweeps_dev = torch.from_numpy(sw.view(np.uint8).copy()).to(self.device)

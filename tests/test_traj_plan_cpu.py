@@ -89,3 +89,44 @@ def test_choose_tunes_on_first_sight_only_when_enabled(tmp_path, monkeypatch):
     assert autotune.choose_traj(20, torch.complex64) == 11
     assert autotune.choose_traj(20, torch.complex64) == 11  # cached: measured once
     assert calls == [20]
+
+
+@pytest.mark.parametrize("m,rmax", [(13, 4), (12, 3), (3, 4), (2, 3), (1, 4)])
+def test_runs_cover_every_gate_within_r_bits_in_a_valid_order(m, rmax):
+    from qaravan_gb300.trajectories import plan_runs
+    rng = np.random.default_rng(m * 10 + rmax)
+    pos = []
+    for _ in range(60):
+        if m >= 2 and rng.random() < 0.5:
+            a, b = rng.choice(m, size=2, replace=False)
+            pos.append([int(a), int(b)])
+        else:
+            pos.append([int(rng.integers(m))])
+    runs = plan_runs(pos, m, rmax)
+    R = min(rmax, m)
+    order = [i for _, members in runs for i in members]
+    assert sorted(order) == list(range(len(pos)))
+    where = {i: k for k, i in enumerate(order)}
+    for bits, members in runs:
+        assert len(bits) == R and len(set(bits)) == R and all(0 <= b < m for b in bits)
+        for i in members:
+            assert set(pos[i]) <= set(bits)
+    for a in range(len(pos)):
+        for b in range(a + 1, len(pos)):
+            if set(pos[a]) & set(pos[b]):
+                assert where[a] < where[b]
+
+
+def test_tfi_runs_hold_several_gates():
+    from qaravan_gb300.trajectories import plan_runs
+    n = 20
+    gl = workloads.tfi_trotter_circuit(n, 0.05, 4).gate_list
+    bits = [[n - 1 - int(q) for q in g.indices] for g in gl]
+    plan = plan_traj_sweeps(bits, n, 13, 5)
+    nruns = 0
+    for L, high, taken in plan:
+        tpos = {b: b for b in range(L)}
+        for h, b in enumerate(high):
+            tpos[b] = L + h
+        nruns += len(plan_runs([[tpos[b] for b in bits[g]] for g in taken], L + len(high), 4))
+    assert nruns * 2.5 < len(gl)  # several gates per shared-memory pass
