@@ -881,6 +881,35 @@ def reference_arm(args):
                                      "d2h_bytes_per_step": 0}}), flush=True)
 
 
+def _time_traj_gates(sim):
+    """Per-gate mode: one run with CUDA events around every gate's launches on the launching
+    stream: a list of (gate index, union bits, lowest union bit, ms). The
+    union is the gate's sites plus the previous gate's (pending damping)."""
+    import torch
+    from qaravan_gb300 import _lib
+    L = _lib.lib()
+    n, T = sim.n, sim.ntraj
+    code = _lib.dtype_code(sim.dtype)
+    st = _lib.stream_ptr(sim.device)
+    stream = torch.cuda.current_stream(sim.device)
+    sv, isz = sim.state.data_ptr(), sim.mats.element_size()
+    _lib.check(L.qgb_init_basis(sv, code, n, 0, T, 2 ** n, st), "init_basis")
+    rows, prev, kprev, prev_sites = [], None, 0, []
+    for i, g in enumerate(sim.gates):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _lib.check(L.qgb_traj_step(sv, code, n, T, 2 ** n, sim._site_arrays[i], len(g.indices),
+                                   sim.mats.data_ptr() + sim.offs[i] * isz, prev, kprev, sim.kraus.data_ptr(),
+                                   sim.p_dep, sim.gamma, sim.seed, i, sim.partials.data_ptr(), None, None, st),
+                   "traj_step")
+        e1.record(stream)
+        union = set(g.indices) | set(prev_sites)
+        rows.append((i, len(union), n - 1 - max(union), e0, e1))
+        prev, kprev, prev_sites = sim._site_arrays[i], len(g.indices), list(g.indices)
+    torch.cuda.synchronize(sim.device)
+    return [(i, k, lo, e0.elapsed_time(e1)) for i, k, lo, e0, e1 in rows]
+
+
 def run_case(args):
     """Small committed workloads for profiler captures (one run each, no CUDA
     graph, so that a profiler sees every launch):
@@ -912,7 +941,7 @@ def run_case(args):
         sim = TrajectorySim(workloads.tfi_trotter_circuit(n, 0.05, steps), T, p_dep=1e-3, gamma=5e-4, seed=2026,
                             mode="per_gate")
         sim.run()
-        rows = sim.time_gates()
+        rows = _time_traj_gates(sim)
         alg = 2 * T * 2 ** n * 8
         total = sum(ms for *_, ms in rows)
         print(f"{n} qubits, {T} trajectories, {len(rows)} gates: {total / len(rows):.3f} ms/gate, "

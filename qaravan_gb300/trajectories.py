@@ -309,32 +309,6 @@ class TrajectorySim:
         self.graph.replay()
         return self.state
 
-    def time_gates(self):
-        """Per-gate mode: one run with CUDA events around every gate's launches on the launching
-        stream: a list of (gate index, union bits, lowest union bit, ms). The
-        union is the gate's sites plus the previous gate's (pending damping)."""
-        L = _lib.lib()
-        n, T = self.n, self.ntraj
-        code = _lib.dtype_code(self.dtype)
-        st = _lib.stream_ptr(self.device)
-        stream = torch.cuda.current_stream(self.device)
-        sv, isz = self.state.data_ptr(), self.mats.element_size()
-        _lib.check(L.qgb_init_basis(sv, code, n, 0, T, 2 ** n, st), "init_basis")
-        rows, prev, kprev, prev_sites = [], None, 0, []
-        for i, g in enumerate(self.gates):
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            _lib.check(L.qgb_traj_step(sv, code, n, T, 2 ** n, self._site_arrays[i], len(g.indices),
-                                       self.mats.data_ptr() + self.offs[i] * isz, prev, kprev, self.kraus.data_ptr(),
-                                       self.p_dep, self.gamma, self.seed, i, self.partials.data_ptr(), None, None, st),
-                       "traj_step")
-            e1.record(stream)
-            union = set(g.indices) | set(prev_sites)
-            rows.append((i, len(union), n - 1 - max(union), e0, e1))
-            prev, kprev, prev_sites = self._site_arrays[i], len(g.indices), list(g.indices)
-        torch.cuda.synchronize(self.device)
-        return [(i, k, lo, e0.elapsed_time(e1)) for i, k, lo, e0, e1 in rows]
-
     def expectations(self, terms):
         """(ntraj, nterms) float64 of c_t <psi|P_t|psi> per trajectory."""
         return pauli_expectations(self.state, self.n, terms, batch=self.ntraj, stride=2 ** self.n)
