@@ -220,12 +220,73 @@ def fma_peaks():
     out = torch.empty(152 * 32, dtype=torch.float64, device="cuda")
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     res = {}
-    for name, prec, iters in (("fp32_tflops", 0, 200000), ("fp64_tflops", 1, 20000)):
+    for name, prec, iters in (("fp32_tflops", 0, 200000), ("fp64_tflops", 1, 20000), ("fp32x2_tflops", 2, 200000)):
         def run():
             _lib.check(L.qgb_fma_probe(prec, iters, 8, out.data_ptr(), _lib.stream_ptr()), "fma_probe")
         ms = _event_ms(run, 1, 3)
-        res[name] = round(2 * 8 * iters * 256 * 8 * sms / (ms / 1e3) / 1e12, 2)
+        res[name] = round((2 if prec == 2 else 1) * 2 * 8 * iters * 256 * 8 * sms / (ms / 1e3) / 1e12, 2)
     return res
+
+
+def c128_roofline(plan, n, ms, double_float, peaks):
+    """Roofline of a complex128 sweep plan: float64 kernels against the measured
+    FP64 FMA rate (8 flops per complex multiply-add); double-float kernels
+    against the measured FP32 rate, counting the FP32 pipe's work -- one
+    double-float complex multiply-add is 4 real terms of 1 multiply, 3 FMAs and
+    8 adds, 48 FP32 instructions, each counted as the probe counts an FMA (2
+    flops) -- so that `frac` is the FP32 pipe's busy fraction."""
+    from qaravan_gb300.compiler import plan_flops
+    flops64 = plan_flops(plan)[1] * 2 ** n  # 8 per complex multiply-add
+    out = {"tflops_fp64_equivalent": round(flops64 / (ms / 1e3) / 1e12, 3)}
+    if double_float:
+        achieved = 2 * 48 * (flops64 / 8) / (ms / 1e3) / 1e12
+        out["roofline"] = {"bound": "fp32", "achieved": round(achieved, 2), "peak": peaks["fp32_tflops"],
+                           "unit": "TFLOP/s", "frac": round(achieved / peaks["fp32_tflops"], 3),
+                           "counting": "48 FP32 instructions per complex multiply-add, 2 flops each",
+                           "peak_source": "qgb_fma_probe float32 FMA rate measured in this run"}
+    else:
+        achieved = flops64 / (ms / 1e3) / 1e12
+        out["roofline"] = {"bound": "fp64", "achieved": round(achieved, 3), "peak": peaks["fp64_tflops"],
+                           "unit": "TFLOP/s", "frac": round(achieved / peaks["fp64_tflops"], 3),
+                           "peak_source": "qgb_fma_probe float64 FMA rate measured in this run"}
+    return out
+
+
+def section_c128(n, gates, steps=3):
+    """The benchmark circuit in complex128 through StatevectorSim's default
+    complex128 path (double-float tile sweeps), timed over `steps` runs after a
+    warm-up, with its roofline; its final state against the float64 kernels'."""
+    import torch
+    from qaravan_gb300 import StatevectorSim, _lib
+    from qaravan_gb300.circuits import Circuit
+    L = _lib.lib()
+    circ = Circuit(gates, n=n)
+    code = _lib.dtype_code(torch.complex128)
+    out = {}
+    states = {}
+    for arith, name in ((1, "double_float"), (0, "float64")):
+        _lib.check(L.qgb_set_c128_arith(arith))
+        ex = StatevectorSim(circ, dtype=torch.complex128).compile()
+        st = torch.empty(2 ** n, dtype=torch.complex128, device="cuda")
+
+        def step():
+            _lib.check(L.qgb_init_basis(st.data_ptr(), code, n, 0, 1, 0, _lib.stream_ptr()), "init")
+            ex.run(st)
+        ms = _event_ms(step, 1, steps if arith == 1 else 1)
+        out[name] = {"gates_per_s": round(len(gates) / (ms / 1e3), 1), "ms": round(ms, 2),
+                     "hbm_passes": ex.plan.n_sweeps}
+        out[name].update(c128_roofline(ex.plan, n, ms, arith == 1, out.setdefault("fma_peaks", fma_peaks())))
+        states[name] = st
+        del ex
+    _lib.check(L.qgb_set_c128_arith(1))
+    d = (states["double_float"] - states["float64"]).abs()
+    out["max_abs_amplitude_diff_double_float_vs_float64"] = float(d.max().item())
+    out["max_abs_amplitude"] = float(states["float64"].abs().max().item())
+    out["norm_error_double_float"] = float(abs(torch.linalg.vector_norm(states["double_float"]).item() - 1.0))
+    out["speedup_double_float_vs_float64"] = round(out["float64"]["ms"] / out["double_float"]["ms"], 2)
+    del states, d
+    torch.cuda.empty_cache()
+    return out
 
 
 def section_variants(n, gates):
@@ -251,8 +312,15 @@ def section_variants(n, gates):
             ("c64_fused_w6_tensorcores_no_norm_restore", torch.complex64, "fused", 6, 14, 3),
             ("c64_sweep_w3_t12", torch.complex64, "sweep", 3, 12, 0),
             ("c64_sweep_w4_t14", torch.complex64, "sweep", 4, 14, 0),
-            ("c128_sweep_w3_t13", torch.complex128, "sweep", 3, 13, 0)]:
+            ("c128_sweep_w3_t13_fp64", torch.complex128, "sweep", 3, 13, 0),
+            ("c128_sweep_w2_t12_df", torch.complex128, "sweep", 2, 12, 1),
+            ("c128_sweep_w3_t12_df", torch.complex128, "sweep", 3, 12, 1),
+            ("c128_sweep_w3_t13_df", torch.complex128, "sweep", 3, 13, 1),
+            ("c128_sweep_w4_t13_df", torch.complex128, "sweep", 4, 13, 1)]:
         try:
+            if dtype == torch.complex128:  # impl: the complex128 arithmetic (0 float64, 1 double-float)
+                _lib.check(L.qgb_set_c128_arith(impl))
+                impl = 0
             _lib.check(L.qgb_set_dense_impl(min(impl, 2)))
             engine.set_norm_restore({3: "off", 4: "row"}.get(impl, "chain"))
             ex = StatevectorSim(circ, dtype=dtype, mode=mode, fusion_width=width, tile_bits=tile).compile()
@@ -266,19 +334,14 @@ def section_variants(n, gates):
             out[name] = {"gates_per_s": round(len(gates) / (ms / 1e3), 1), "ms": round(ms, 2),
                          "hbm_passes": ex.plan.n_sweeps}
             if dtype == torch.complex128:
-                from qaravan_gb300.compiler import plan_flops
-                flops = plan_flops(ex.plan)[1] * 2 ** n
-                out[name]["tflops"] = round(flops / (ms / 1e3) / 1e12, 3)
-                peaks = out.setdefault("fma_peaks", fma_peaks())
-                out[name]["roofline"] = {"bound": "fp64", "achieved": out[name]["tflops"],
-                                         "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
-                                         "frac": round(out[name]["tflops"] / peaks["fp64_tflops"], 3),
-                                         "peak_source": "qgb_fma_probe float64 FMA rate measured in this run"}
+                out[name].update(c128_roofline(ex.plan, n, ms, name.endswith("_df"),
+                                               out.setdefault("fma_peaks", fma_peaks())))
             del st, ex
         except Exception as e:  # a variant that does not fit is reported, not fatal
             out[name] = {"error": str(e)[:200]}
         torch.cuda.empty_cache()
     _lib.check(L.qgb_set_dense_impl(before))
+    _lib.check(L.qgb_set_c128_arith(1))
     engine.set_norm_restore("chain")
     return out
 
@@ -786,10 +849,12 @@ def gpu_arm(args):
     # run in complex128 (CUDA-core tile sweeps, the path pinned to the reference fixtures at 1e-12)
     accuracy = None
     if rank == 0 and dtype == torch.complex64 and not args.no_accuracy:
+        _lib.check(_lib.lib().qgb_set_c128_arith(0))  # float64 arithmetic for the reference state
         ref_sim = StatevectorSim(circ, dtype=torch.complex128)
         ref_state = ref_sim.get_statevector().reshape(-1)
+        _lib.check(_lib.lib().qgb_set_c128_arith(1))
         diff = (state.to(torch.complex128) - ref_state).abs()
-        accuracy = {"reference": "same circuit in complex128 (CUDA-core tile sweeps)",
+        accuracy = {"reference": "same circuit in complex128 (float64 CUDA-core tile sweeps)",
                     "max_abs_amplitude_error": float(diff.max().item()),
                     "rms_amplitude_error": float(diff.square().mean().sqrt().item()),
                     "max_abs_amplitude": float(ref_state.abs().max().item()),
@@ -798,10 +863,10 @@ def gpu_arm(args):
     del state, ex, sim
     torch.cuda.empty_cache()
     sections = {}
-    all_sections = ["variants", "torch_backend_gpu", "config1", "adjoint", "adjoint_batch", "trajectories",
+    all_sections = ["c128", "variants", "torch_backend_gpu", "config1", "adjoint", "adjoint_batch", "trajectories",
                     "dm_batch"]
     wanted = args.sections.split(",") if args.sections != "all" else all_sections
-    for name, fn in [("variants", lambda: section_variants(n, gates)),
+    for name, fn in [("c128", lambda: section_c128(n, gates)), ("variants", lambda: section_variants(n, gates)),
                      ("torch_backend_gpu", lambda: section_torch_backend_gpu(gates, n)),
                      ("config1", section_config1), ("adjoint", section_adjoint),
                      ("adjoint_batch", section_adjoint_batch),

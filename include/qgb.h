@@ -131,8 +131,9 @@ int qgb_check_status(void* stream);
 int qgb_wait_probe(int mode, unsigned long long limit_ns, const int* flag, void* stream);
 /* Peak rate of the fused multiply-add pipe (no counterpart in the reference):
  * sm_count * blocks_per_sm CTAs of 256 threads each run 8 independent chains
- * of `iters` FMAs in float32 (precision 0) or float64 (precision 1);
- * 2 * 8 * iters * 256 * CTAs flops, no memory traffic. Time it with events on
+ * of `iters` FMAs in float32 (precision 0), float64 (precision 1) or packed
+ * float32 pairs (precision 2, fma.rn.f32x2: twice the flops per instruction);
+ * 2 * 8 * iters * 256 * CTAs flops (twice that for precision 2), no memory traffic. Time it with events on
  * `stream`; `out` is a device buffer of at least one value per CTA that is
  * never written in practice. The complex128 kernels' roofline is this rate. */
 int qgb_fma_probe(int precision, int iters, int blocks_per_sm, void* out, void* stream);
@@ -206,6 +207,15 @@ int qgb_apply_sweep(void* sv, int dtype, int n, const qgb_sweep* sweep, const vo
  * 1 = TMA-staged tiles with a producer warp when the geometry allows it
  * (runs of at least 128 bytes). Process-wide; both give identical results. */
 int qgb_set_sweep_impl(int impl);
+
+/* Arithmetic of complex128 tile sweeps (qgb_apply_sweep): 1 (default) =
+ * double-float -- each float64 component carried as a pair of floats (48
+ * significant bits) inside the tile, FP32 instructions only, the state in HBM
+ * still complex128 -- 0 = float64 kernels. Process-wide; QGB_C128_ARITH=fp64
+ * selects 0 at start-up. No reference counterpart: the reference's numpy
+ * complex128 op_action (tensorQ/statevector_sim.py:124-140) has one arithmetic. */
+int qgb_set_c128_arith(int mode);
+int qgb_get_c128_arith(void);
 
 /* Selects the kernel for complex64 dense blocks of k >= 4 qubits on at least
  * 2^(k+7) amplitudes: 0 = CUDA-core kernels only, 1 = tensor cores (tcgen05,

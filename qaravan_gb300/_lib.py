@@ -71,6 +71,8 @@ SIGNATURES = {
     "qgb_dm_trace_factor": (C.c_int, [_vp, _i, _i, _vp, _i, _vp]),
     "qgb_apply_sweep": (C.c_int, [_vp, _i, _i, C.POINTER(Sweep), _vp, _i64, _i64, _i64, _vp]),
     "qgb_set_sweep_impl": (C.c_int, [_i]),
+    "qgb_set_c128_arith": (C.c_int, [_i]),
+    "qgb_get_c128_arith": (C.c_int, []),
     "qgb_init_basis": (C.c_int, [_vp, _i, _i, _u64, _i64, _i64, _vp]),
     "qgb_scale": (C.c_int, [_vp, _i, _i, _vp, _i64, _i64, _vp]),
     "qgb_pauli_layer": (C.c_int, [_vp, _i, _i, _vp, _vp, _vp, _i64, _i64, _vp]),

@@ -105,15 +105,40 @@ __global__ void __launch_bounds__(256) fma_probe_kernel(T* out, int iters, T a, 
     for (int j = 0; j < 8; ++j) s += x[j];
     if (s == T(-1.2345e-7)) out[blockIdx.x] = s;
 }
+
+// The same chains as packed pairs (fma.rn.f32x2: one instruction, two float FMAs).
+__global__ void __launch_bounds__(256) fma_probe_f32x2_kernel(float* out, int iters, float a, float b) {
+    unsigned long long x[8], a2, b2;
+    asm("mov.b64 %0, {%1, %1};" : "=l"(a2) : "f"(a));
+    asm("mov.b64 %0, {%1, %1};" : "=l"(b2) : "f"(b));
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const float v = float(threadIdx.x + j) * 1e-3f;
+        asm("mov.b64 %0, {%1, %2};" : "=l"(x[j]) : "f"(v), "f"(v + 1.f));
+    }
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) asm("fma.rn.f32x2 %0, %0, %1, %2;" : "+l"(x[j]) : "l"(a2), "l"(b2));
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        float u, v;
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(u), "=f"(v) : "l"(x[j]));
+        s += u + v;
+    }
+    if (s == -1.2345e-7f) out[blockIdx.x] = s;
+}
 }  // namespace qgb
 
 extern "C" int qgb_fma_probe(int precision, int iters, int blocks_per_sm, void* out, void* stream) {
-    if ((precision != 0 && precision != 1) || iters < 1 || blocks_per_sm < 1 || blocks_per_sm > 32 || !out)
+    if (precision < 0 || precision > 2 || iters < 1 || blocks_per_sm < 1 || blocks_per_sm > 32 || !out)
         return qgb_host::set_error(QGB_EINVAL, "fma probe arguments invalid");
     const unsigned grid = unsigned(qgb_host::sm_count() * blocks_per_sm);
     cudaStream_t st = (cudaStream_t)stream;
     if (precision == 0) qgb::fma_probe_kernel<float><<<grid, 256, 0, st>>>((float*)out, iters, 0.9999999f, 1e-7f);
-    else qgb::fma_probe_kernel<double><<<grid, 256, 0, st>>>((double*)out, iters, 0.9999999999, 1e-12);
+    else if (precision == 1) qgb::fma_probe_kernel<double><<<grid, 256, 0, st>>>((double*)out, iters, 0.9999999999, 1e-12);
+    else qgb::fma_probe_f32x2_kernel<<<grid, 256, 0, st>>>((float*)out, iters, 0.9999999f, 1e-7f);
     return qgb_host::check_launch("fma probe");
 }
 

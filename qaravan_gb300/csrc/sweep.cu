@@ -224,5 +224,6 @@ extern "C" int qgb_apply_sweep(void* sv, int dtype, int n, const qgb_sweep* swee
         const int rc = launch_sweep_tma(dtype, sv, mats, a, kmax, st);
         if (rc != 1) return rc;
     }
+    if (dtype == QGB_C128 && c128_arith() == 1) return launch_sweep_df(sv, mats, a, kmax, st);
     return dtype == QGB_C64 ? dispatch_ldst<float>(sv, mats, a, kmax, st) : dispatch_ldst<double>(sv, mats, a, kmax, st);
 }

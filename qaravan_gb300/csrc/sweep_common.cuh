@@ -162,4 +162,8 @@ namespace qgb_host {
 // is not eligible (caller falls back to the load/store kernel), else a QGB code.
 int launch_sweep_tma(int dtype, void* sv, const void* mats, const qgb::SweepArgs& a, int kmax, cudaStream_t st);
 int sweep_status_read_clear();
+// complex128 tile sweeps in double-float arithmetic (sweep_df.cu); c128_arith() is
+// 1 when they are selected (the default), 0 for the float64 kernels.
+int c128_arith();
+int launch_sweep_df(void* sv, const void* mats, const qgb::SweepArgs& a, int kmax, cudaStream_t st);
 }  // namespace qgb_host
