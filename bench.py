@@ -310,6 +310,7 @@ def section_variants(n, gates):
             ("c64_fused_w6_tensorcores", torch.complex64, "fused", 6, 14, 2),
             ("c64_fused_w6_tensorcores_row_norm_restore", torch.complex64, "fused", 6, 14, 4),
             ("c64_fused_w6_tensorcores_no_norm_restore", torch.complex64, "fused", 6, 14, 3),
+            ("c64_tcsweep_w5", torch.complex64, "tcsweep", 5, 13, 2),
             ("c64_sweep_w3_t12", torch.complex64, "sweep", 3, 12, 0),
             ("c64_sweep_w4_t14", torch.complex64, "sweep", 4, 14, 0),
             ("c128_sweep_w3_t13_fp64", torch.complex128, "sweep", 3, 13, 0),
@@ -744,7 +745,8 @@ def gpu_arm(args):
                          low_bits=args.low)
     ex = sim.compile()
     ex_kmax = max([len(st.bits) for st in ex.plan.steps if hasattr(st, "bits")] +
-                  [len(p) for st in ex.plan.steps if hasattr(st, "ops") for p, _ in st.ops] + [2])
+                  [len(p) for st in ex.plan.steps if hasattr(st, "ops") for p, _ in st.ops] +
+                  [len(p) for st in ex.plan.steps if hasattr(st, "blocks") for p, _ in st.blocks] + [2])
     state = torch.empty(2 ** n, dtype=dtype, device="cuda")
     L = _lib.lib()
     code = _lib.dtype_code(dtype)
@@ -789,8 +791,10 @@ def gpu_arm(args):
     if dom:
         mean_ms = statistics.mean(durs[dom])
         achieved = alg_bytes / (mean_ms / 1e3) / 1e9
-        kname = {"sweep": f"sweep_ldst_kernel<{'float' if itemsize == 8 else 'double'},{ex_kmax}>",
-                 "dense": f"dense_reg_kernel<{'float' if itemsize == 8 else 'double'},{ex_kmax}>"}[dom]
+        kname = {"sweep": (f"sweep_ldst_kernel<float,{ex_kmax}>" if itemsize == 8 else
+                           f"sweep_df_kernel<{ex_kmax}>"),
+                 "dense": f"dense_reg_kernel<{'float' if itemsize == 8 else 'double'},{ex_kmax}>",
+                 "tcsweep": "tc_sweep_kernel"}[dom]
         tc_mode = _lib.lib().qgb_get_dense_impl()
         if dom == "dense" and itemsize == 8 and n >= 13 and (ex_kmax >= 5 and tc_mode >= 1 or
                                                             ex_kmax == 4 and tc_mode == 2):
@@ -1045,7 +1049,7 @@ def main():
     p.add_argument("--qubits", type=int, default=N_QUBITS)
     p.add_argument("--depth", type=int, default=DEPTH)
     p.add_argument("--dtype", default="c64", choices=["c64", "c128"])
-    p.add_argument("--mode", default="fused", choices=["gate", "fused", "sweep"])
+    p.add_argument("--mode", default="fused", choices=["gate", "fused", "sweep", "tcsweep"])
     p.add_argument("--width", type=int, default=6)
     p.add_argument("--tile", type=int, default=14)
     p.add_argument("--low", type=int, default=None)

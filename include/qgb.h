@@ -63,6 +63,22 @@ typedef struct {
     int64_t op_mat[QGB_SWEEP_MAX_OPS];
 } qgb_sweep;
 
+/* One tensor-core tile sweep: the tile is 8192 amplitudes, the flat bits
+ * [0, low_bits) (low_bits >= 4: contiguous runs of at least 128 bytes) and the
+ * 13 - low_bits listed high bits; up to QGB_TCS_MAX_BLOCKS fused 5-qubit
+ * blocks are applied to it in order, each on five tile bits. block_pos[b][j]
+ * is the tile bit (0 .. 12; tile bit low_bits+h is flat bit high_bits[h]) of
+ * matrix bit (4 - j); block_mat[b] the element offset of its 32 x 32
+ * complex64 matrix in `mats`. */
+#define QGB_TCS_MAX_BLOCKS 4
+typedef struct {
+    int32_t low_bits;
+    int32_t high_bits[9];
+    int32_t n_blocks;
+    int32_t block_pos[QGB_TCS_MAX_BLOCKS][5];
+    int64_t block_mat[QGB_TCS_MAX_BLOCKS];
+} qgb_tc_sweep;
+
 /* One pass of the adjoint reverse sweep over a batch of (state, co-state)
  * pairs, with the tile geometry of qgb_sweep. The ops are gates on 1 or 2
  * sites listed in the order the reverse sweep meets them (the circuit's last
@@ -207,6 +223,21 @@ int qgb_apply_sweep(void* sv, int dtype, int n, const qgb_sweep* sweep, const vo
  * 1 = TMA-staged tiles with a producer warp when the geometry allows it
  * (runs of at least 128 bytes). Process-wide; both give identical results. */
 int qgb_set_sweep_impl(int impl);
+
+/* Several fused 5-qubit blocks per read and write of a complex64 state, on
+ * the tensor cores (tcgen05, split-fp16 operands, fp32 accumulation): the
+ * multi-block counterpart of qgb_op_action for fused circuits (the reference
+ * applies each gate as its own op_action contraction,
+ * tensorQ/statevector_sim.py:124-140, in BaseSim.run's loop,
+ * core/base_sim.py:30-53). One state of n >= 14 qubits. With `chain` (6
+ * doubles of device scratch, zeroed by the call at link 0) the sweep is a link
+ * of the norm chain of unitary passes, as qgb_op_action_unitary_chain: link
+ * numbers consecutive unitary passes from 0; the first pass of every epoch of
+ * 4 corrects the norm drift measured at the end of the previous epoch. With
+ * chain = NULL the blocks need not be unitary. */
+int qgb_apply_tc_sweep(void* sv, int dtype, int n, const qgb_tc_sweep* sweep, const void* mats, double* chain,
+                       int link, void* stream);
+size_t qgb_tc_sweep_bytes(void);
 
 /* Arithmetic of complex128 tile sweeps (qgb_apply_sweep): 1 (default) =
  * double-float -- each float64 component carried as a pair of floats (48

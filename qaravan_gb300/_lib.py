@@ -13,6 +13,7 @@ import torch
 from . import build as _build
 
 QGB_C64, QGB_C128 = 0, 1
+QGB_OK, QGB_EINVAL, QGB_ECUDA, QGB_ETIMEOUT, QGB_ESCRATCH = 0, -1, -2, -3, -4
 QGB_MAX_K = 6
 QGB_SWEEP_MAX_OPS = 64
 QGB_SWEEP_MAX_HIGH = 10
@@ -35,6 +36,20 @@ class Sweep(C.Structure):
         ("op_k", C.c_int32 * QGB_SWEEP_MAX_OPS),
         ("op_pos", (C.c_int32 * QGB_MAX_K) * QGB_SWEEP_MAX_OPS),
         ("op_mat", C.c_int64 * QGB_SWEEP_MAX_OPS),
+    ]
+
+
+QGB_TCS_MAX_BLOCKS = 4
+
+
+class TcSweep(C.Structure):
+    """Mirror of ``qgb_tc_sweep``."""
+    _fields_ = [
+        ("low_bits", C.c_int32),
+        ("high_bits", C.c_int32 * 9),
+        ("n_blocks", C.c_int32),
+        ("block_pos", (C.c_int32 * 5) * QGB_TCS_MAX_BLOCKS),
+        ("block_mat", C.c_int64 * QGB_TCS_MAX_BLOCKS),
     ]
 
 
@@ -72,6 +87,8 @@ SIGNATURES = {
     "qgb_apply_sweep": (C.c_int, [_vp, _i, _i, C.POINTER(Sweep), _vp, _i64, _i64, _i64, _vp]),
     "qgb_set_sweep_impl": (C.c_int, [_i]),
     "qgb_set_c128_arith": (C.c_int, [_i]),
+    "qgb_apply_tc_sweep": (C.c_int, [_vp, _i, _i, C.POINTER(TcSweep), _vp, _vp, _i, _vp]),
+    "qgb_tc_sweep_bytes": (C.c_size_t, []),
     "qgb_get_c128_arith": (C.c_int, []),
     "qgb_init_basis": (C.c_int, [_vp, _i, _i, _u64, _i64, _i64, _vp]),
     "qgb_scale": (C.c_int, [_vp, _i, _i, _vp, _i64, _i64, _vp]),

@@ -5,8 +5,9 @@ Three kinds of choice:
 
 * ``sv``: how a statevector circuit runs -- ``(mode, fusion_width,
   tile_bits)``: one HBM pass per fused block of 4-6 qubits (6-qubit blocks run
-  on the tensor cores, fewer bits on the CUDA cores) or shared-memory tile
-  sweeps of 2-4-qubit blocks with 12-14-bit tiles. Used by ``StatevectorSim``
+  on the tensor cores, fewer bits on the CUDA cores), up to four 5-qubit blocks
+  per pass on the tensor cores (``tcsweep``), or shared-memory tile sweeps of
+  2-4-qubit blocks with 12-14-bit tiles. Used by ``StatevectorSim``
   when its ``mode`` is ``"auto"``.
 * ``traj``: the tile bits of the persistent trajectory kernel (11-14). Used by
   ``TrajectorySim``.
@@ -33,7 +34,8 @@ import os
 import torch
 
 SV_CANDIDATES = {
-    torch.complex64: [("fused", 6, 14), ("fused", 5, 14), ("fused", 4, 14), ("sweep", 4, 14), ("sweep", 3, 12)],
+    torch.complex64: [("fused", 6, 14), ("fused", 5, 14), ("fused", 4, 14), ("tcsweep", 5, 13), ("sweep", 4, 14),
+                      ("sweep", 3, 12)],
     torch.complex128: [("sweep", 3, 13), ("sweep", 2, 13), ("sweep", 4, 12), ("fused", 3, 13), ("fused", 2, 13)],
 }
 TRAJ_CANDIDATES = {torch.complex64: [11, 12, 13, 14], torch.complex128: [11, 12, 13]}

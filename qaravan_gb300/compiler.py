@@ -60,6 +60,16 @@ class SweepStep:
 
 
 @dataclass
+class TcSweepStep:
+    """Up to four 5-qubit blocks applied to each 8192-amplitude tile (the low
+    ``low_bits`` flat bits times ``high_bits``) in one pass on the tensor cores."""
+    low_bits: int
+    high_bits: list
+    blocks: list  # (tile positions of the block's five bits in matrix order, matrix index)
+    unitary: bool = False  # every block is unitary: the pass may join the norm chain
+
+
+@dataclass
 class NormalizeStep:
     pass
 
@@ -106,7 +116,7 @@ class Plan:
 
     @property
     def n_sweeps(self):
-        return sum(1 for s in self.steps if isinstance(s, (DenseStep, SweepStep)))
+        return sum(1 for s in self.steps if isinstance(s, (DenseStep, SweepStep, TcSweepStep)))
 
 
 # ----------------------------------------------------------------- algebra
@@ -251,8 +261,9 @@ def recipe_matrix(recipe, op_matrices):
 
 # --------------------------------------------------------- sweep planning
 
-def plan_sweeps(blocks, nbits, tile_bits, low_bits=None, max_high=QGB_SWEEP_MAX_HIGH):
-    """Group blocks into tile sweeps; returns a list of (low_bits, high_bits, [blocks])."""
+def plan_sweeps(blocks, nbits, tile_bits, low_bits=None, max_high=QGB_SWEEP_MAX_HIGH, max_ops=QGB_SWEEP_MAX_OPS):
+    """Group blocks into tile sweeps of at most ``max_ops`` blocks; returns a
+    list of (low_bits, high_bits, [blocks])."""
     m = min(tile_bits, nbits, QGB_SWEEP_MAX_TILE_BITS)
     L = min(5 if low_bits is None else low_bits, m)
     if m == nbits:
@@ -276,7 +287,7 @@ def plan_sweeps(blocks, nbits, tile_bits, low_bits=None, max_high=QGB_SWEEP_MAX_
                 rest.extend(remaining[j:])
                 break
             bset = set(blk.bits)
-            if bset & blocked or len(taken) >= QGB_SWEEP_MAX_OPS:
+            if bset & blocked or len(taken) >= max_ops:
                 blocked |= bset
                 rest.append(blk)
                 continue
@@ -404,7 +415,9 @@ def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, 
     into a :class:`Plan`.
 
     ``mode``: ``"gate"`` one pass per op; ``"fused"`` one pass per fused block of
-    ``width`` bits; ``"sweep"`` fused blocks grouped into shared-memory tile sweeps.
+    ``width`` bits; ``"sweep"`` fused blocks grouped into shared-memory tile sweeps;
+    ``"tcsweep"`` 5-qubit blocks, up to four per pass, on the tensor cores
+    (statevectors of at least 14 qubits; otherwise as ``"fused"``).
     ``itemsize`` (8 for complex64, 16 for complex128) caps the tile at 128 KiB
     of shared memory. ``device_fusion``: block matrices are left as
     :class:`Recipe` objects for the executor to compose on the GPU.
@@ -460,7 +473,11 @@ def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, 
             for o, u, w_ in zip(seg, uflags, whole_cuts(seg, [[i] for i in range(len(seg))])):
                 plan.steps.append(DenseStep(list(o.bits), plan.add_matrix(o.matrix), u, w_))
             continue
-        w = max(width, max(len(o.bits) for o in seg))
+        # tensor-core tile sweeps: 5-qubit blocks, four at most per 13-bit tile, one state of >= 14
+        # qubits; density-matrix segments keep the trace chain of the dense passes instead
+        tcs = (mode == "tcsweep" and nbits >= 14 and max(len(o.bits) for o in seg) <= 5
+               and not any(o.pair is not None or o.kind == "channel" for o in seg))
+        w = 5 if tcs else max(width, max(len(o.bits) for o in seg))
         if device_fusion:
             base = len(plan.op_matrices)
             plan.op_matrices.extend(np.ascontiguousarray(o.matrix, dtype=np.complex128) for o in seg)
@@ -474,7 +491,10 @@ def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, 
             bflags = [bool(np.abs(b.matrix.conj().T @ b.matrix - np.eye(b.matrix.shape[0])).max() < 1e-6)
                       for b in blocks]
             wflags = [all(o.pair is None for o in seg)] * len(blocks)  # membership unknown here
-        if mode == "fused" or w > max_sweep_k or tile_bits <= 0:
+        if tcs:
+            _plan_tc_sweeps(plan, blocks, bflags, nbits, low_bits)
+            continue
+        if mode in ("fused", "tcsweep") or w > max_sweep_k or tile_bits <= 0:
             for b, u, w_ in zip(blocks, bflags, wflags):
                 plan.steps.append(DenseStep(list(b.bits), plan.add_matrix(b.matrix), u, w_))
             continue
@@ -489,6 +509,33 @@ def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, 
     return plan
 
 
+TCS_MAX_BLOCKS = 4  # QGB_TCS_MAX_BLOCKS
+
+
+def _plan_tc_sweeps(plan, blocks, bflags, nbits, low_bits=None):
+    """Tensor-core tile sweeps of 13-bit tiles (low bits >= 4, runs of 128
+    bytes) holding up to four blocks; every block is widened to exactly five
+    tile bits (identity on the added ones, the lowest free tile bits first, so
+    that tile bit 0 -- adjacent amplitudes -- is a target where possible)."""
+    flag = {id(b): f for b, f in zip(blocks, bflags)}
+    lb = 4 if low_bits is None else max(4, min(int(low_bits), 13))
+    for L, high, taken in plan_sweeps(blocks, nbits, 13, lb, max_high=9, max_ops=TCS_MAX_BLOCKS):
+        tpos = {b: b for b in range(L)}
+        for h, b in enumerate(high):
+            tpos[b] = L + h
+        tile = sorted(tpos)
+        entries = []
+        for blk in taken:
+            bits = list(blk.bits)
+            full = bits + [b for b in tile if b not in bits][:5 - len(bits)]
+            if isinstance(blk.matrix, Recipe):
+                mat = Recipe(full, blk.matrix.entries)
+            else:
+                mat = embed(blk.matrix, bits, full)
+            entries.append(([tpos[b] for b in full], plan.add_matrix(mat)))
+        plan.steps.append(TcSweepStep(L, list(high), entries, all(flag[id(b)] for b in taken)))
+
+
 def plan_flops(plan):
     """(algorithmic bytes, flops) per vector element summed over passes: bytes
     are two vector passes (read + write) per dense/sweep step; flops are
@@ -501,4 +548,7 @@ def plan_flops(plan):
         elif isinstance(s, SweepStep):
             passes += 1
             flops += sum(8 * 2 ** len(p) for p, _ in s.ops)
+        elif isinstance(s, TcSweepStep):
+            passes += 1
+            flops += sum(8 * 2 ** len(p) for p, _ in s.blocks)
     return passes, flops

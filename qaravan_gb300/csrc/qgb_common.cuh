@@ -174,6 +174,7 @@ int try_dense_tc(void* sv, const void* op, int nbits, const int* sorted, const i
                  int k, int64_t op_stride, int64_t batch, int64_t sv_stride, int unitary, cudaStream_t st,
                  double* chain = nullptr, int link = 0, const double* scale = nullptr);
 int tc_status_read_clear();
+int tcs_status_read_clear();
 int traj_status_read_clear();
 int fuse_status_read_clear();
 }  // namespace qgb_host

@@ -19,7 +19,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .compiler import DenseStep, NormalizeStep, PauliMixStep, Plan, Recipe, SweepStep
+from .compiler import DenseStep, NormalizeStep, PauliMixStep, Plan, Recipe, SweepStep, TcSweepStep
 
 # Unitary fused blocks control the norm on the tensor-core path, removing the
 # round-toward-zero shrinkage of tensor-core accumulation (~1e-7 of the norm per
@@ -140,6 +140,17 @@ class Executor:
                         sw.op_pos[i][j] = p
                     sw.op_mat[i] = offs[mi]
                 self._steps.append(("sweep", sw))
+            elif isinstance(s, TcSweepStep):
+                ts = _lib.TcSweep()
+                ts.low_bits = s.low_bits
+                for i, b in enumerate(s.high_bits):
+                    ts.high_bits[i] = b
+                ts.n_blocks = len(s.blocks)
+                for i, (pos, mi) in enumerate(s.blocks):
+                    for j, p in enumerate(pos):
+                        ts.block_pos[i][j] = p
+                    ts.block_mat[i] = offs[mi]
+                self._steps.append(("tcsweep", ts, s.unitary))
             elif isinstance(s, NormalizeStep):
                 self._steps.append(("normalize",))
             elif isinstance(s, PauliMixStep):
@@ -290,6 +301,20 @@ class Executor:
                            "apply_sweep")
                 launches += 1
                 link = 0
+            elif s[0] == "tcsweep":
+                if batch != 1 or mats is not self.mats:
+                    raise _lib.QgbError("tensor-core sweeps run one state with the plan's own matrices")
+                if s[2] and _NORM_RESTORE != "off":
+                    if getattr(self, "_chain", None) is None:
+                        self._chain = torch.zeros(6, dtype=torch.float64, device=self.device)
+                    _lib.check(L.qgb_apply_tc_sweep(ptr, self.code, nb, C.byref(s[1]), mptr, self._chain.data_ptr(),
+                                                    link, st), "apply_tc_sweep")
+                    link += 1
+                else:
+                    _lib.check(L.qgb_apply_tc_sweep(ptr, self.code, nb, C.byref(s[1]), mptr, None, 0, st),
+                               "apply_tc_sweep")
+                    link = 0
+                launches += 1
             elif s[0] == "pauli_mix":
                 _, strings, coeff, nterms = s
                 if getattr(self, "_mix_buf", None) is None or self._mix_buf.numel() < state.numel():

@@ -93,3 +93,41 @@ def test_dm_op_lowering_matches_reference_superops():
     v0[0] = 1
     out = run_plan_numpy(plan, v0).reshape(2 ** n, 2 ** n)
     assert np.max(np.abs(out - z["dm"])) < 1e-12
+
+
+@pytest.mark.parametrize("n,depth,dev", [(14, 4, True), (16, 6, False), (17, 5, True)])
+def test_tensor_core_sweep_plan_replays_to_the_circuit(n, depth, dev):
+    """The "tcsweep" plan (up to four 5-qubit blocks per 13-bit tile, low bits
+    >= 4), replayed block by block through the oracle's op_action, gives the
+    circuit's state; narrower blocks are widened with identity bits of the tile."""
+    from oracle import ref
+    from qaravan_gb300 import workloads
+    from qaravan_gb300.compiler import Recipe, TcSweepStep, compile_ops, recipe_matrix
+    from qaravan_gb300.statevector import gates_to_ops
+    gates = workloads.brickwork_gates(n, depth, 40 + n)
+    plan = compile_ops(gates_to_ops(gates, n), n, mode="tcsweep", width=5, device_fusion=dev)
+    st = ref.initial_sv(n)
+    for s in plan.steps:
+        assert isinstance(s, TcSweepStep)
+        assert s.low_bits >= 4 and s.low_bits + len(s.high_bits) == 13 and 1 <= len(s.blocks) <= 4
+        tile = list(range(s.low_bits)) + list(s.high_bits)
+        for pos, mi in s.blocks:
+            assert len(pos) == 5 and len(set(pos)) == 5 and all(0 <= p < 13 for p in pos)
+            m = plan.matrices[mi]
+            mat = recipe_matrix(m, plan.op_matrices) if isinstance(m, Recipe) else m
+            st = ref.op_action(mat, [n - 1 - tile[p] for p in pos], st)
+    assert np.max(np.abs(st.reshape(-1) - ref.run_sv(gates, n).reshape(-1))) < 1e-12
+
+
+def test_tensor_core_sweep_plan_of_the_28_qubit_brickwork():
+    from qaravan_gb300 import workloads
+    from qaravan_gb300.compiler import TcSweepStep, compile_ops
+    from qaravan_gb300.statevector import gates_to_ops
+    n = 28
+    plan = compile_ops(gates_to_ops(workloads.brickwork_gates(n, 20, 2028), n), n, mode="tcsweep", width=5,
+                       device_fusion=True)
+    assert all(isinstance(s, TcSweepStep) for s in plan.steps)
+    assert plan.n_sweeps == 35 and sum(len(s.blocks) for s in plan.steps) == 102
+    # below 14 qubits (one tile) the mode falls back to one pass per fused block
+    small = compile_ops(gates_to_ops(workloads.brickwork_gates(13, 2, 1), 13), 13, mode="tcsweep", width=5)
+    assert not any(isinstance(s, TcSweepStep) for s in small.steps)
