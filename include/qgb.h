@@ -239,6 +239,61 @@ int qgb_apply_tc_sweep(void* sv, int dtype, int n, const qgb_tc_sweep* sweep, co
                        int link, void* stream);
 size_t qgb_tc_sweep_bytes(void);
 
+/* An uneven batch of complex64 density matrices in one persistent launch on
+ * the tensor cores (qgb_dm_batch_run): the batched counterpart of running
+ * DensityMatrixSim (tensorQ/density_matrix_sim.py:38-42, driven by
+ * core/base_sim.py:30-53) circuit by circuit, with each circuit's results
+ * Tr rho, Tr rho^2 and Re Tr(rho Z_q) (tensorQ/density_matrix_sim.py:49-89)
+ * from its last pass. A circuit (7..14 qubits) is a vec(rho) of 4^n entries
+ * at `state` (16-byte aligned, overwritten: the run starts from
+ * |0...0><0...0|) and its passes first_pass .. first_pass + n_passes - 1
+ * of the pass table, in order; results go to row out_row. A pass applies a
+ * 64 x 64 complex64 matrix (device address `mat`, matrix order) to the six
+ * vec(rho) bits `bits` (bit bits[j] <-> matrix bit 5 - j). flags: 1 the pass
+ * multiplies its matrix by 1 / the output trace of pass tslot (an earlier
+ * pass of the same circuit flagged 2: the trace chain), 2 the pass measures
+ * its output's trace, 4 the circuit's last pass (required on it, and only on
+ * it), 8 the circuit's first pass (likewise). Every sum runs in a fixed order:
+ * results are bitwise reproducible. */
+typedef struct {
+    uint64_t state;
+    int32_t n;
+    int32_t first_pass;
+    int32_t n_passes;
+    int32_t out_row;
+} qgb_dm_circuit;
+
+typedef struct {
+    uint64_t mat;
+    int32_t circ;
+    int32_t bits[6];
+    int32_t flags;
+    int32_t tslot;
+    int32_t pad;
+} qgb_dm_pass;
+
+size_t qgb_dm_batch_circuit_bytes(void);
+size_t qgb_dm_batch_pass_bytes(void);
+/* Work items of the batch: per pass, its tiles of 8192 entries dealt
+ * round-robin to min(items_per_pass, tiles / 16) items (at least one;
+ * concurrent items of a pass stream neighbouring memory; items_per_pass = the
+ * SM count makes a large circuit's pass one wave), plus one finishing item per
+ * circuit (-1 on bad arguments). */
+int64_t qgb_dm_batch_items(const qgb_dm_circuit* circs, int ncirc, int items_per_pass);
+/* Bytes of the device table (pass geometry, circuits, items). */
+size_t qgb_dm_batch_table_bytes(int ncirc, int npasses, int64_t nitems);
+/* Fills `table` (host memory of table_bytes) after checking the circuits and
+ * passes; the caller copies it to device memory for qgb_dm_batch_run. */
+int qgb_dm_batch_build(void* table, size_t table_bytes, const qgb_dm_circuit* circs, int ncirc,
+                       const qgb_dm_pass* passes, int npasses, int items_per_pass);
+/* Bytes of the device work buffer (counters and one slot per item). */
+size_t qgb_dm_batch_work_bytes(int ncirc, int64_t nitems);
+/* Runs every pass of every circuit in one persistent launch; out (device,
+ * out_rows x out_cols float64, out_cols >= 16) and the work buffer are
+ * cleared by the call. Asynchronous on `stream`. */
+int qgb_dm_batch_run(const void* table, size_t table_bytes, int ncirc, int npasses, int64_t nitems, double* out,
+                     int out_rows, int out_cols, void* work, size_t work_bytes, void* stream);
+
 /* Arithmetic of complex128 tile sweeps (qgb_apply_sweep): 1 (default) =
  * double-float -- each float64 component carried as a pair of floats (48
  * significant bits) inside the tile, FP32 instructions only, the state in HBM

@@ -88,6 +88,13 @@ SIGNATURES = {
     "qgb_set_sweep_impl": (C.c_int, [_i]),
     "qgb_set_c128_arith": (C.c_int, [_i]),
     "qgb_apply_tc_sweep": (C.c_int, [_vp, _i, _i, C.POINTER(TcSweep), _vp, _vp, _i, _vp]),
+    "qgb_dm_batch_circuit_bytes": (C.c_size_t, []),
+    "qgb_dm_batch_pass_bytes": (C.c_size_t, []),
+    "qgb_dm_batch_items": (C.c_int64, [_vp, _i, _i]),
+    "qgb_dm_batch_table_bytes": (C.c_size_t, [_i, _i, _i64]),
+    "qgb_dm_batch_build": (C.c_int, [_vp, _sz, _vp, _i, _vp, _i, _i]),
+    "qgb_dm_batch_work_bytes": (C.c_size_t, [_i, _i64]),
+    "qgb_dm_batch_run": (C.c_int, [_vp, _sz, _i, _i, _i64, _vp, _i, _i, _vp, _sz, _vp]),
     "qgb_tc_sweep_bytes": (C.c_size_t, []),
     "qgb_get_c128_arith": (C.c_int, []),
     "qgb_init_basis": (C.c_int, [_vp, _i, _i, _u64, _i64, _i64, _vp]),

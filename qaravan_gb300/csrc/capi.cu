@@ -163,6 +163,9 @@ extern "C" int qgb_check_status(void* stream) {
     const int tcs = qgb_host::tcs_status_read_clear();
     if (tcs < 0) return qgb_host::set_error(QGB_ECUDA, "tensor-core sweep status read failed");
     if (tcs != 0) return qgb_host::set_error(QGB_ETIMEOUT, "a tensor-core sweep wait gave up (code %d)", tcs);
+    const int dmb = qgb_host::dmb_status_read_clear();
+    if (dmb < 0) return qgb_host::set_error(QGB_ECUDA, "density-matrix batch status read failed");
+    if (dmb != 0) return qgb_host::set_error(QGB_ETIMEOUT, "a density-matrix batch wait gave up (code %d)", dmb);
     const int tj = qgb_host::traj_status_read_clear();
     if (tj < 0) return qgb_host::set_error(QGB_ECUDA, "trajectory status read failed");
     if (tj != 0) return qgb_host::set_error(QGB_EINVAL, "more than 16 jumps in one sweep of a trajectory (code %d)", tj);

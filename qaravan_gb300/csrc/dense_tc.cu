@@ -65,29 +65,6 @@ namespace qgb {
 
 __device__ int g_tc_status = 0;
 
-struct TcArgs {
-    int k;
-    int vec2;                            // global bit 0 is a target: components (2m, 2m+1) adjacent
-    int vec4;                            // global bits 0 and 1 are targets: rows are runs of >= 4 components
-    int L;                               // tile bits 0..L-1 are global bits 0..L-1 (L >= 7)
-    int tile_bits[13];                   // global bit of each tile bit, ascending
-    int pos_g[13];                       // tile positions of the 13 - k group bits, ascending
-    int perm_in[1 << QGB_MAX_K];         // memory-order input component j -> matrix column
-    int perm_out[1 << QGB_MAX_K];        // memory-order output component i -> matrix row
-    uint32_t uts[1 << (QGB_MAX_K - 1)];  // swizzled tile-index offsets of the low-half components
-    uint32_t ut_h;                       // tile-index offset of the upper half (target sorted[k-1])
-    uint64_t g512[16];                   // global offset of tile index 512 m
-    uint64_t off[1 << (QGB_MAX_K - 1)];  // global offsets of the low-half components
-    uint64_t hstride;                    // global offset of the upper half
-    uint64_t hoff[64];                   // global offset of tile bits L..12, indexed by u >> L
-    uint64_t tiles_per_state;            // 2^(n - 13)
-    uint64_t tiles;                      // tiles_per_state * batch
-    int64_t sv_stride;
-    double* chain;                       // norm chain (3 slots of {reference, output} squared norms) or null
-    const double* scale;                 // MODE 0: device factor f, the op applied is f * M (null: 1)
-    int c_prev, c_cur, c_next;           // slots of the previous epoch, this epoch, the next epoch (-1: none)
-    int c_head, c_tail;                  // this pass opens its epoch (corrects) / closes it (measures its output)
-};
 
 
 
@@ -621,19 +598,13 @@ int set_dense_impl(int mode) {
     return QGB_OK;
 }
 
-// Tensor-core path for a complex64 dense op; returns QGB_EDECLINE (and touches
-// nothing) when the op is not one it takes, so that the caller runs the
-// CUDA-core kernel instead.
-int try_dense_tc(void* sv, const void* op, int nbits, const int* sorted, const int* in_bits, const int* out_bits,
-                 int k, int64_t op_stride, int64_t batch, int64_t sv_stride, int unitary, cudaStream_t st,
-                 double* chain, int link, const double* scale) {
-    const int mode = dense_impl();
-    if (scale && unitary != 0) return QGB_EDECLINE;  // a factor goes with plain (MODE 0) passes only
-    if (unitary == 2 && (batch > 1 || !chain)) return QGB_EDECLINE;  // the chain follows one state
-    if (mode == 0 || k < 4 || k > 6 || (k == 4 && mode < 2)) return QGB_EDECLINE;
-    if (nbits < 13) return QGB_EDECLINE;              // fewer than one 8192-amplitude tile
-    if (batch > 1 && op_stride != 0) return QGB_EDECLINE;  // one operator for the whole batch
-    TcArgs a{};
+// The geometry of a tensor-core pass (tile bits, group and component offsets,
+// permutations) for a dense op of width k on nbits-bit vectors; `sorted` holds
+// the target bits ascending, in_bits / out_bits the matrix-order bits of the
+// op's columns and rows. Returns QGB_OK or a QGB error.
+int build_tc_args(TcArgs& a, int nbits, const int* sorted, const int* in_bits, const int* out_bits, int k,
+                  int64_t batch, int64_t sv_stride) {
+    a = TcArgs{};
     a.k = k;
     const int D = 1 << k;
     uint64_t scat[1 << QGB_MAX_K];
@@ -652,8 +623,6 @@ int try_dense_tc(void* sv, const void* op, int nbits, const int* sorted, const i
             if (scat[j] == oo) a.perm_out[j] = c;
         }
     }
-    // cp.async copies 16-byte granules: the state (and every state of a batch) must start 16-byte aligned
-    if ((reinterpret_cast<uintptr_t>(sv) % 16) || (batch > 1 && (sv_stride % 2))) return QGB_EDECLINE;
     a.vec2 = sorted[0] == 0 ? 1 : 0;
     a.vec4 = (k >= 2 && sorted[0] == 0 && sorted[1] == 1) ? 1 : 0;
     // tile bits: the targets and the 13 - k lowest other bits
@@ -699,6 +668,28 @@ int try_dense_tc(void* sv, const void* op, int nbits, const int* sorted, const i
     a.tiles_per_state = uint64_t(1) << (nbits - 13);  // 8192 amplitudes per tile
     a.tiles = a.tiles_per_state * uint64_t(batch);
     a.sv_stride = batch > 1 ? sv_stride : 0;
+    return QGB_OK;
+}
+
+// Tensor-core path for a complex64 dense op; returns QGB_EDECLINE (and touches
+// nothing) when the op is not one it takes, so that the caller runs the
+// CUDA-core kernel instead.
+int try_dense_tc(void* sv, const void* op, int nbits, const int* sorted, const int* in_bits, const int* out_bits,
+                 int k, int64_t op_stride, int64_t batch, int64_t sv_stride, int unitary, cudaStream_t st,
+                 double* chain, int link, const double* scale) {
+    const int mode = dense_impl();
+    if (scale && unitary != 0) return QGB_EDECLINE;  // a factor goes with plain (MODE 0) passes only
+    if (unitary == 2 && (batch > 1 || !chain)) return QGB_EDECLINE;  // the chain follows one state
+    if (mode == 0 || k < 4 || k > 6 || (k == 4 && mode < 2)) return QGB_EDECLINE;
+    if (nbits < 13) return QGB_EDECLINE;              // fewer than one 8192-amplitude tile
+    if (batch > 1 && op_stride != 0) return QGB_EDECLINE;  // one operator for the whole batch
+    TcArgs a{};
+    // cp.async copies 16-byte granules: the state (and every state of a batch) must start 16-byte aligned
+    if ((reinterpret_cast<uintptr_t>(sv) % 16) || (batch > 1 && (sv_stride % 2))) return QGB_EDECLINE;
+    {
+        const int rc = build_tc_args(a, nbits, sorted, in_bits, out_bits, k, batch, sv_stride);
+        if (rc != QGB_OK) return rc;
+    }
     a.scale = scale;
     float2* s = static_cast<float2*>(sv);
     const float2* m = static_cast<const float2*>(op);

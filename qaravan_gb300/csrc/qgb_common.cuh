@@ -175,6 +175,7 @@ int try_dense_tc(void* sv, const void* op, int nbits, const int* sorted, const i
                  double* chain = nullptr, int link = 0, const double* scale = nullptr);
 int tc_status_read_clear();
 int tcs_status_read_clear();
+int dmb_status_read_clear();
 int traj_status_read_clear();
 int fuse_status_read_clear();
 }  // namespace qgb_host

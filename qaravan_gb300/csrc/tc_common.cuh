@@ -17,6 +17,30 @@ constexpr int kChainEpoch = 4;                 // passes per norm-chain epoch
 constexpr int kTcDataThreads = 256;           // 8 data warps
 constexpr int kTcThreads = kTcDataThreads + 32;  // + the MMA warp
 
+struct TcArgs {
+    int k;
+    int vec2;                            // global bit 0 is a target: components (2m, 2m+1) adjacent
+    int vec4;                            // global bits 0 and 1 are targets: rows are runs of >= 4 components
+    int L;                               // tile bits 0..L-1 are global bits 0..L-1 (L >= 7)
+    int tile_bits[13];                   // global bit of each tile bit, ascending
+    int pos_g[13];                       // tile positions of the 13 - k group bits, ascending
+    int perm_in[1 << QGB_MAX_K];         // memory-order input component j -> matrix column
+    int perm_out[1 << QGB_MAX_K];        // memory-order output component i -> matrix row
+    uint32_t uts[1 << (QGB_MAX_K - 1)];  // swizzled tile-index offsets of the low-half components
+    uint32_t ut_h;                       // tile-index offset of the upper half (target sorted[k-1])
+    uint64_t g512[16];                   // global offset of tile index 512 m
+    uint64_t off[1 << (QGB_MAX_K - 1)];  // global offsets of the low-half components
+    uint64_t hstride;                    // global offset of the upper half
+    uint64_t hoff[64];                   // global offset of tile bits L..12, indexed by u >> L
+    uint64_t tiles_per_state;            // 2^(n - 13)
+    uint64_t tiles;                      // tiles_per_state * batch
+    int64_t sv_stride;
+    double* chain;                       // norm chain (3 slots of {reference, output} squared norms) or null
+    const double* scale;                 // MODE 0: device factor f, the op applied is f * M (null: 1)
+    int c_prev, c_cur, c_next;           // slots of the previous epoch, this epoch, the next epoch (-1: none)
+    int c_head, c_tail;                  // this pass opens its epoch (corrects) / closes it (measures its output)
+};
+
 template <int K> struct TcGeom {
     static constexpr int D = 1 << K;     // complex components per group
     static constexpr int H = D / 2;      // components per thread and group
@@ -232,3 +256,9 @@ template <int N> __device__ __forceinline__ void tmem_ld_row(uint32_t taddr, flo
 }
 
 }  // namespace qgb
+
+namespace qgb_host {
+// dense_tc.cu: the geometry of one tensor-core pass (also used by the batched kernels)
+int build_tc_args(qgb::TcArgs& a, int nbits, const int* sorted, const int* in_bits, const int* out_bits, int k,
+                  int64_t batch, int64_t sv_stride);
+}  // namespace qgb_host

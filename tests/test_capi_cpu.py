@@ -148,3 +148,51 @@ def test_adjoint_sweep_host_validation(lib):
     assert b"overlap" in lib.qgb_last_error()
     assert lib.qgb_adjoint_sweep_scratch_bytes(20, 12, 64, 64) == 8 * 64 * 32 * 64
     assert lib.qgb_adjoint_sweep_scratch_bytes(24, 12, 10, 1) == 8 * 2048 * 10
+
+
+def test_dm_batch_tables_are_checked_on_the_host(lib):
+    """qgb_dm_batch_build validates circuits and passes before anything runs
+    (host code only: no GPU needed)."""
+    import ctypes as C
+    import numpy as np
+    from qaravan_gb300 import _lib
+    from qaravan_gb300.batch import _DMB_CIRC, _DMB_PASS
+    assert lib.qgb_dm_batch_circuit_bytes() == _DMB_CIRC.itemsize
+    assert lib.qgb_dm_batch_pass_bytes() == _DMB_PASS.itemsize
+
+    def tables(n=8, npass=3, **over):
+        c = np.zeros(1, dtype=_DMB_CIRC)
+        c[0] = (4096, n, 0, npass, 0)
+        p = np.zeros(npass, dtype=_DMB_PASS)
+        for j in range(npass):
+            p[j]["mat"] = 8192
+            p[j]["circ"] = 0
+            p[j]["bits"] = [0, 1, 2, 3, 4, 5]
+            p[j]["flags"] = (8 if j == 0 else 0) | (4 if j == npass - 1 else 0)
+            p[j]["tslot"] = -1
+        for k, v in over.items():
+            idx, field = k.split("_", 1)
+            p[int(idx[1:])][field] = v
+        return c, p
+
+    def build(c, p):
+        n_items = lib.qgb_dm_batch_items(c.ctypes.data, len(c), 4)
+        nbytes = lib.qgb_dm_batch_table_bytes(len(c), len(p), n_items)
+        buf = np.zeros(nbytes, dtype=np.uint8)
+        return lib.qgb_dm_batch_build(buf.ctypes.data, nbytes, c.ctypes.data, len(c), p.ctypes.data, len(p), 4)
+
+    c, p = tables()
+    assert build(c, p) == 0
+    # 8 qubits: 2^16 entries = 8 tiles -> one item per pass (items hold 16 tiles unless the pass
+    # has fewer), 3 passes, 1 finishing item; 12 qubits: 2048 tiles -> min(4, 2048 / 16) = 4 items
+    assert lib.qgb_dm_batch_items(c.ctypes.data, 1, 4) == 4
+    c12, _ = tables(n=12)
+    assert lib.qgb_dm_batch_items(c12.ctypes.data, 1, 4) == 3 * 4 + 1
+    assert build(*tables(p1_bits=[0, 1, 2, 3, 4, 4])) == _lib.QGB_EINVAL      # repeated bit
+    assert build(*tables(p1_bits=[0, 1, 2, 3, 4, 16])) == _lib.QGB_EINVAL     # bit beyond 2n
+    assert build(*tables(p1_flags=8)) == _lib.QGB_EINVAL                      # first-pass flag on pass 1
+    assert build(*tables(p2_flags=0)) == _lib.QGB_EINVAL                      # last pass not flagged
+    assert build(*tables(p2_flags=5, p2_tslot=1)) == _lib.QGB_EINVAL          # head reads a pass that is no tail
+    assert build(*tables(p1_flags=2, p2_flags=5, p2_tslot=1)) == 0             # tail then head
+    assert build(*tables(n=15)) == _lib.QGB_EINVAL                             # beyond 14 qubits
+    assert build(*tables(p0_mat=0)) == _lib.QGB_EINVAL                         # no matrix
