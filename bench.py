@@ -993,7 +993,9 @@ def run_case(args):
         gate by gate with CUDA events around every gate (default 20 1024 2);
       trajectories [qubits trajectories steps tile_bits]: the same workload in
         one persistent launch (default 18 256 2 13);
-      dm_batch [circuits seed]: the uneven noisy density-matrix batch (default 32 7)."""
+      dm_batch [circuits seed]: the uneven noisy density-matrix batch (default 32 7);
+      dm_batch_n [circuits qubits depth]: a batch of equal circuits of one size in the
+        persistent launch (default 6 12 20)."""
     import torch
     from qaravan_gb300 import build as qbuild
     qbuild.build()
@@ -1040,6 +1042,18 @@ def run_case(args):
         torch.cuda.synchronize()
         res = batch.results()
         print(f"{count} circuits: {len(batch.small)} in the batched launch, {len(batch.large)} stream-parallel; "
+              f"max trace error {max(abs(r['trace'] - 1) for r in res):.2e}")
+    elif args.case == "dm_batch_n":
+        from qaravan_gb300 import DensityMatrixSim
+        from qaravan_gb300.batch import DensityMatrixBatch
+        count, n, depth = (vals + [6, 12, 20][len(vals):])[:3]
+        sims = [DensityMatrixSim(workloads.noisy_brickwork_circuit(n, depth, 100 + j, p=1e-3), dtype=torch.complex64)
+                for j in range(count)]
+        batch = DensityMatrixBatch(sims, dtype=torch.complex64)
+        ms = _event_ms(batch.run, 1, 1)
+        res = batch.results()
+        print(f"{count} circuits of {n} qubits, depth {depth}: {len(batch.pers)} persistent, "
+              f"{batch.persistent_passes} passes, {batch.persistent_items} items, {ms:.2f} ms; "
               f"max trace error {max(abs(r['trace'] - 1) for r in res):.2e}")
     else:
         raise SystemExit(f"unknown case {args.case!r}")
