@@ -446,6 +446,14 @@ int qgb_adjoint_step_rotation(void* phi, void* lam, int dtype, int n, const int*
                               int64_t op_stride, const double* generator, int64_t batch, int64_t sv_stride,
                               double* grad_out, void* scratch, size_t scratch_bytes, void* stream);
 
+/* Register runs of the adjoint reverse sweep (qgb_adjoint_sweep_step): -1
+ * (default) or 3 groups consecutive gates whose sites fit 3 tile bits and
+ * applies each group to registers holding 8 amplitudes of the state and the
+ * co-state (one shared-memory pass and one barrier per group; real matrices,
+ * diagonals and permutations specialised); 0 runs one shared-memory pass per
+ * gate. Process-wide; results agree to rounding. No reference counterpart. */
+int qgb_set_adjoint_runs(int bits);
+
 /* Scratch bytes for qgb_adjoint_sweep_step (a function of the problem only). */
 size_t qgb_adjoint_sweep_scratch_bytes(int n, int tile_bits, int n_ops, int64_t batch);
 

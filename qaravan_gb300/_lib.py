@@ -87,6 +87,7 @@ SIGNATURES = {
     "qgb_apply_sweep": (C.c_int, [_vp, _i, _i, C.POINTER(Sweep), _vp, _i64, _i64, _i64, _vp]),
     "qgb_set_sweep_impl": (C.c_int, [_i]),
     "qgb_set_c128_arith": (C.c_int, [_i]),
+    "qgb_set_adjoint_runs": (C.c_int, [_i]),
     "qgb_apply_tc_sweep": (C.c_int, [_vp, _i, _i, C.POINTER(TcSweep), _vp, _vp, _i, _vp]),
     "qgb_dm_batch_circuit_bytes": (C.c_size_t, []),
     "qgb_dm_batch_pass_bytes": (C.c_size_t, []),

@@ -41,6 +41,12 @@ struct AdjSweepArgs {
     int gcol[QGB_SWEEP_MAX_OPS][4];
     float2 gval[QGB_SWEEP_MAX_OPS][4];  // entries of a Pauli product: 0, +-1, +-i (exact in float)
     int64_t mat_stride, batch, sv_stride;
+    // register runs: consecutive ops on at most `rbits` tile bits, applied to groups of
+    // 2^rbits amplitudes of both tiles held in registers (0: one shared-memory pass per op)
+    int rbits;
+    int run_len[QGB_SWEEP_MAX_OPS];     // at a run's first op: its op count (0 elsewhere)
+    int run_pos[QGB_SWEEP_MAX_OPS][4];  // at a run's first op: the tile bit of each local bit of the run
+    int op_lpos[QGB_SWEEP_MAX_OPS][2];  // every op's sites as local bits of its run
     uint64_t tiles;        // tiles per state
     uint64_t chunk_tiles;  // tiles per chunk
     uint64_t chunks;       // chunks over all states
@@ -246,6 +252,303 @@ __device__ __forceinline__ void adj_tile_run(cplx<T>* __restrict__ pt, cplx<T>* 
     }
 }
 
+// ---- register runs -------------------------------------------------------
+// An op of a run acts on a group of 2^R amplitudes of phi and lam held in
+// registers; local bit P of the group <-> tile bit run_pos[P]. Positions are
+// runtime values: each (R, positions) case is its own fully unrolled instance,
+// chosen by a switch. For each op: the derivative (if wanted) at the op's
+// output, Im sum_r conj(l_r) (gval_r p_{gcol_r}), then U^dagger on both --
+// dense, diagonal (two products per row) or a permutation with unit entries
+// (register moves), as classified when the state's matrices were staged.
+constexpr int kAdjDense = 0, kAdjDiag = 1, kAdjPerm = 2, kAdjReal = 3;  // kAdjReal: a dense real matrix (RY)
+
+template <int R, int P, int MODE, bool WANT, typename C, typename T>
+__device__ __forceinline__ void adj_reg1(C (&p)[1 << R], C (&l)[1 << R], const C* __restrict__ u,
+                                         const uint8_t* __restrict__ col, const float2* gv, const int* gc, T& s) {
+    constexpr int D = 1 << R, bit = 1 << P;
+    const C u0 = u[0], u1 = u[1], u2 = u[2], u3 = u[3];
+    // generator rows: one entry in {+1, -1, +i, -i} per row -- Im(conj(l) g q) is a sign times
+    // Im(conj(l) q) (g real) or Re(conj(l) q) (g imaginary): no products by g
+    const T gs0 = T(gv[0].x + gv[0].y), gs1 = T(gv[1].x + gv[1].y);
+    const bool gi0 = gv[0].y != 0.f, gi1 = gv[1].y != 0.f;
+    const int c0 = gc[0], c1 = gc[1];
+    const int k0 = col[0], k1 = col[1];
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+        if (c & bit) continue;
+        const C p0 = p[c], p1 = p[c | bit], l0 = l[c], l1 = l[c | bit];
+        if constexpr (WANT) {
+            const C q0 = c0 ? p1 : p0, q1 = c1 ? p1 : p0;
+            const T im0 = l0.x * q0.y - l0.y * q0.x, re0 = l0.x * q0.x + l0.y * q0.y;
+            const T im1 = l1.x * q1.y - l1.y * q1.x, re1 = l1.x * q1.x + l1.y * q1.y;
+            s += gs0 * (gi0 ? re0 : im0) + gs1 * (gi1 ? re1 : im1);
+        }
+        if constexpr (MODE == kAdjReal) {
+            const T a = u0.x, b = u1.x, cc = u2.x, d = u3.x;
+            p[c] = mk<T>(a * p0.x + b * p1.x, a * p0.y + b * p1.y);
+            p[c | bit] = mk<T>(cc * p0.x + d * p1.x, cc * p0.y + d * p1.y);
+            l[c] = mk<T>(a * l0.x + b * l1.x, a * l0.y + b * l1.y);
+            l[c | bit] = mk<T>(cc * l0.x + d * l1.x, cc * l0.y + d * l1.y);
+        } else if constexpr (MODE == kAdjDiag) {
+            C x = mk<T>(0, 0), y = mk<T>(0, 0), z = mk<T>(0, 0), t = mk<T>(0, 0);
+            cfma(x, u0, p0);
+            cfma(y, u3, p1);
+            cfma(z, u0, l0);
+            cfma(t, u3, l1);
+            p[c] = x;
+            p[c | bit] = y;
+            l[c] = z;
+            l[c | bit] = t;
+        } else if constexpr (MODE == kAdjPerm) {
+            p[c] = k0 ? p1 : p0;
+            p[c | bit] = k1 ? p1 : p0;
+            l[c] = k0 ? l1 : l0;
+            l[c | bit] = k1 ? l1 : l0;
+        } else {
+            C x = mk<T>(0, 0), y = mk<T>(0, 0), z = mk<T>(0, 0), t = mk<T>(0, 0);
+            cfma(x, u0, p0);
+            cfma(x, u1, p1);
+            cfma(y, u2, p0);
+            cfma(y, u3, p1);
+            cfma(z, u0, l0);
+            cfma(z, u1, l1);
+            cfma(t, u2, l0);
+            cfma(t, u3, l1);
+            p[c] = x;
+            p[c | bit] = y;
+            l[c] = z;
+            l[c | bit] = t;
+        }
+    }
+}
+
+// matrix bit 1 (most significant) <-> local bit P0 (the op's first site), bit 0 <-> P1
+template <int R, int P0, int P1, int MODE, bool WANT, typename C, typename T>
+__device__ __forceinline__ void adj_reg2(C (&p)[1 << R], C (&l)[1 << R], const C* __restrict__ u,
+                                         const uint8_t* __restrict__ col, const float2* gv, const int* gc, T& s) {
+    constexpr int D = 1 << R, b0 = 1 << P0, b1 = 1 << P1;
+    int gcr[4], colr[4];
+    T gsr[4];
+    bool gir[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        gcr[r] = gc[r];
+        colr[r] = col[r];
+        gsr[r] = T(gv[r].x + gv[r].y);
+        gir[r] = gv[r].y != 0.f;
+    }
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+        if ((c & b0) || (c & b1)) continue;
+        const int ix[4] = {c, c | b1, c | b0, c | b0 | b1};
+        C x[4], y[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            x[r] = p[ix[r]];
+            y[r] = l[ix[r]];
+        }
+        if constexpr (WANT) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                C q = x[0];  // x[gc[r]] by selects (no dynamic register indexing)
+#pragma unroll
+                for (int e = 1; e < 4; ++e)
+                    if (gcr[r] == e) q = x[e];
+                s += gsr[r] * (gir[r] ? y[r].x * q.x + y[r].y * q.y : y[r].x * q.y - y[r].y * q.x);
+            }
+        }
+        if constexpr (MODE == kAdjDiag) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const C d = u[5 * r];
+                C a = mk<T>(0, 0), b = mk<T>(0, 0);
+                cfma(a, d, x[r]);
+                cfma(b, d, y[r]);
+                p[ix[r]] = a;
+                l[ix[r]] = b;
+            }
+        } else if constexpr (MODE == kAdjPerm) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                C a = x[0], b = y[0];
+#pragma unroll
+                for (int e = 1; e < 4; ++e)
+                    if (colr[r] == e) {
+                        a = x[e];
+                        b = y[e];
+                    }
+                p[ix[r]] = a;
+                l[ix[r]] = b;
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                C a = mk<T>(0, 0), b = mk<T>(0, 0);
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const C m = u[4 * r + e];
+                    cfma(a, m, x[e]);
+                    cfma(b, m, y[e]);
+                }
+                p[ix[r]] = a;
+                l[ix[r]] = b;
+            }
+        }
+    }
+}
+
+// the op's class and derivative flag, chosen once per op (each case its own unrolled code)
+template <int R, int P, typename C, typename T>
+__device__ __forceinline__ void adj_reg1_any(C (&p)[1 << R], C (&l)[1 << R], const C* u, int mode, const uint8_t* col,
+                                             bool want, const float2* gv, const int* gc, T& s) {
+    if (want) {
+        switch (mode) {
+            case kAdjReal: adj_reg1<R, P, kAdjReal, true>(p, l, u, col, gv, gc, s); break;
+            case kAdjDiag: adj_reg1<R, P, kAdjDiag, true>(p, l, u, col, gv, gc, s); break;
+            case kAdjPerm: adj_reg1<R, P, kAdjPerm, true>(p, l, u, col, gv, gc, s); break;
+            default: adj_reg1<R, P, kAdjDense, true>(p, l, u, col, gv, gc, s); break;
+        }
+    } else {
+        switch (mode) {
+            case kAdjReal: adj_reg1<R, P, kAdjReal, false>(p, l, u, col, gv, gc, s); break;
+            case kAdjDiag: adj_reg1<R, P, kAdjDiag, false>(p, l, u, col, gv, gc, s); break;
+            case kAdjPerm: adj_reg1<R, P, kAdjPerm, false>(p, l, u, col, gv, gc, s); break;
+            default: adj_reg1<R, P, kAdjDense, false>(p, l, u, col, gv, gc, s); break;
+        }
+    }
+}
+
+template <int R, int P0, int P1, typename C, typename T>
+__device__ __forceinline__ void adj_reg2_any(C (&p)[1 << R], C (&l)[1 << R], const C* u, int mode, const uint8_t* col,
+                                             bool want, const float2* gv, const int* gc, T& s) {
+    if (want) {
+        switch (mode) {
+            case kAdjDiag: adj_reg2<R, P0, P1, kAdjDiag, true>(p, l, u, col, gv, gc, s); break;
+            case kAdjPerm: adj_reg2<R, P0, P1, kAdjPerm, true>(p, l, u, col, gv, gc, s); break;
+            default: adj_reg2<R, P0, P1, kAdjDense, true>(p, l, u, col, gv, gc, s); break;
+        }
+    } else {
+        switch (mode) {
+            case kAdjDiag: adj_reg2<R, P0, P1, kAdjDiag, false>(p, l, u, col, gv, gc, s); break;
+            case kAdjPerm: adj_reg2<R, P0, P1, kAdjPerm, false>(p, l, u, col, gv, gc, s); break;
+            default: adj_reg2<R, P0, P1, kAdjDense, false>(p, l, u, col, gv, gc, s); break;
+        }
+    }
+}
+
+template <int R, typename C, typename T>
+__device__ __forceinline__ void adj_apply1(C (&p)[1 << R], C (&l)[1 << R], int P, const C* u, int mode,
+                                           const uint8_t* col, bool want, const float2* gv, const int* gc, T& s) {
+    switch (P) {
+        case 0: adj_reg1_any<R, 0>(p, l, u, mode, col, want, gv, gc, s); break;
+        case 1: if constexpr (R > 1) adj_reg1_any<R, 1>(p, l, u, mode, col, want, gv, gc, s); break;
+        case 2: if constexpr (R > 2) adj_reg1_any<R, 2>(p, l, u, mode, col, want, gv, gc, s); break;
+        case 3: if constexpr (R > 3) adj_reg1_any<R, 3>(p, l, u, mode, col, want, gv, gc, s); break;
+    }
+}
+
+template <int R, int CODE, typename C, typename T>
+__device__ __forceinline__ void adj_apply2_case(C (&p)[1 << R], C (&l)[1 << R], const C* u, int mode,
+                                                const uint8_t* col, bool want, const float2* gv, const int* gc, T& s) {
+    constexpr int P0 = CODE / 4, P1 = CODE % 4;
+    if constexpr (P0 < R && P1 < R && P0 != P1) adj_reg2_any<R, P0, P1>(p, l, u, mode, col, want, gv, gc, s);
+}
+
+template <int R, typename C, typename T>
+__device__ __forceinline__ void adj_apply2(C (&p)[1 << R], C (&l)[1 << R], int P0, int P1, const C* u, int mode,
+                                           const uint8_t* col, bool want, const float2* gv, const int* gc, T& s) {
+    switch (P0 * 4 + P1) {
+        case 1: adj_apply2_case<R, 1>(p, l, u, mode, col, want, gv, gc, s); break;
+        case 2: adj_apply2_case<R, 2>(p, l, u, mode, col, want, gv, gc, s); break;
+        case 3: adj_apply2_case<R, 3>(p, l, u, mode, col, want, gv, gc, s); break;
+        case 4: adj_apply2_case<R, 4>(p, l, u, mode, col, want, gv, gc, s); break;
+        case 6: adj_apply2_case<R, 6>(p, l, u, mode, col, want, gv, gc, s); break;
+        case 7: adj_apply2_case<R, 7>(p, l, u, mode, col, want, gv, gc, s); break;
+        case 8: adj_apply2_case<R, 8>(p, l, u, mode, col, want, gv, gc, s); break;
+        case 9: adj_apply2_case<R, 9>(p, l, u, mode, col, want, gv, gc, s); break;
+        case 11: adj_apply2_case<R, 11>(p, l, u, mode, col, want, gv, gc, s); break;
+        case 12: adj_apply2_case<R, 12>(p, l, u, mode, col, want, gv, gc, s); break;
+        case 13: adj_apply2_case<R, 13>(p, l, u, mode, col, want, gv, gc, s); break;
+        case 14: adj_apply2_case<R, 14>(p, l, u, mode, col, want, gv, gc, s); break;
+    }
+}
+
+// Every run of the pass on one staged pair of tiles: groups of 2^R amplitudes,
+// one group per thread at a time, a barrier after each run. umode / ucol: each
+// op's U^dagger class and, for a permutation, its source column per row.
+template <typename T, int R>
+__device__ __forceinline__ void adj_tile_runs(cplx<T>* __restrict__ pt, cplx<T>* __restrict__ lt, int m,
+                                              const AdjSweepArgs& a, const cplx<T>* __restrict__ ush,
+                                              const uint8_t* __restrict__ umode, const uint8_t* __restrict__ ucol,
+                                              double* __restrict__ red, int tid, int nthr) {
+    using C = cplx<T>;
+    constexpr int D = 1 << R;
+    const int warp = tid >> 5, lane = tid & 31;
+    for (int i0 = 0; i0 < a.n_ops;) {
+        const int nr = a.run_len[i0];
+        int rp[R], srt[R];
+#pragma unroll
+        for (int j = 0; j < R; ++j) rp[j] = srt[j] = a.run_pos[i0][j];
+#pragma unroll
+        for (int x = 1; x < R; ++x)
+#pragma unroll
+            for (int y = x; y > 0; --y)
+                if (srt[y - 1] > srt[y]) {
+                    const int t = srt[y];
+                    srt[y] = srt[y - 1];
+                    srt[y - 1] = t;
+                }
+        uint32_t soff[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            uint32_t o = 0;
+#pragma unroll
+            for (int j = 0; j < R; ++j) o |= uint32_t((c >> j) & 1) << rp[j];
+            soff[c] = swz<T>(o);
+        }
+        const uint32_t groups = 1u << (m - R);
+        for (uint32_t gb = 0; gb < groups; gb += uint32_t(nthr)) {  // every thread the same trip count
+            const uint32_t g = gb + uint32_t(tid);
+            const bool ok = g < groups;
+            uint32_t base = ok ? g : 0u;
+#pragma unroll
+            for (int j = 0; j < R; ++j) base = ((base >> srt[j]) << (srt[j] + 1)) | (base & ((1u << srt[j]) - 1));
+            const uint32_t sb = swz<T>(base);
+            C p[D], l[D];
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                p[c] = ok ? pt[sb ^ soff[c]] : mk<T>(T(0), T(0));
+                l[c] = ok ? lt[sb ^ soff[c]] : mk<T>(T(0), T(0));
+            }
+            for (int q = 0; q < nr; ++q) {
+                const int op = i0 + q;
+                const bool want = a.op_out[op] >= 0;
+                T sd = T(0);
+                if (a.op_k[op] == 1)
+                    adj_apply1<R>(p, l, a.op_lpos[op][0], ush + op * 16, umode[op], ucol + op * 4, want, a.gval[op],
+                                  a.gcol[op], sd);
+                else
+                    adj_apply2<R>(p, l, a.op_lpos[op][0], a.op_lpos[op][1], ush + op * 16, umode[op], ucol + op * 4,
+                                  want, a.gval[op], a.gcol[op], sd);
+                if (want) {  // uniform over the CTA: every lane reaches the shuffles
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) sd += __shfl_xor_sync(0xffffffffu, sd, o);
+                    if (lane == 0) red[op * kAdjMaxWarps + warp] += double(sd);
+                }
+            }
+            if (ok) {
+#pragma unroll
+                for (int c = 0; c < D; ++c) {
+                    pt[sb ^ soff[c]] = p[c];
+                    lt[sb ^ soff[c]] = l[c];
+                }
+            }
+        }
+        __syncthreads();
+        i0 += nr;
+    }
+}
+
 // Length of the run of ops starting at op0 on the same sites (same k and tile bits, in order).
 __device__ __forceinline__ int adj_run_length(const AdjSweepArgs& a, int op0) {
     int r = 1;
@@ -280,11 +583,13 @@ __global__ void __launch_bounds__(kAdjMaxThreads) adjoint_sweep_kernel(cplx<T>* 
     const int L = a.L, H = a.H, m = a.m;
     const int nwarps = blockDim.x >> 5;
     // layout: nbuf x (phi tile, lam tile) | ush (n_ops x 16 complex: U^dagger of the current state) |
-    //         hoff (2^H uint64) | red (n_ops x kAdjMaxWarps double)
+    //         hoff (2^H uint64) | red (n_ops x kAdjMaxWarps double) | umode (n_ops) | ucol (n_ops x 4)
     C* bufs = reinterpret_cast<C*>(smem_raw);
     C* ush = bufs + (size_t(2 * nbuf) << m);
     uint64_t* hoff = reinterpret_cast<uint64_t*>(ush + size_t(a.n_ops) * 16);
     double* red = reinterpret_cast<double*>(hoff + (size_t(1) << H));
+    uint8_t* umode = reinterpret_cast<uint8_t*>(red + size_t(a.n_ops) * kAdjMaxWarps);
+    uint8_t* ucol = umode + a.n_ops;
     int64_t staged = -1;  // state whose matrices sit in ush
     for (uint32_t h = threadIdx.x; h < (1u << H); h += blockDim.x) {
         uint64_t o = 0;
@@ -340,13 +645,43 @@ __global__ void __launch_bounds__(kAdjMaxThreads) adjoint_sweep_kernel(cplx<T>* 
                     ush[e] = mk<T>(u.x, -u.y);
                 }
             }
+            if (a.rbits > 0) {
+                __syncthreads();
+                // classify each op's U^dagger: diagonal, a permutation with unit entries, or dense
+                for (int op = threadIdx.x; op < a.n_ops; op += blockDim.x) {
+                    const int d = 1 << a.op_k[op];
+                    const C* u = ush + op * 16;
+                    bool diag = true, perm = true, real = true;
+                    for (int r = 0; r < d; ++r) {
+                        int nz = 0, cc = 0;
+                        for (int c = 0; c < d; ++c) {
+                            const C v = u[r * d + c];
+                            const bool z = v.x == T(0) && v.y == T(0);
+                            if (v.y != T(0)) real = false;
+                            if (r != c && !z) diag = false;
+                            if (!z) {
+                                ++nz;
+                                cc = c;
+                                perm = perm && v.x == T(1) && v.y == T(0);
+                            }
+                        }
+                        perm = perm && nz == 1;
+                        ucol[op * 4 + r] = uint8_t(cc);
+                    }
+                    umode[op] = uint8_t(diag ? kAdjDiag : (perm ? kAdjPerm : ((real && d == 2) ? kAdjReal : kAdjDense)));
+                }
+            }
             staged = b;
         }
         __syncthreads();
-        for (int op = 0; op < a.n_ops;) {
-            op += a.op_k[op] == 1 ? adj_tile_ops<T, 1>(pt, lt, m, a, op, ush, red, threadIdx.x, blockDim.x)
-                                  : adj_tile_ops<T, 2>(pt, lt, m, a, op, ush, red, threadIdx.x, blockDim.x);
-            __syncthreads();
+        if (a.rbits == 3) {
+            adj_tile_runs<T, 3>(pt, lt, m, a, ush, umode, ucol, red, threadIdx.x, blockDim.x);
+        } else {
+            for (int op = 0; op < a.n_ops;) {
+                op += a.op_k[op] == 1 ? adj_tile_ops<T, 1>(pt, lt, m, a, op, ush, red, threadIdx.x, blockDim.x)
+                                      : adj_tile_ops<T, 2>(pt, lt, m, a, op, ush, red, threadIdx.x, blockDim.x);
+                __syncthreads();
+            }
         }
         const uint64_t base = base_of(w);
         for (uint32_t e = per16 * threadIdx.x; e < (1u << m); e += per16 * blockDim.x) {
@@ -398,7 +733,7 @@ namespace {
 template <typename T>
 size_t adj_smem_bytes(int m, int H, int n_ops, int nbuf) {
     return sizeof(cplx<T>) * ((size_t(2 * nbuf) << m) + size_t(n_ops) * 16) + sizeof(uint64_t) * (size_t(1) << H) +
-           sizeof(double) * size_t(n_ops) * kAdjMaxWarps;
+           sizeof(double) * size_t(n_ops) * kAdjMaxWarps + size_t(n_ops) * 5;
 }
 
 template <typename T>
@@ -432,7 +767,23 @@ int launch_adj(void* phi, void* lam, const void* mats, const AdjSweepArgs& a, do
     return set_error(QGB_EINVAL, "adjoint sweep tile of 2^%d amplitudes does not fit in shared memory", a.m);
 }
 
+int g_adj_run_bits = -1;  // register runs: -1 default (on), 0 per-op passes
+
+// Register runs span 3 tile bits (8-amplitude groups of both tiles); 16-amplitude
+// groups measured slower (more registers and code per op) and are not built.
+int adj_run_bits(int dtype) {
+    (void)dtype;
+    return g_adj_run_bits == 0 ? 0 : 3;
+}
+
 }  // namespace
+
+extern "C" int qgb_set_adjoint_runs(int bits) {
+    if (bits != -1 && bits != 0 && bits != 3)
+        return set_error(QGB_EINVAL, "adjoint register-run width %d (-1 default, 0 off, 3)", bits);
+    g_adj_run_bits = bits;
+    return QGB_OK;
+}
 
 extern "C" size_t qgb_adjoint_sweep_scratch_bytes(int n, int tile_bits, int n_ops, int64_t batch) {
     if (n < 1 || n > QGB_MAX_QUBITS || tile_bits < 1 || tile_bits > n || n_ops < 1 || n_ops > QGB_SWEEP_MAX_OPS ||
@@ -515,6 +866,35 @@ extern "C" int qgb_adjoint_sweep_step(void* phi, void* lam, int dtype, int n, co
         }
     }
     if (any_out && !grad_out) return set_error(QGB_EINVAL, "derivatives requested without an output");
+    // register runs: greedy, consecutive ops while their sites fit rbits tile bits
+    a.rbits = adj_run_bits(dtype);
+    if (a.rbits > m) a.rbits = m;
+    if (a.rbits >= 3) {
+        for (int i0 = 0; i0 < sw.n_ops;) {
+            uint32_t bits = 0;
+            int i = i0;
+            for (; i < sw.n_ops; ++i) {
+                uint32_t nb = bits;
+                for (int j = 0; j < a.op_k[i]; ++j) nb |= 1u << a.op_pos[i][j];
+                if (__builtin_popcount(nb) > a.rbits) break;
+                bits = nb;
+            }
+            // the run's local bits: its own tile bits ascending, then the lowest unused ones
+            int nrp = 0;
+            for (int b = 0; b < m && nrp < a.rbits; ++b)
+                if ((bits >> b) & 1u) a.run_pos[i0][nrp++] = b;
+            for (int b = 0; b < m && nrp < a.rbits; ++b)
+                if (!((bits >> b) & 1u)) a.run_pos[i0][nrp++] = b;
+            a.run_len[i0] = i - i0;
+            for (int o = i0; o < i; ++o)
+                for (int j = 0; j < a.op_k[o]; ++j)
+                    for (int r = 0; r < a.rbits; ++r)
+                        if (a.run_pos[i0][r] == a.op_pos[o][j]) a.op_lpos[o][j] = r;
+            i0 = i;
+        }
+    } else {
+        a.rbits = 0;
+    }
     a.mat_stride = batch > 1 ? mat_stride : 0;
     a.batch = batch;
     a.sv_stride = batch > 1 ? sv_stride : 0;

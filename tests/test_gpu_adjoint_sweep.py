@@ -1,8 +1,11 @@
 """The adjoint tile sweep (many gates per pass over state and co-state) against
 the per-gate reverse steps through the C ABI: final states, co-states and every
 rotation derivative, for batches with per-state matrices, 1- and 2-site gates
-on low and high bits and tiles that force several passes; and the batched
-ansatz with and without tile passes."""
+(dense, diagonal, and permutations such as CNOT, SWAP, X) on low and high bits,
+tiles that force several passes, with the gates applied in register runs
+(the default: consecutive gates on at most 3 tile bits per shared-memory pass)
+and one shared-memory pass per gate; and the batched ansatz with and without
+tile passes."""
 import ctypes as C
 
 import numpy as np
@@ -23,9 +26,22 @@ def _haar(d, rng):
     return q * (np.diag(r) / np.abs(np.diag(r)))
 
 
+_PERMS = [np.array([[0, 1], [1, 0]], complex),                                       # X
+          np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 0, 1], [0, 0, 1, 0]], complex),  # CNOT
+          np.array([[1, 0, 0, 0], [0, 0, 1, 0], [0, 1, 0, 0], [0, 0, 0, 1]], complex)]  # SWAP
+
+
+@pytest.fixture(params=[-1, 0], ids=["register_runs", "pass_per_gate"])
+def runs(request):
+    from qaravan_gb300 import _lib
+    _lib.check(_lib.lib().qgb_set_adjoint_runs(request.param), "set_adjoint_runs")
+    yield request.param
+    _lib.lib().qgb_set_adjoint_runs(-1)
+
+
 @pytest.mark.parametrize("dtype,tol", [(torch.complex64, 2e-5), (torch.complex128, 1e-12)])
 @pytest.mark.parametrize("n,tile", [(9, 6), (11, 8), (7, 7)])
-def test_adjoint_sweep_matches_per_gate_steps(dtype, tol, n, tile):
+def test_adjoint_sweep_matches_per_gate_steps(dtype, tol, n, tile, runs):
     from qaravan_gb300 import _lib
     from qaravan_gb300.adjoint import _GEN, _GEN_C, _adjoint_sweep_struct, _plan_reverse
     L = _lib.lib()
@@ -49,6 +65,8 @@ def test_adjoint_sweep_matches_per_gate_steps(dtype, tol, n, tile):
             if kind:
                 t = rng.uniform(-3, 3)
                 m = np.cos(t) * np.eye(d) - 1j * np.sin(t) * _GEN[kind]
+            elif g % 3 == 0:  # fixed permutation gates: X, CNOT, SWAP
+                m = _PERMS[0] if d == 2 else _PERMS[1 + (g // 3) % 2]
             else:
                 m = _haar(d, rng)
             mats[s, g, :d * d] = m.reshape(-1)
@@ -98,7 +116,7 @@ def test_adjoint_sweep_matches_per_gate_steps(dtype, tol, n, tile):
 
 
 @pytest.mark.parametrize("dtype,tol", [(torch.complex64, 2e-5), (torch.complex128, 1e-11)])
-def test_batched_ansatz_tile_passes_match_per_gate_passes(dtype, tol):
+def test_batched_ansatz_tile_passes_match_per_gate_passes(dtype, tol, runs):
     from qaravan_gb300 import workloads
     from qaravan_gb300.adjoint import BatchedAnsatz
     n, layers, P = 14, 4, 5
