@@ -140,40 +140,27 @@ def _cpu_threads():
     return threads
 
 
-def cpu_depth_unit_c64(gates, n, reps=1):
-    """The reference's torch backend on the host cores (complex64; op_action =
-    permute + tensordot on torch CPU tensors, restated in oracle/): seconds per
-    gate over `reps` passes of the circuit's first depth unit."""
-    import torch
+def cpu_baseline(gates, n, depth, numpy_gates=4):
+    """The reference's CPU path on the host cores, all threads: the reference arm
+    of this script (its torch backend in complex64 -- the benchmark's own dtype --
+    over the circuit's first depth unit, 5 steps of 11 gates after 3 warm-up
+    gates) run as a fresh child process, so that this figure and the reference
+    arm's line are one measurement on a clean process (timed here, after the GPU
+    sections, the same gates ran at about half that rate); beside it the numpy
+    complex128 path on a few gates of that unit, and the 12-qubit depth-20
+    complex128 circuit run whole (median of 5)."""
+    import subprocess
+    import sys
     from oracle import ref
-    unit = depth_unit(gates, n)
-    mats = [torch.tensor(np.asarray(g.matrix), dtype=torch.complex64) for g in unit]
-    state = torch.zeros([2] * n, dtype=torch.complex64)
-    state.view(-1)[0] = 1
-    state = ref.op_action_torch(mats[0], unit[0].indices, state)  # warm-up (allocator, BLAS threads)
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        for m, g in zip(mats, unit):
-            state = ref.op_action_torch(m, g.indices, state)
-    dt = time.perf_counter() - t0
-    del state
-    return dt / (reps * len(unit)), len(unit)
-
-
-def cpu_baseline(gates, n, numpy_gates=4):
-    """The reference's CPU path on the host cores, all threads: one full depth unit
-    (55 gates at 28 qubits) through its torch backend in complex64 -- the
-    benchmark's own dtype -- extrapolated to the circuit by the gate count;
-    beside it the numpy complex128 path on a few gates of that unit, and the
-    12-qubit depth-20 complex128 circuit run whole (median of 5)."""
-    from oracle import ref
-    threads = _cpu_threads()
-    s_per_gate, ngates = cpu_depth_unit_c64(gates, n)
-    out = {"value": round(1.0 / s_per_gate, 4), "unit": "gates/s", "cores": threads, "kind": "port",
-           "sample": f"one full depth unit ({ngates} gates: {n} SU(2) + {n - 1} SU(4)) of the {n}-qubit brickwork, "
-                     f"complex64, the reference torch backend's op_action (permute + tensordot on CPU tensors, "
-                     f"restated in oracle/), {ngates * s_per_gate:.1f} s; the {len(gates)}-gate circuit "
-                     f"extrapolates to {len(gates) * s_per_gate:.0f} s"}
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "LOCAL_RANK", "WORLD_SIZE", "MASTER_ADDR",
+                                                            "MASTER_PORT", "LOCAL_WORLD_SIZE", "GROUP_RANK")}
+    env["CUDA_VISIBLE_DEVICES"] = ""
+    cmd = [sys.executable, os.path.abspath(__file__), "--impl", "reference", "--steps", "5", "--warmup", "3",
+           "--qubits", str(n), "--depth", str(depth)]
+    res = subprocess.run(cmd, env=env, capture_output=True, text=True, timeout=900, check=True)
+    line = [ln for ln in res.stdout.splitlines() if ln.startswith("{")][-1]
+    out = dict(json.loads(line)["cpu_baseline"])
+    out["sample"] += "; measured by the reference arm of this script (--impl reference) in a child process"
     # numpy complex128 (the reference's default backend) on the first gates of the same unit
     unit = depth_unit(gates, n)
     state = ref.initial_sv(n)
@@ -886,7 +873,8 @@ def gpu_arm(args):
             except Exception as e:  # secondary sections never suppress the headline line
                 sections[name] = {"error": f"{type(e).__name__}: {str(e)[:300]}"}
             torch.cuda.empty_cache()
-    cpu = None if args.no_cpu else cpu_baseline(gates, n)
+    # the CPU baseline is rank 0's at N=1 only
+    cpu = None if (args.no_cpu or world > 1) else cpu_baseline(gates, n, args.depth)
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": "gates/s", "n_gates": gates_per_step,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
@@ -945,7 +933,7 @@ def reference_arm(args):
            "sample": f"{applied} gates ({per_step} per step) of the first depth unit ({len(unit)} gates: {n} SU(2) + "
                      f"{n - 1} SU(4)) of the {n}-qubit brickwork, complex64, the reference torch backend's op_action "
                      f"(permute + tensordot on CPU tensors, restated in oracle/); the {len(gates)}-gate circuit "
-                     f"extrapolates to {len(gates) / value:.0f} s"}
+                     f"extrapolates to {len(gates) / value:.3g} s"}
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "gates/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 1),
