@@ -542,6 +542,16 @@ def section_adjoint_batch(n=20, layers=40, sets=64, single_sample=8):
     t_batch = time.perf_counter() - t0
     peak = torch.cuda.max_memory_allocated() - base
     E, grad = E.cpu().numpy(), grad.cpu().numpy()
+    # the same batch with the forward as one tile-pass op per gate (no fused blocks)
+    b_pg = BatchedAnsatz.hea(n, layers, dtype=torch.complex64, fused_width=0)
+    b_pg.energy_and_grad(flat, terms)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, g_pg = b_pg.energy_and_grad(flat, terms)
+    torch.cuda.synchronize()
+    t_pg = time.perf_counter() - t0
+    g_pg = g_pg.cpu().numpy()
+    del b_pg
 
     def single(s):
         th = torch.tensor(pset[s], dtype=torch.float64, requires_grad=True)
@@ -575,6 +585,10 @@ def section_adjoint_batch(n=20, layers=40, sets=64, single_sample=8):
     return {"qubits": n, "layers": layers, "parameter_sets": sets, "params_per_set": 2 * n * layers,
             "gates_per_set": len(ba.gates), "dtype": "c64",
             "batched_s": round(t_batch, 4), "gradients_per_s": round(sets / t_batch, 2),
+            "forward": {"fused_blocks": ba._fused["blocks"] if ba._fused else None,
+                        "fused_passes": ba._fused["passes"] if ba._fused else None,
+                        "per_gate_forward_batched_s": round(t_pg, 4),
+                        "max_rel_grad_diff_fused_vs_per_gate": float(np.abs(grad - g_pg).max() / np.abs(g_pg).max())},
             "peak_state_multiples_per_set": round(peak / (sets * 2 ** n * 8), 2),
             "single_set_adjoint_s": round(t_single, 4),
             "speedup_vs_single_set_adjoint": round(t_single * sets / t_batch, 2),
@@ -639,9 +653,12 @@ def section_dm_batch(count=256, seed=7):
     from qaravan_gb300.batch import DensityMatrixBatch
     specs = workloads.uneven_dm_specs(count, seed)
     t0 = time.perf_counter()
-    sims = [DensityMatrixSim(workloads.noisy_brickwork_circuit(n, d, s, p=1e-3), dtype=torch.complex64)
-            for n, d, s in specs]
+    circs = [workloads.noisy_brickwork_circuit(n, d, s, p=1e-3) for n, d, s in specs]
+    gen_s = time.perf_counter() - t0  # the synthetic input: seeded Haar gates and noise carriers
+    t0 = time.perf_counter()
+    sims = [DensityMatrixSim(c, dtype=torch.complex64) for c in circs]
     batch = DensityMatrixBatch(sims, dtype=torch.complex64)
+    torch.cuda.synchronize()
     compile_s = time.perf_counter() - t0
     ms = _event_ms(lambda: batch.run(graph=True), 1, 1)
     res = batch.results()
@@ -654,7 +671,7 @@ def section_dm_batch(count=256, seed=7):
     out = {"circuits": count, "small_batched": len(batch.small), "persistent": len(batch.pers),
            "stream_parallel": len(batch.large), "launches_per_batch": batch.launches,
            "persistent_items": getattr(batch, "persistent_items", 0),
-           "compile_s": round(compile_s, 2), "ms_per_batch": round(ms, 1),
+           "circuit_generation_s": round(gen_s, 2), "compile_s": round(compile_s, 2), "ms_per_batch": round(ms, 1),
            "circuits_per_s": round(count / (ms / 1e3), 2),
            "max_trace_error": float(max(abs(r["trace"] - 1) for r in res)),
            "state_gb": round(sum(4 ** n * 8 for n, _, _ in specs) / 1e9, 1),

@@ -244,6 +244,22 @@ def _forward_sweep_struct(L, high, ops):
     return sw
 
 
+def _forward_sweep_struct_pos(L, high, ops):
+    """``qgb_sweep`` for one pass; ``ops``: (tile positions in matrix order, matrix element offset)."""
+    sw = _lib.Sweep()
+    sw.low_bits = L
+    sw.n_high = len(high)
+    for i, b in enumerate(high):
+        sw.high_bits[i] = b
+    sw.n_ops = len(ops)
+    for i, (pos, off) in enumerate(ops):
+        sw.op_k[i] = len(pos)
+        for j, p in enumerate(pos):
+            sw.op_pos[i][j] = p
+        sw.op_mat[i] = int(off)
+    return sw
+
+
 def _rotation_angle(g):
     """The torch angle of a rotation gate whose matrix is still the one built
     from it, else None."""
@@ -424,6 +440,63 @@ def adjoint_energy(sim, terms):
 # ------------------------------------------------------------ parameter-set batches
 
 
+def plan_fused_forward(n, gate_bits, fixed, width, itemsize):
+    """The forward pass of a parametrised gate structure as fused blocks of
+    ``width`` qubits in tile sweeps. The block structure is planned once (the
+    fusion compiler on the gate bits ``gate_bits`` -- flat bits in matrix order
+    per gate -- with the fixed gates' matrices ``fixed`` ((gate, matrix) pairs)
+    and unit placeholders for the rotations, which are unitary at every angle);
+    each call then composes every parameter set's block matrices on the device
+    (``qgb_fuse_blocks``, float64 products) from that set's gate matrices, laid
+    out [set][gate][16]. Returns the tables of one set -- ``blocks1`` (block
+    matrix at element ``out`` of the set's ``total``), ``ents1`` (gate g's matrix
+    at element 16 g) -- and the sweeps as (low bits, high bits, [(tile positions,
+    block offset)]), or None when the plan is not all device-fused tile sweeps."""
+    from .compiler import Recipe, SweepStep
+    from .engine import _FUSE_BLOCK, _FUSE_ENTRY
+    G = len(gate_bits)
+    fixed_m = dict(fixed)
+    ops = [Op(gate_bits[g], fixed_m[g] if g in fixed_m else np.eye(2 ** len(gate_bits[g]), dtype=np.complex128))
+           for g in range(G)]
+    plan = compile_ops(ops, n, mode="sweep", width=width, tile_bits=13, max_sweep_k=min(width, 4),
+                       itemsize=itemsize, device_fusion=True)
+    if not plan.matrices or not all(isinstance(m, Recipe) for m in plan.matrices) or \
+            not all(isinstance(st, SweepStep) for st in plan.steps):
+        return None
+    offs, total, ents1 = [], 0, []
+    blocks1 = np.zeros(len(plan.matrices), dtype=_FUSE_BLOCK)
+    for i, r in enumerate(plan.matrices):
+        offs.append(total)
+        pos_of = {b: j for j, b in enumerate(r.bits)}
+        blocks1[i] = (total, len(r.bits), len(ents1), len(ents1) + len(r.entries), 0)
+        for mi, obits in r.entries:
+            ents1.append((len(obits), [pos_of[b] for b in obits] + [0] * (6 - len(obits)), 0, mi * 16))
+        total += 4 ** len(r.bits)
+    ents1 = np.array(ents1, dtype=_FUSE_ENTRY)
+    sweeps = [(st.low_bits, list(st.high_bits), [(list(pos), offs[mi]) for pos, mi in st.ops]) for st in plan.steps]
+    tmpl = np.zeros((G, 16), dtype=np.complex128)
+    for g, m in fixed:
+        tmpl[g, :m.size] = m.reshape(-1)
+    return {"blocks1": blocks1, "ents1": ents1, "total": total, "sweeps": sweeps, "template": tmpl,
+            "passes": len(plan.steps), "blocks": len(plan.matrices)}
+
+
+def fused_tables(fplan, nsets, ngates):
+    """The block and entry tables of ``nsets`` parameter sets, one host byte
+    buffer: set s's blocks write at ``s * total`` and read its gate matrices at
+    ``s * ngates * 16``. Returns (buffer, byte offset of the entries)."""
+    blocks = np.tile(fplan["blocks1"], nsets)
+    ents = np.tile(fplan["ents1"], nsets)
+    nb1, ne1 = len(fplan["blocks1"]), len(fplan["ents1"])
+    s = np.repeat(np.arange(nsets, dtype=np.int64), nb1)
+    blocks["out"] += s * fplan["total"]
+    blocks["op_begin"] += (s * ne1).astype(np.int32)
+    blocks["op_end"] += (s * ne1).astype(np.int32)
+    ents["mat"] += np.repeat(np.arange(nsets, dtype=np.int64), ne1) * (ngates * 16)
+    pad = (-blocks.nbytes) % 16
+    return np.concatenate([blocks.view(np.uint8), np.zeros(pad, np.uint8), ents.view(np.uint8)]), blocks.nbytes + pad
+
+
 class BatchedAnsatz:
     """Energies and angle gradients of one parametrised circuit structure for
     many parameter sets at once (the reference differentiates one set at a time
@@ -445,7 +518,8 @@ class BatchedAnsatz:
     ``qgb_adjoint_sweep_step``; ``tile_bits=0`` runs one pass per gate.
     Memory: three states per set."""
 
-    def __init__(self, n, gates, nparams=None, dtype=torch.complex64, device="cuda", tile_bits=None):
+    def __init__(self, n, gates, nparams=None, dtype=torch.complex64, device="cuda", tile_bits=None,
+                 fused_width=4):
         self.n = int(n)
         self.dtype, self.device = dtype, torch.device(device)
         if self.device.type != "cuda":
@@ -492,18 +566,60 @@ class BatchedAnsatz:
         # every set's own matrices; reverse: the adjoint sweep, derivative slot = gate index.
         self.tile_bits = _tile_bits(dtype) if tile_bits is None else int(tile_bits)
         self._fwd, self._rev = [], []
+        self._fused = None
         if self.tile_bits > 0:
             bits = [[self.n - 1 - q for q in idx] for _, idx, _ in self.gates]
-            fwd_tile = min(self.tile_bits + 1, self.n)  # one state only: twice the tile of the reverse pass
-            for lo, high, ops in _plan_reverse([(g, bits[g]) for g in range(len(bits))], self.n, fwd_tile):
-                self._fwd.append(_forward_sweep_struct(lo, high, [(b, g * 16) for g, b in ops]))
+            if fused_width:
+                isz = torch.empty(0, dtype=self.dtype).element_size()
+                self._fused = plan_fused_forward(self.n, bits, fixed, int(fused_width), isz)
+            if self._fused is not None:
+                L = _lib.lib()
+                if L.qgb_fuse_block_bytes() != self._fused["blocks1"].itemsize or \
+                        L.qgb_fuse_entry_bytes() != self._fused["ents1"].itemsize:
+                    raise _lib.QgbError("fusion table layout mismatch with the library")
+                self._fused["template_dev"] = torch.from_numpy(self._fused["template"]).to(self.device)
+                self._fused["sweep_structs"] = [_forward_sweep_struct_pos(lo, high, ops)
+                                                for lo, high, ops in self._fused["sweeps"]]
+            if self._fused is None:
+                fwd_tile = min(self.tile_bits + 1, self.n)  # one state only: twice the tile of the reverse pass
+                for lo, high, ops in _plan_reverse([(g, bits[g]) for g in range(len(bits))], self.n, fwd_tile):
+                    self._fwd.append(_forward_sweep_struct(lo, high, [(b, g * 16) for g, b in ops]))
             tile = min(self.tile_bits, self.n)
             for lo, high, ops in _plan_reverse([(g, bits[g]) for g in reversed(range(len(bits)))], self.n, tile):
                 self._rev.append(_adjoint_sweep_struct(lo, high, [(b, g * 16, g if kinds[g] else -1, kinds[g])
                                                                   for g, b in ops]))
 
+    def _fused_tables(self, P):
+        """Device copy of the fused forward's tables for ``P`` sets (kept for the
+        next call with the same ``P``)."""
+        f = self._fused
+        if f.get("sets") != P:
+            host, f["ent_start"] = fused_tables(f, P, len(self.gates))
+            f["tables"] = torch.from_numpy(host).to(self.device)
+            f["sets"] = P
+        return f["tables"]
+
+    def _forward_fused(self, psi, params, P, st):
+        """Composes every set's block matrices and applies the fused sweeps to the
+        ``P`` states in ``psi`` (|0> on entry)."""
+        L = _lib.lib()
+        f = self._fused
+        G, N = len(self.gates), 2 ** self.n
+        tables = self._fused_tables(P)
+        opm = f["template_dev"].unsqueeze(0).expand(P, G, 16).contiguous()
+        _lib.check(L.qgb_param_matrices(self._kinds.data_ptr(), self._pidx.data_ptr(), G, params.data_ptr(),
+                                        self.nparams, P, opm.data_ptr(), _lib.QGB_C128, 16, 16 * G, st),
+                   "param_matrices")
+        fused = torch.empty(P * f["total"], dtype=self.dtype, device=self.device)
+        _lib.check(L.qgb_fuse_blocks(fused.data_ptr(), self.code, fused.numel(), tables.data_ptr(),
+                                     P * len(f["blocks1"]), tables.data_ptr() + f["ent_start"],
+                                     P * len(f["ents1"]), opm.data_ptr(), opm.numel(), st), "fuse_blocks")
+        for sw in f["sweep_structs"]:
+            _lib.check(L.qgb_apply_sweep(psi.data_ptr(), self.code, self.n, C.byref(sw), fused.data_ptr(),
+                                         f["total"], P, N, st), "apply_sweep")
+
     @classmethod
-    def hea(cls, n, layers, dtype=torch.complex64, device="cuda"):
+    def hea(cls, n, layers, dtype=torch.complex64, device="cuda", fused_width=4):
         """The hardware-efficient ansatz of the adjoint benchmark: per layer RY(theta)
         then RZ(phi) on every qubit, then a CNOT ladder; parameter index
         2 * (l * n + q) + (0 theta, 1 phi), the flattening of ``workloads.hea_params``."""
@@ -516,7 +632,7 @@ class BatchedAnsatz:
             for q in range(n - 1):
                 g = CNOT([q + 1, q], n)  # the gate object of workloads.hea_circuit (its own site order)
                 gates.append(("fixed", list(g.indices), np.asarray(g.matrix, dtype=np.complex128)))
-        return cls(n, gates, nparams=2 * layers * n, dtype=dtype, device=device)
+        return cls(n, gates, nparams=2 * layers * n, dtype=dtype, device=device, fused_width=fused_width)
 
     def _matrices(self, params, P):
         G = len(self.gates)
@@ -543,7 +659,9 @@ class BatchedAnsatz:
         _lib.check(L.qgb_init_basis(psi.data_ptr(), self.code, n, 0, P, N, st), "init")
         base = mats.data_ptr()
         set_stride = 16 * len(self.gates)
-        if self._fwd:
+        if self._fused is not None:
+            self._forward_fused(psi, params, P, st)
+        elif self._fwd:
             for sw in self._fwd:
                 _lib.check(L.qgb_apply_sweep(psi.data_ptr(), self.code, n, C.byref(sw), base, set_stride, P, N, st),
                            "apply_sweep")

@@ -423,6 +423,9 @@ def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, 
     :class:`Recipe` objects for the executor to compose on the GPU.
     """
     tile_bits = min(tile_bits, 14 if itemsize <= 8 else 13)
+    # unitarity of every op with a matrix, batched once (the plan key, trace checks and fusion use it)
+    mops = [o for o in ops if o is not None and o.kind != "pauli_mix"]
+    ucache = dict(zip(map(id, mops), unitary_flags(mops))) if mops else {}
     # density matrices: does every op keep the trace, or is it followed by a renormalisation?
     dm = any(o is not None and (o.pair is not None or o.kind == "channel") for o in ops)
     trace_kept = False
@@ -431,18 +434,26 @@ def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, 
         trace_kept = True
         pending_loss = False
         tp_list = []
+        tpc: dict = {}  # channel ops sharing one superoperator array: checked once
         for o in ops:
             if o is None:
                 pending_loss = False
                 continue
-            tp = o.kind == "pauli_mix" or trace_preserving(o)
+            if o.kind == "pauli_mix":
+                tp = True
+            elif o.pair is not None:
+                tp = ucache[id(o)]
+            else:
+                tp = tpc.get(id(o.matrix))
+                if tp is None:
+                    tp = tpc[id(o.matrix)] = trace_preserving(o)
             tp_list.append(tp)
             pending_loss |= not tp
         trace_kept = not pending_loss
         tp_flags = tuple(tp_list)
     key = None
     if device_fusion and mode != "gate" and ops and not any(o is not None and o.kind == "pauli_mix" for o in ops):
-        flags = unitary_flags([o for o in ops if o is not None])
+        flags = [ucache[id(o)] for o in ops if o is not None]
         key = (nbits, mode, width, tile_bits, low_bits, max_sweep_k, itemsize,
                tuple(None if o is None else tuple(o.bits) for o in ops), tuple(flags), tuple(_pair_offsets(ops)),
                tp_flags)
@@ -468,7 +479,7 @@ def compile_ops(ops, nbits, mode="sweep", width=2, tile_bits=13, low_bits=None, 
             continue
         if not seg:
             continue
-        uflags = unitary_flags(seg)
+        uflags = [ucache[id(o)] for o in seg]
         if mode == "gate":
             for o, u, w_ in zip(seg, uflags, whole_cuts(seg, [[i] for i in range(len(seg))])):
                 plan.steps.append(DenseStep(list(o.bits), plan.add_matrix(o.matrix), u, w_))

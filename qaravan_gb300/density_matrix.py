@@ -74,17 +74,31 @@ def _pauli_mix_op(nm, idx, n):
     return Op([], None, kind="pauli_mix", terms=terms)
 
 
-def dm_ops_for_gate(g, n):
-    """Ops on vec(rho) for one reference op (gate, Reset projector or noise carrier)."""
+def dm_ops_for_gate(g, n, cache=None):
+    """Ops on vec(rho) for one reference op (gate, Reset projector or noise carrier).
+
+    ``cache`` (optional dict, valid while the noise models are not modified):
+    noise superoperators already built in this op sequence, keyed by the noise
+    model, gate time, dynamical-decoupling flag and site order, shared
+    read-only between the carriers that use them."""
     idx = [int(q) for q in g.indices]
     ket = [2 * n - 1 - q for q in idx]
     bra = [n - 1 - q for q in idx]
     if g.name == "ID" and getattr(g, "nm", None) is not None:
         if 2 * len(idx) > 6 and hasattr(g.nm, "strings") and hasattr(g.nm, "probs"):
             return [_pauli_mix_op(g.nm, idx, n)]
-        s = np.asarray(g.nm.get_superop(g.time, getattr(g, "dd", False)), dtype=np.complex128)
-        s = s.reshape(4 ** len(idx), 4 ** len(idx))
-        return [Op(bra + ket, _sorted_rows(s, idx), kind="channel")]
+        dd = getattr(g, "dd", False)
+        key = (id(g.nm), g.time, bool(dd), tuple(np.argsort(idx)))
+        m = cache.get(key) if cache is not None else None
+        if m is None:
+            s = np.asarray(g.nm.get_superop(g.time, dd), dtype=np.complex128)
+            m = np.array(_sorted_rows(s.reshape(4 ** len(idx), 4 ** len(idx)), idx))
+            if cache is not None:
+                m.flags.writeable = False
+                cache[key] = (m, g.nm)  # the model kept alive with its key
+        else:
+            m = m[0]
+        return [Op(bra + ket, m, kind="channel")]
     if type(g).__name__ == "SuperOp":  # its matrix is the superoperator (tensorQ/density_matrix_sim.py:40)
         s = np.asarray(g.matrix, dtype=np.complex128).reshape(4 ** len(idx), 4 ** len(idx))
         return [Op(bra + ket, _sorted_rows(s, idx), kind="channel")]
@@ -144,8 +158,9 @@ class DensityMatrixSim:
         seq = circuit_ops(c)
         n = self.num_sites
         ops = []
+        cache: dict = {}
         for g in seq:
-            ops.extend(dm_ops_for_gate(g, n))
+            ops.extend(dm_ops_for_gate(g, n, cache))
             if g.name == "Reset" and getattr(g, "normalize", True):
                 ops.append(None)
         return ops

@@ -109,3 +109,35 @@ def test_all_rotation_kinds_and_shared_parameters(dtype, tol):
         for j, i in enumerate(rot):
             want[gates[i][2]] += per_gate[j]
         assert np.max(np.abs(grad[s] - want)) / np.max(np.abs(want)) < tol
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.complex64, 1e-5), (torch.complex128, 1e-11)])
+def test_fused_forward_matches_per_gate_forward(dtype, tol):
+    """The forward as fused 3- and 4-qubit blocks composed per parameter set on
+    the device (the default) against one tile-pass op per gate, at 15 qubits
+    (tiles smaller than the state), with mixed rotation kinds and a shared angle."""
+    from qaravan_gb300.adjoint import BatchedAnsatz
+    from qaravan_gb300.gates import CNOT
+    n, P = 15, 4
+    gates = []
+    for l in range(3):
+        for q in range(n):
+            gates.append((("RY", "RX", "RZ")[(q + l) % 3], [q], 2 * (l * n + q)))
+            gates.append(("RZ", [q], 2 * (l * n + q) + 1))
+        for q in range(0, n - 1, 2):
+            gates.append(("RZZ", [q, q + 1], 2 * l * n))
+        for q in range(1, n - 1, 2):
+            g = CNOT([q + 1, q], n)
+            gates.append(("fixed", list(g.indices), np.asarray(g.matrix)))
+    terms = _tfi_terms(n)
+    rng = np.random.default_rng(4)
+    x = rng.uniform(-2, 2, size=(P, 2 * 3 * n))
+    ref_ba = BatchedAnsatz(n, gates, nparams=x.shape[1], dtype=dtype, fused_width=0)
+    assert ref_ba._fused is None
+    e0, g0 = (t.cpu().numpy() for t in ref_ba.energy_and_grad(x, terms))
+    for width in (3, 4):
+        ba = BatchedAnsatz(n, gates, nparams=x.shape[1], dtype=dtype, fused_width=width)
+        assert ba._fused is not None and ba._fused["blocks"] < len(gates)
+        e1, g1 = (t.cpu().numpy() for t in ba.energy_and_grad(x, terms))
+        assert np.max(np.abs(e1 - e0)) < tol * np.max(np.abs(e0)) * 10
+        assert np.max(np.abs(g1 - g0)) / np.max(np.abs(g0)) < tol
