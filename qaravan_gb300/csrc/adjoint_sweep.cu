@@ -47,6 +47,7 @@ struct AdjSweepArgs {
     int run_len[QGB_SWEEP_MAX_OPS];     // at a run's first op: its op count (0 elsewhere)
     int run_pos[QGB_SWEEP_MAX_OPS][4];  // at a run's first op: the tile bit of each local bit of the run
     int op_lpos[QGB_SWEEP_MAX_OPS][2];  // every op's sites as local bits of its run
+    int op_gcls[QGB_SWEEP_MAX_OPS];     // generator class of a wanted derivative (kGenNone: none)
     uint64_t tiles;        // tiles per state
     uint64_t chunk_tiles;  // tiles per chunk
     uint64_t chunks;       // chunks over all states
@@ -261,27 +262,44 @@ __device__ __forceinline__ void adj_tile_run(cplx<T>* __restrict__ pt, cplx<T>* 
 // dense, diagonal (two products per row) or a permutation with unit entries
 // (register moves), as classified when the state's matrices were staged.
 constexpr int kAdjDense = 0, kAdjDiag = 1, kAdjPerm = 2, kAdjReal = 3;  // kAdjReal: a dense real matrix (RY)
+// permutations of a two-site U^dagger known at compile time (register renaming, no selects):
+// rows (0, 1, 2, 3) <- columns (0, 1, 3, 2) [CNOT, control on the first site], (0, 3, 2, 1)
+// [CNOT, control on the second site], (0, 2, 1, 3) [SWAP]
+constexpr int kAdjPermCX = 4, kAdjPermXC = 5, kAdjPermSwap = 6;
+// generator classes of a wanted derivative (host-classified Pauli-product rows): none, diagonal
+// (row r reads column r), flipped (one site: row r reads r ^ 1; two sites: 3 - r), any other
+constexpr int kGenNone = 0, kGenDiag = 1, kGenFlip = 2, kGenAny = 3;
 
-template <int R, int P, int MODE, bool WANT, typename C, typename T>
+// The derivative Im sum_r conj(l_r) (g_r p_{col r}) of one op over a group: complex sums
+// W_r = sum conj(l_r) q_r per generator row r, combined once per op as Im(g_r W_r) =
+// g_r.x W_r.y + g_r.y W_r.x (g_r in {+-1, +-i}).
+template <typename T, typename C>
+__device__ __forceinline__ void wacc(C& w, const C& l, const C& q) {
+    w.x = fmaf(l.x, q.x, fmaf(l.y, q.y, w.x));
+    w.y = fmaf(l.x, q.y, fmaf(-l.y, q.x, w.y));
+}
+template <>
+__device__ __forceinline__ void wacc<double, double2>(double2& w, const double2& l, const double2& q) {
+    w.x = fma(l.x, q.x, fma(l.y, q.y, w.x));
+    w.y = fma(l.x, q.y, fma(-l.y, q.x, w.y));
+}
+
+template <int R, int P, int MODE, int GEN, typename C, typename T>
 __device__ __forceinline__ void adj_reg1(C (&p)[1 << R], C (&l)[1 << R], const C* __restrict__ u,
-                                         const uint8_t* __restrict__ col, const float2* gv, const int* gc, T& s) {
+                                         const float2* gv, T& s) {
     constexpr int D = 1 << R, bit = 1 << P;
     const C u0 = u[0], u1 = u[1], u2 = u[2], u3 = u[3];
-    // generator rows: one entry in {+1, -1, +i, -i} per row -- Im(conj(l) g q) is a sign times
-    // Im(conj(l) q) (g real) or Re(conj(l) q) (g imaginary): no products by g
-    const T gs0 = T(gv[0].x + gv[0].y), gs1 = T(gv[1].x + gv[1].y);
-    const bool gi0 = gv[0].y != 0.f, gi1 = gv[1].y != 0.f;
-    const int c0 = gc[0], c1 = gc[1];
-    const int k0 = col[0], k1 = col[1];
+    C w0 = mk<T>(T(0), T(0)), w1 = mk<T>(T(0), T(0));
 #pragma unroll
     for (int c = 0; c < D; ++c) {
         if (c & bit) continue;
         const C p0 = p[c], p1 = p[c | bit], l0 = l[c], l1 = l[c | bit];
-        if constexpr (WANT) {
-            const C q0 = c0 ? p1 : p0, q1 = c1 ? p1 : p0;
-            const T im0 = l0.x * q0.y - l0.y * q0.x, re0 = l0.x * q0.x + l0.y * q0.y;
-            const T im1 = l1.x * q1.y - l1.y * q1.x, re1 = l1.x * q1.x + l1.y * q1.y;
-            s += gs0 * (gi0 ? re0 : im0) + gs1 * (gi1 ? re1 : im1);
+        if constexpr (GEN == kGenDiag) {
+            wacc<T>(w0, l0, p0);
+            wacc<T>(w1, l1, p1);
+        } else if constexpr (GEN != kGenNone) {  // one site: off-diagonal rows (X, Y)
+            wacc<T>(w0, l0, p1);
+            wacc<T>(w1, l1, p0);
         }
         if constexpr (MODE == kAdjReal) {
             const T a = u0.x, b = u1.x, cc = u2.x, d = u3.x;
@@ -299,11 +317,11 @@ __device__ __forceinline__ void adj_reg1(C (&p)[1 << R], C (&l)[1 << R], const C
             p[c | bit] = y;
             l[c] = z;
             l[c | bit] = t;
-        } else if constexpr (MODE == kAdjPerm) {
-            p[c] = k0 ? p1 : p0;
-            p[c | bit] = k1 ? p1 : p0;
-            l[c] = k0 ? l1 : l0;
-            l[c | bit] = k1 ? l1 : l0;
+        } else if constexpr (MODE == kAdjPerm) {  // one site: a unit permutation that is not the identity swaps
+            p[c] = p1;
+            p[c | bit] = p0;
+            l[c] = l1;
+            l[c | bit] = l0;
         } else {
             C x = mk<T>(0, 0), y = mk<T>(0, 0), z = mk<T>(0, 0), t = mk<T>(0, 0);
             cfma(x, u0, p0);
@@ -320,23 +338,24 @@ __device__ __forceinline__ void adj_reg1(C (&p)[1 << R], C (&l)[1 << R], const C
             l[c | bit] = t;
         }
     }
+    if constexpr (GEN != kGenNone)
+        s += T(gv[0].x) * w0.y + T(gv[0].y) * w0.x + T(gv[1].x) * w1.y + T(gv[1].y) * w1.x;
 }
 
 // matrix bit 1 (most significant) <-> local bit P0 (the op's first site), bit 0 <-> P1
-template <int R, int P0, int P1, int MODE, bool WANT, typename C, typename T>
+template <int R, int P0, int P1, int MODE, int GEN, typename C, typename T>
 __device__ __forceinline__ void adj_reg2(C (&p)[1 << R], C (&l)[1 << R], const C* __restrict__ u,
                                          const uint8_t* __restrict__ col, const float2* gv, const int* gc, T& s) {
     constexpr int D = 1 << R, b0 = 1 << P0, b1 = 1 << P1;
     int gcr[4], colr[4];
-    T gsr[4];
-    bool gir[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-        gcr[r] = gc[r];
-        colr[r] = col[r];
-        gsr[r] = T(gv[r].x + gv[r].y);
-        gir[r] = gv[r].y != 0.f;
+        gcr[r] = GEN == kGenAny ? gc[r] : 0;
+        colr[r] = MODE == kAdjPerm ? col[r] : 0;
     }
+    C w[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) w[r] = mk<T>(T(0), T(0));
 #pragma unroll
     for (int c = 0; c < D; ++c) {
         if ((c & b0) || (c & b1)) continue;
@@ -347,14 +366,20 @@ __device__ __forceinline__ void adj_reg2(C (&p)[1 << R], C (&l)[1 << R], const C
             x[r] = p[ix[r]];
             y[r] = l[ix[r]];
         }
-        if constexpr (WANT) {
+        if constexpr (GEN == kGenDiag) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r) wacc<T>(w[r], y[r], x[r]);
+        } else if constexpr (GEN == kGenFlip) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r) wacc<T>(w[r], y[r], x[3 - r]);
+        } else if constexpr (GEN == kGenAny) {
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
                 C q = x[0];  // x[gc[r]] by selects (no dynamic register indexing)
 #pragma unroll
                 for (int e = 1; e < 4; ++e)
                     if (gcr[r] == e) q = x[e];
-                s += gsr[r] * (gir[r] ? y[r].x * q.x + y[r].y * q.y : y[r].x * q.y - y[r].y * q.x);
+                wacc<T>(w[r], y[r], q);
             }
         }
         if constexpr (MODE == kAdjDiag) {
@@ -367,6 +392,16 @@ __device__ __forceinline__ void adj_reg2(C (&p)[1 << R], C (&l)[1 << R], const C
                 p[ix[r]] = a;
                 l[ix[r]] = b;
             }
+        } else if constexpr (MODE == kAdjPermCX || MODE == kAdjPermXC || MODE == kAdjPermSwap) {
+            constexpr int s1 = MODE == kAdjPermCX ? 1 : (MODE == kAdjPermXC ? 3 : 2);
+            constexpr int s2 = MODE == kAdjPermCX ? 3 : (MODE == kAdjPermXC ? 2 : 1);
+            constexpr int s3 = MODE == kAdjPermCX ? 2 : (MODE == kAdjPermXC ? 1 : 3);
+            p[ix[1]] = x[s1];
+            p[ix[2]] = x[s2];
+            p[ix[3]] = x[s3];
+            l[ix[1]] = y[s1];
+            l[ix[2]] = y[s2];
+            l[ix[3]] = y[s3];
         } else if constexpr (MODE == kAdjPerm) {
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
@@ -395,81 +430,92 @@ __device__ __forceinline__ void adj_reg2(C (&p)[1 << R], C (&l)[1 << R], const C
             }
         }
     }
+    if constexpr (GEN != kGenNone) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) s += T(gv[r].x) * w[r].y + T(gv[r].y) * w[r].x;
+    }
 }
 
-// the op's class and derivative flag, chosen once per op (each case its own unrolled code)
+// the op's class and generator class, chosen once per op (each case its own unrolled code)
+template <int R, int P, int GEN, typename C, typename T>
+__device__ __forceinline__ void adj_reg1_mode(C (&p)[1 << R], C (&l)[1 << R], const C* u, int mode, const float2* gv,
+                                              T& s) {
+    switch (mode) {
+        case kAdjReal: adj_reg1<R, P, kAdjReal, GEN>(p, l, u, gv, s); break;
+        case kAdjDiag: adj_reg1<R, P, kAdjDiag, GEN>(p, l, u, gv, s); break;
+        case kAdjPerm: adj_reg1<R, P, kAdjPerm, GEN>(p, l, u, gv, s); break;
+        default: adj_reg1<R, P, kAdjDense, GEN>(p, l, u, gv, s); break;
+    }
+}
+
 template <int R, int P, typename C, typename T>
-__device__ __forceinline__ void adj_reg1_any(C (&p)[1 << R], C (&l)[1 << R], const C* u, int mode, const uint8_t* col,
-                                             bool want, const float2* gv, const int* gc, T& s) {
-    if (want) {
-        switch (mode) {
-            case kAdjReal: adj_reg1<R, P, kAdjReal, true>(p, l, u, col, gv, gc, s); break;
-            case kAdjDiag: adj_reg1<R, P, kAdjDiag, true>(p, l, u, col, gv, gc, s); break;
-            case kAdjPerm: adj_reg1<R, P, kAdjPerm, true>(p, l, u, col, gv, gc, s); break;
-            default: adj_reg1<R, P, kAdjDense, true>(p, l, u, col, gv, gc, s); break;
-        }
-    } else {
-        switch (mode) {
-            case kAdjReal: adj_reg1<R, P, kAdjReal, false>(p, l, u, col, gv, gc, s); break;
-            case kAdjDiag: adj_reg1<R, P, kAdjDiag, false>(p, l, u, col, gv, gc, s); break;
-            case kAdjPerm: adj_reg1<R, P, kAdjPerm, false>(p, l, u, col, gv, gc, s); break;
-            default: adj_reg1<R, P, kAdjDense, false>(p, l, u, col, gv, gc, s); break;
-        }
+__device__ __forceinline__ void adj_reg1_any(C (&p)[1 << R], C (&l)[1 << R], const C* u, int mode, int gen,
+                                             const float2* gv, T& s) {
+    switch (gen) {
+        case kGenNone: adj_reg1_mode<R, P, kGenNone>(p, l, u, mode, gv, s); break;
+        case kGenDiag: adj_reg1_mode<R, P, kGenDiag>(p, l, u, mode, gv, s); break;
+        default: adj_reg1_mode<R, P, kGenFlip>(p, l, u, mode, gv, s); break;
+    }
+}
+
+template <int R, int P0, int P1, int GEN, typename C, typename T>
+__device__ __forceinline__ void adj_reg2_mode(C (&p)[1 << R], C (&l)[1 << R], const C* u, int mode,
+                                              const uint8_t* col, const float2* gv, const int* gc, T& s) {
+    switch (mode) {
+        case kAdjDiag: adj_reg2<R, P0, P1, kAdjDiag, GEN>(p, l, u, col, gv, gc, s); break;
+        case kAdjPermCX: adj_reg2<R, P0, P1, kAdjPermCX, GEN>(p, l, u, col, gv, gc, s); break;
+        case kAdjPermXC: adj_reg2<R, P0, P1, kAdjPermXC, GEN>(p, l, u, col, gv, gc, s); break;
+        case kAdjPermSwap: adj_reg2<R, P0, P1, kAdjPermSwap, GEN>(p, l, u, col, gv, gc, s); break;
+        case kAdjPerm: adj_reg2<R, P0, P1, kAdjPerm, GEN>(p, l, u, col, gv, gc, s); break;
+        default: adj_reg2<R, P0, P1, kAdjDense, GEN>(p, l, u, col, gv, gc, s); break;
     }
 }
 
 template <int R, int P0, int P1, typename C, typename T>
-__device__ __forceinline__ void adj_reg2_any(C (&p)[1 << R], C (&l)[1 << R], const C* u, int mode, const uint8_t* col,
-                                             bool want, const float2* gv, const int* gc, T& s) {
-    if (want) {
-        switch (mode) {
-            case kAdjDiag: adj_reg2<R, P0, P1, kAdjDiag, true>(p, l, u, col, gv, gc, s); break;
-            case kAdjPerm: adj_reg2<R, P0, P1, kAdjPerm, true>(p, l, u, col, gv, gc, s); break;
-            default: adj_reg2<R, P0, P1, kAdjDense, true>(p, l, u, col, gv, gc, s); break;
-        }
-    } else {
-        switch (mode) {
-            case kAdjDiag: adj_reg2<R, P0, P1, kAdjDiag, false>(p, l, u, col, gv, gc, s); break;
-            case kAdjPerm: adj_reg2<R, P0, P1, kAdjPerm, false>(p, l, u, col, gv, gc, s); break;
-            default: adj_reg2<R, P0, P1, kAdjDense, false>(p, l, u, col, gv, gc, s); break;
-        }
+__device__ __forceinline__ void adj_reg2_any(C (&p)[1 << R], C (&l)[1 << R], const C* u, int mode, int gen,
+                                             const uint8_t* col, const float2* gv, const int* gc, T& s) {
+    switch (gen) {
+        case kGenNone: adj_reg2_mode<R, P0, P1, kGenNone>(p, l, u, mode, col, gv, gc, s); break;
+        case kGenDiag: adj_reg2_mode<R, P0, P1, kGenDiag>(p, l, u, mode, col, gv, gc, s); break;
+        case kGenFlip: adj_reg2_mode<R, P0, P1, kGenFlip>(p, l, u, mode, col, gv, gc, s); break;
+        default: adj_reg2_mode<R, P0, P1, kGenAny>(p, l, u, mode, col, gv, gc, s); break;
     }
 }
 
 template <int R, typename C, typename T>
-__device__ __forceinline__ void adj_apply1(C (&p)[1 << R], C (&l)[1 << R], int P, const C* u, int mode,
-                                           const uint8_t* col, bool want, const float2* gv, const int* gc, T& s) {
+__device__ __forceinline__ void adj_apply1(C (&p)[1 << R], C (&l)[1 << R], int P, const C* u, int mode, int gen,
+                                           const float2* gv, T& s) {
     switch (P) {
-        case 0: adj_reg1_any<R, 0>(p, l, u, mode, col, want, gv, gc, s); break;
-        case 1: if constexpr (R > 1) adj_reg1_any<R, 1>(p, l, u, mode, col, want, gv, gc, s); break;
-        case 2: if constexpr (R > 2) adj_reg1_any<R, 2>(p, l, u, mode, col, want, gv, gc, s); break;
-        case 3: if constexpr (R > 3) adj_reg1_any<R, 3>(p, l, u, mode, col, want, gv, gc, s); break;
+        case 0: adj_reg1_any<R, 0>(p, l, u, mode, gen, gv, s); break;
+        case 1: if constexpr (R > 1) adj_reg1_any<R, 1>(p, l, u, mode, gen, gv, s); break;
+        case 2: if constexpr (R > 2) adj_reg1_any<R, 2>(p, l, u, mode, gen, gv, s); break;
+        case 3: if constexpr (R > 3) adj_reg1_any<R, 3>(p, l, u, mode, gen, gv, s); break;
     }
 }
 
 template <int R, int CODE, typename C, typename T>
-__device__ __forceinline__ void adj_apply2_case(C (&p)[1 << R], C (&l)[1 << R], const C* u, int mode,
-                                                const uint8_t* col, bool want, const float2* gv, const int* gc, T& s) {
+__device__ __forceinline__ void adj_apply2_case(C (&p)[1 << R], C (&l)[1 << R], const C* u, int mode, int gen,
+                                                const uint8_t* col, const float2* gv, const int* gc, T& s) {
     constexpr int P0 = CODE / 4, P1 = CODE % 4;
-    if constexpr (P0 < R && P1 < R && P0 != P1) adj_reg2_any<R, P0, P1>(p, l, u, mode, col, want, gv, gc, s);
+    if constexpr (P0 < R && P1 < R && P0 != P1) adj_reg2_any<R, P0, P1>(p, l, u, mode, gen, col, gv, gc, s);
 }
 
 template <int R, typename C, typename T>
 __device__ __forceinline__ void adj_apply2(C (&p)[1 << R], C (&l)[1 << R], int P0, int P1, const C* u, int mode,
-                                           const uint8_t* col, bool want, const float2* gv, const int* gc, T& s) {
+                                           int gen, const uint8_t* col, const float2* gv, const int* gc, T& s) {
     switch (P0 * 4 + P1) {
-        case 1: adj_apply2_case<R, 1>(p, l, u, mode, col, want, gv, gc, s); break;
-        case 2: adj_apply2_case<R, 2>(p, l, u, mode, col, want, gv, gc, s); break;
-        case 3: adj_apply2_case<R, 3>(p, l, u, mode, col, want, gv, gc, s); break;
-        case 4: adj_apply2_case<R, 4>(p, l, u, mode, col, want, gv, gc, s); break;
-        case 6: adj_apply2_case<R, 6>(p, l, u, mode, col, want, gv, gc, s); break;
-        case 7: adj_apply2_case<R, 7>(p, l, u, mode, col, want, gv, gc, s); break;
-        case 8: adj_apply2_case<R, 8>(p, l, u, mode, col, want, gv, gc, s); break;
-        case 9: adj_apply2_case<R, 9>(p, l, u, mode, col, want, gv, gc, s); break;
-        case 11: adj_apply2_case<R, 11>(p, l, u, mode, col, want, gv, gc, s); break;
-        case 12: adj_apply2_case<R, 12>(p, l, u, mode, col, want, gv, gc, s); break;
-        case 13: adj_apply2_case<R, 13>(p, l, u, mode, col, want, gv, gc, s); break;
-        case 14: adj_apply2_case<R, 14>(p, l, u, mode, col, want, gv, gc, s); break;
+        case 1: adj_apply2_case<R, 1>(p, l, u, mode, gen, col, gv, gc, s); break;
+        case 2: adj_apply2_case<R, 2>(p, l, u, mode, gen, col, gv, gc, s); break;
+        case 3: adj_apply2_case<R, 3>(p, l, u, mode, gen, col, gv, gc, s); break;
+        case 4: adj_apply2_case<R, 4>(p, l, u, mode, gen, col, gv, gc, s); break;
+        case 6: adj_apply2_case<R, 6>(p, l, u, mode, gen, col, gv, gc, s); break;
+        case 7: adj_apply2_case<R, 7>(p, l, u, mode, gen, col, gv, gc, s); break;
+        case 8: adj_apply2_case<R, 8>(p, l, u, mode, gen, col, gv, gc, s); break;
+        case 9: adj_apply2_case<R, 9>(p, l, u, mode, gen, col, gv, gc, s); break;
+        case 11: adj_apply2_case<R, 11>(p, l, u, mode, gen, col, gv, gc, s); break;
+        case 12: adj_apply2_case<R, 12>(p, l, u, mode, gen, col, gv, gc, s); break;
+        case 13: adj_apply2_case<R, 13>(p, l, u, mode, gen, col, gv, gc, s); break;
+        case 14: adj_apply2_case<R, 14>(p, l, u, mode, gen, col, gv, gc, s); break;
     }
 }
 
@@ -522,14 +568,14 @@ __device__ __forceinline__ void adj_tile_runs(cplx<T>* __restrict__ pt, cplx<T>*
             }
             for (int q = 0; q < nr; ++q) {
                 const int op = i0 + q;
-                const bool want = a.op_out[op] >= 0;
+                const int gen = a.op_gcls[op];
+                const bool want = gen != kGenNone;
                 T sd = T(0);
                 if (a.op_k[op] == 1)
-                    adj_apply1<R>(p, l, a.op_lpos[op][0], ush + op * 16, umode[op], ucol + op * 4, want, a.gval[op],
-                                  a.gcol[op], sd);
+                    adj_apply1<R>(p, l, a.op_lpos[op][0], ush + op * 16, umode[op], gen, a.gval[op], sd);
                 else
-                    adj_apply2<R>(p, l, a.op_lpos[op][0], a.op_lpos[op][1], ush + op * 16, umode[op], ucol + op * 4,
-                                  want, a.gval[op], a.gcol[op], sd);
+                    adj_apply2<R>(p, l, a.op_lpos[op][0], a.op_lpos[op][1], ush + op * 16, umode[op], gen,
+                                  ucol + op * 4, a.gval[op], a.gcol[op], sd);
                 if (want) {  // uniform over the CTA: every lane reaches the shuffles
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) sd += __shfl_xor_sync(0xffffffffu, sd, o);
@@ -572,8 +618,11 @@ __device__ __forceinline__ int adj_tile_ops(cplx<T>* pt, cplx<T>* lt, int m, con
     return r;
 }
 
+// complex64: 256 threads and 3 CTAs per SM (80 registers): the passes are latency-bound, and
+// the third CTA's warps outweigh the few register spills (64-set, 20-qubit gradient 0.42 ->
+// 0.36 s); complex128 keeps 128 registers (up to 512 threads when one CTA fits)
 template <typename T>
-__global__ void __launch_bounds__(kAdjMaxThreads) adjoint_sweep_kernel(cplx<T>* __restrict__ phi,
+__global__ void __launch_bounds__(sizeof(T) == 4 ? 256 : kAdjMaxThreads, sizeof(T) == 4 ? 3 : 1) adjoint_sweep_kernel(cplx<T>* __restrict__ phi,
                                                                        cplx<T>* __restrict__ lam,
                                                                        const cplx<T>* __restrict__ mats,
                                                                        const __grid_constant__ AdjSweepArgs a,
@@ -668,7 +717,14 @@ __global__ void __launch_bounds__(kAdjMaxThreads) adjoint_sweep_kernel(cplx<T>* 
                         perm = perm && nz == 1;
                         ucol[op * 4 + r] = uint8_t(cc);
                     }
-                    umode[op] = uint8_t(diag ? kAdjDiag : (perm ? kAdjPerm : ((real && d == 2) ? kAdjReal : kAdjDense)));
+                    int mode = diag ? kAdjDiag : (perm ? kAdjPerm : ((real && d == 2) ? kAdjReal : kAdjDense));
+                    if (mode == kAdjPerm && d == 4) {
+                        const uint8_t* c4 = ucol + op * 4;
+                        if (c4[0] == 0 && c4[1] == 1 && c4[2] == 3 && c4[3] == 2) mode = kAdjPermCX;
+                        else if (c4[0] == 0 && c4[1] == 3 && c4[2] == 2 && c4[3] == 1) mode = kAdjPermXC;
+                        else if (c4[0] == 0 && c4[1] == 2 && c4[2] == 1 && c4[3] == 3) mode = kAdjPermSwap;
+                    }
+                    umode[op] = uint8_t(mode);
                 }
             }
             staged = b;
@@ -752,7 +808,7 @@ int launch_adj(void* phi, void* lam, const void* mats, const AdjSweepArgs& a, do
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem) != cudaSuccess)
             return check_launch("adjoint sweep occupancy");
         if (per_sm < 1) continue;
-        if (per_sm == 1) {
+        if (per_sm == 1 && sizeof(T) == 8) {
             int p512 = 0;
             if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p512, kern, 512, smem) != cudaSuccess)
                 return check_launch("adjoint sweep occupancy");
@@ -851,9 +907,12 @@ extern "C" int qgb_adjoint_sweep_step(void* phi, void* lam, int dtype, int n, co
         a.op_k[i] = k;
         a.op_mat[i] = sw.op_mat[i];
         a.op_out[i] = sw.op_out[i] < 0 ? -1 : sw.op_out[i];
+        a.op_gcls[i] = kGenNone;
         if (a.op_out[i] >= 0) {
             any_out = true;
             const int d = 1 << k;
+            uint32_t cols = 0;
+            bool gdiag = true, gflip = true;
             for (int r = 0; r < d; ++r) {
                 const int c = sw.op_gen_col[i][r];
                 const double re = sw.op_gen_val[i][r][0], im = sw.op_gen_val[i][r][1];
@@ -862,7 +921,13 @@ extern "C" int qgb_adjoint_sweep_step(void* phi, void* lam, int dtype, int n, co
                     return set_error(QGB_EINVAL, "adjoint sweep op %d: generator row %d is not a Pauli-product row", i, r);
                 a.gcol[i][r] = c;
                 a.gval[i][r] = make_float2(float(re), float(im));
+                cols |= 1u << c;
+                gdiag = gdiag && c == r;
+                gflip = gflip && c == d - 1 - r;
             }
+            if (cols != (1u << d) - 1u)
+                return set_error(QGB_EINVAL, "adjoint sweep op %d: generator rows are not a permutation", i);
+            a.op_gcls[i] = gdiag ? kGenDiag : (gflip ? kGenFlip : kGenAny);
         }
     }
     if (any_out && !grad_out) return set_error(QGB_EINVAL, "derivatives requested without an output");

@@ -28,7 +28,27 @@ def _haar(d, rng):
 
 _PERMS = [np.array([[0, 1], [1, 0]], complex),                                       # X
           np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 0, 1], [0, 0, 1, 0]], complex),  # CNOT
-          np.array([[1, 0, 0, 0], [0, 0, 1, 0], [0, 1, 0, 0], [0, 0, 0, 1]], complex)]  # SWAP
+          np.array([[1, 0, 0, 0], [0, 0, 1, 0], [0, 1, 0, 0], [0, 0, 0, 1]], complex),  # SWAP
+          np.array([[1, 0, 0, 0], [0, 0, 0, 1], [0, 0, 1, 0], [0, 1, 0, 0]], complex),  # CNOT, control second
+          np.array([[0, 0, 1, 0], [0, 0, 0, 1], [1, 0, 0, 0], [0, 1, 0, 0]], complex)]  # X on the first site
+
+
+@pytest.fixture(scope="module", autouse=True)
+def extra_generators():
+    """Two-site generators whose rows are neither diagonal nor flipped (X (x) Z,
+    Y (x) X), as rotation kinds 7 and 8 of the tables the sweep structs read."""
+    from qaravan_gb300 import _lib, adjoint
+    px, py, pz = adjoint._PX, adjoint._PY, adjoint._PZ
+    extra = {7: np.kron(px, pz), 8: np.kron(py, px)}
+    for k, m in extra.items():
+        adjoint._GEN[k] = m
+        adjoint._GEN_C[k] = _lib.double_array(np.stack([m.real, m.imag], axis=-1).reshape(-1))
+        adjoint._GEN_ROWS[k] = [(int(np.flatnonzero(m[r])[0]), complex(m[r, np.flatnonzero(m[r])[0]]))
+                                for r in range(4)]
+    yield
+    for k in extra:
+        for t in (adjoint._GEN, adjoint._GEN_C, adjoint._GEN_ROWS):
+            t.pop(k, None)
 
 
 @pytest.fixture(params=[-1, 0], ids=["register_runs", "pass_per_gate"])
@@ -56,7 +76,7 @@ def test_adjoint_sweep_matches_per_gate_steps(dtype, tol, n, tile, runs):
             gates.append(([q], int(rng.integers(1, 4)) if rng.random() < 0.7 else 0))
         else:
             a, b = rng.choice(n, size=2, replace=False)
-            gates.append(([int(a), int(b)], int(rng.integers(4, 7)) if rng.random() < 0.6 else 0))
+            gates.append(([int(a), int(b)], int(rng.integers(4, 9)) if rng.random() < 0.6 else 0))
     G = len(gates)
     mats = np.zeros((B, G, 16), dtype=np.complex128)
     for s in range(B):
@@ -65,8 +85,8 @@ def test_adjoint_sweep_matches_per_gate_steps(dtype, tol, n, tile, runs):
             if kind:
                 t = rng.uniform(-3, 3)
                 m = np.cos(t) * np.eye(d) - 1j * np.sin(t) * _GEN[kind]
-            elif g % 3 == 0:  # fixed permutation gates: X, CNOT, SWAP
-                m = _PERMS[0] if d == 2 else _PERMS[1 + (g // 3) % 2]
+            elif g % 3 == 0:  # fixed permutation gates: X, CNOT (either control), SWAP, X on one site of two
+                m = _PERMS[0] if d == 2 else _PERMS[1 + (g // 3) % 4]
             else:
                 m = _haar(d, rng)
             mats[s, g, :d * d] = m.reshape(-1)
