@@ -65,9 +65,18 @@ class _Runner:
             o += k
         return out, flat
 
-    def forward_state(self, mats):
+    def forward_state(self, mats, flat=None):
         n = self.n
-        host, flat = self.host_matrices(mats)
+        if flat is None:
+            host, flat = self.host_matrices(mats)
+        else:  # per-gate views of the flattened matrices
+            o = 0
+            host = []
+            for m in mats:
+                k = m.numel()
+                d = int(round(k ** 0.5))
+                host.append(flat[o:o + k].reshape(d, d))
+                o += k
         self._flat = flat
         ops = [Op([n - 1 - q for q in g.indices], m) for g, m in zip(self.gates, host)]
         kcap = 5 if self.dtype == torch.complex64 else 4
@@ -118,7 +127,9 @@ class _Runner:
         def flush():
             if not run:
                 return
-            key = (n, tile, tuple((i, kind, tuple(bits), int(offs[i])) for (i, kind), bits in run))
+            rows = np.array([(i, kind, bits[0], bits[1] if len(bits) > 1 else -1) for (i, kind), bits in run],
+                            dtype=np.int64)
+            key = (n, tile, rows.tobytes(), offs[rows[:, 0]].tobytes())
             sweeps = _REV_CACHE.pop(key, None)
             if sweeps is None:
                 sweeps = [_adjoint_sweep_struct(lo, high, [(bits, int(offs[i]), i * 32 if kind else -1, kind)
@@ -305,7 +316,7 @@ class _Inputs:
     back through ``matrix_exp``. Every other gate contributes its matrix."""
 
     def __init__(self, gates, closed_form=False):
-        self.mats = _matrices(gates, closed_form)
+        self.mats, self.flat = _matrices(gates, closed_form)
         self.rot, angles = [], []
         for i, g in enumerate(gates):
             a = _rotation_angle(g)
@@ -347,7 +358,7 @@ class _Inputs:
 class _StateFn(torch.autograd.Function):
     @staticmethod
     def forward(ctx, runner, inputs, *args):
-        psi = runner.forward_state(inputs.mats)
+        psi = runner.forward_state(inputs.mats, inputs.flat)
         ctx.runner, ctx.inputs = runner, inputs
         ctx.save_for_backward(psi)
         return psi
@@ -366,7 +377,7 @@ class _EnergyFn(torch.autograd.Function):
     @staticmethod
     def forward(ctx, runner, terms, inputs, *args):
         from .statevector import pauli_expectations
-        psi = runner.forward_state(inputs.mats)
+        psi = runner.forward_state(inputs.mats, inputs.flat)
         e = pauli_expectations(psi, runner.n, terms).sum()
         ctx.runner, ctx.terms, ctx.inputs = runner, terms, inputs
         ctx.save_for_backward(psi)
@@ -392,13 +403,17 @@ _GEN_T = {k: torch.from_numpy(m) for k, m in _GEN.items()}
 
 
 def _matrices(gates, closed_form=False):
-    """Every gate's matrix as a torch tensor. With ``closed_form``, rotation gates
-    whose matrix has not been built yet (torch angles, see ``ParamGate``) get
-    cos(theta) I - i sin(theta) P from their construction-time angles, all of a
-    kind in one vectorised step, instead of one ``matrix_exp`` each; the two
-    differ by the series truncation of ``matrix_exp`` (about 2e-10), far below
-    complex64 rounding, so the complex64 paths use it."""
+    """Every gate's matrix as a torch tensor, and all of them flattened into one
+    complex128 host array (row-major, gate after gate). With ``closed_form``,
+    rotation gates whose matrix has not been built yet (torch angles, see
+    ``ParamGate``) get cos(theta) I - i sin(theta) P from their construction-time
+    angles, all of a kind in one vectorised step, instead of one ``matrix_exp``
+    each; the two differ by the series truncation of ``matrix_exp`` (about
+    2e-10), far below complex64 rounding, so the complex64 paths use it."""
     mats = [None] * len(gates)
+    sizes = np.array([4 ** len(g.indices) for g in gates], dtype=np.int64)
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    flat = np.empty(int(offs[-1]), dtype=np.complex128)
     if closed_form:
         by_kind = {}
         for i, g in enumerate(gates):
@@ -406,20 +421,39 @@ def _matrices(gates, closed_form=False):
             if kind is not None and getattr(g, "matrix_pending", lambda: False)() and _rotation_angle(g) is not None:
                 by_kind.setdefault(kind, []).append(i)
         for kind, idx in by_kind.items():
-            vals = [gates[i].angle_values()[0].reshape(()).to(torch.float64) for i in idx]
-            try:
-                th = torch.stack(vals).cpu()  # one copy when the angles share a device
-            except RuntimeError:
-                th = torch.stack([v.cpu() for v in vals])
+            if all(gates[i].angles_unchanged() for i in idx):
+                # the live angles hold the construction-time values: one gather when they
+                # are views of one parameter tensor
+                th = _stack_angles([gates[i].angles[0] for i in idx]).detach()
+            else:
+                vals = [gates[i].angle_values()[0].reshape(()).to(torch.float64) for i in idx]
+                try:
+                    th = torch.stack(vals).cpu()  # one copy when the angles share a device
+                except RuntimeError:
+                    th = torch.stack([v.cpu() for v in vals])
             gen = _GEN_T[kind]
             eye = torch.eye(gen.shape[0], dtype=torch.complex128)
             m = torch.cos(th)[:, None, None] * eye - 1j * torch.sin(th)[:, None, None] * gen
-            for j, i in enumerate(idx):
-                mats[i] = m[j]
+            dd = gen.shape[0] ** 2
+            ia = np.asarray(idx)
+            flat[(offs[ia][:, None] + np.arange(dd)[None, :]).reshape(-1)] = m.numpy().reshape(-1)
+            for i, v in zip(idx, m.unbind(0)):
+                mats[i] = v
+    shared: dict = {}  # one tensor per distinct host matrix object (fixed gates repeat theirs)
     for i, g in enumerate(gates):
         if mats[i] is None:
-            mats[i] = g.matrix if torch.is_tensor(g.matrix) else torch.as_tensor(np.asarray(g.matrix, dtype=np.complex128))
-    return mats
+            gm = g.matrix
+            if torch.is_tensor(gm):
+                mats[i] = gm
+                flat[offs[i]:offs[i + 1]] = gm.detach().reshape(-1).to("cpu", torch.complex128).numpy()
+            else:
+                hit = shared.get(id(gm))
+                if hit is None or hit[0] is not gm:
+                    a = np.asarray(gm, dtype=np.complex128)
+                    hit = shared[id(gm)] = (gm, torch.as_tensor(a), a.reshape(-1))
+                mats[i] = hit[1]
+                flat[offs[i]:offs[i + 1]] = hit[2]
+    return mats, flat
 
 
 def run_with_adjoint(sim):

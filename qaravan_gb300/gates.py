@@ -342,8 +342,14 @@ class ParamGate(Gate):
 
     def angle_values(self):
         """The angles' values at construction (detached)."""
-        return self.__dict__.get("_angle_values", tuple(
-            a.detach() if _is_torch(a) else a for a in self.angles))
+        v = self.__dict__.get("_angle_values")
+        return v if v is not None else tuple(a.detach() if _is_torch(a) else a for a in self.angles)
+
+    def angles_unchanged(self):
+        """True while no torch angle was modified in place since construction
+        (the live angles then hold the construction-time values)."""
+        vers = self.__dict__.get("_angle_versions")
+        return vers is None or all(not _is_torch(a) or a._version == v for a, v in zip(self.angles, vers))
 
     def _build_matrix(self):
         m = self._built.get("matrix")
