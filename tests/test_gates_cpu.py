@@ -160,9 +160,9 @@ def test_closed_form_rotations_for_complex64_adjoint():
     th = torch.tensor(rng.uniform(0, 2 * np.pi, size=6), dtype=torch.float64, requires_grad=True)
     gates = [RX(0, th[0]), RY(1, th[1]), RZ(2, th[2]), RXX([0, 1], th[3]), RYY([1, 2], th[4]), RZZ([2, 0], th[5]),
              CNOT([0, 1], 3)]
-    fast = _matrices(gates, closed_form=True)
+    fast, _ = _matrices(gates, closed_form=True)
     assert all(g.matrix_pending() for g in gates[:6])
-    slow = _matrices(gates)
+    slow, _ = _matrices(gates)
     for a, b in zip(fast, slow):
         assert a.shape == b.shape and torch.max(torch.abs(a - b.detach())).item() < 1e-9
 
