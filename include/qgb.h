@@ -85,7 +85,9 @@ typedef struct {
  * gate first; gates on disjoint sites may be swapped). For op i and pair b:
  * if op_out[i] >= 0, grad_out[op_out[i] * batch + b] = Im <lam_b| P_i |phi_b>
  * at the gate's output, P_i the rotation generator given by one nonzero per
- * row (column op_gen_col[i][r], value op_gen_val[i][r] = (re, im)); then
+ * row (column op_gen_col[i][r], value op_gen_val[i][r] = (re, im)): a Pauli
+ * product, so every value is +-1 or +-i and the columns are a permutation
+ * (other rows are rejected with QGB_EINVAL); then
  * phi_b and lam_b <- U^dagger, U the 2^k x 2^k matrix at
  * mats + b * mat_stride + op_mat[i] elements (matrix order as qgb_sweep). */
 typedef struct {
@@ -450,7 +452,9 @@ int qgb_adjoint_step_rotation(void* phi, void* lam, int dtype, int n, const int*
  * (default) or 3 groups consecutive gates whose sites fit 3 tile bits and
  * applies each group to registers holding 8 amplitudes of the state and the
  * co-state (one shared-memory pass and one barrier per group; real matrices,
- * diagonals and permutations specialised); 0 runs one shared-memory pass per
+ * diagonals, CNOT/SWAP/X permutations and the generator's row pattern --
+ * diagonal, flipped or other -- specialised at compile time); 0 runs one
+ * shared-memory pass per
  * gate. Process-wide; results agree to rounding. No reference counterpart. */
 int qgb_set_adjoint_runs(int bits);
 

@@ -201,10 +201,33 @@ __device__ __forceinline__ void reg_damp_at(C (&v)[1 << R], int P, int mode, T s
     }
 }
 
+// Per-warp accumulators of the damping weights: for complex64 a float sum with its
+// compensation term (Kahan summation on the FP32 pipe, the weights' own float
+// precision kept over any number of tiles -- a float64 add per warp, op and tile
+// kept GB300's narrow FP64 pipe 38 % busy); for complex128 a double.
+struct WAccF {
+    float s, c;
+};
+template <typename T> struct WAccOf { using type = double; };
+template <> struct WAccOf<float> { using type = WAccF; };
+static_assert(sizeof(WAccF) == sizeof(double), "weight accumulator layout");
+
+__device__ __forceinline__ void wacc_add(double& a, double v) { a += v; }
+__device__ __forceinline__ void wacc_add(WAccF& a, float v) {
+    const float y = __fsub_rn(v, a.c);
+    const float t = __fadd_rn(a.s, y);
+    a.c = __fsub_rn(__fsub_rn(t, a.s), y);
+    a.s = t;
+}
+__device__ __forceinline__ double wacc_value(const double& a) { return a; }
+__device__ __forceinline__ double wacc_value(const WAccF& a) { return double(a.s) - double(a.c); }
+__device__ __forceinline__ void wacc_zero(double& a) { a = 0.0; }
+__device__ __forceinline__ void wacc_zero(WAccF& a) { a.s = 0.f; a.c = 0.f; }
+
 // Per-sweep, per-trajectory state in dynamic shared memory.
 template <typename T> struct TrajSweepSmem {
     cplx<T>* msh;     // [op][16]: the op's matrix with its sampled Paulis folded in (first op: times the prescale)
-    double* chw_w;    // [warp][2 * kTrajMaxOps]: per-warp weights of |1> before each damping, summed in order
+    typename WAccOf<T>::type* chw_w;  // [warp][2 * kTrajMaxOps]: per-warp weights of |1> before each damping
     T* djump;         // [op][2]: jump factor sqrt(gamma) / sqrt(gamma W) where a jump is replayed
     uint8_t* dmode;   // [op][2]: 0 none, 1 K0, 2 jump
     uint8_t* dflag;   // [op]: the folded matrix is diagonal
@@ -219,7 +242,7 @@ __device__ __forceinline__ void traj_tile_runs(cplx<T>* __restrict__ tile, int m
     using C = cplx<T>;
     constexpr int D = 1 << R;
     const int warp = tid >> 5, lane = tid & 31;
-    double* myw = sm.chw_w + size_t(warp) * (2 * kTrajMaxOps);
+    auto* myw = sm.chw_w + size_t(warp) * (2 * kTrajMaxOps);
     for (int i0 = 0; i0 < nops;) {
         const int nr = ops[i0].run;
         int rp[R], srt[R];
@@ -284,8 +307,8 @@ __device__ __forceinline__ void traj_tile_runs(cplx<T>* __restrict__ tile, int m
                         w1 += __shfl_xor_sync(0xffffffffu, w1, o);
                     }
                     if (lane == 0) {
-                        myw[2 * i] += double(w0);
-                        myw[2 * i + 1] += double(w1);
+                        wacc_add(myw[2 * i], w0);
+                        wacc_add(myw[2 * i + 1], w1);
                     }
                 }
             }
@@ -318,7 +341,8 @@ template <typename T> constexpr int traj_rmax() { return sizeof(T) == 4 ? 4 : 3;
 // damping modes | diagonal flags
 template <typename T> __host__ __device__ constexpr size_t traj_aux_bytes() {
     return sizeof(uint32_t) * (size_t(1) << QGB_SWEEP_MAX_HIGH) + sizeof(cplx<T>) * kTrajMaxOps * 16 +
-           sizeof(double) * (kTrajThreads / 32) * 2 * kTrajMaxOps + sizeof(T) * 2 * kTrajMaxOps + 2 * kTrajMaxOps +
+           sizeof(typename WAccOf<T>::type) * (kTrajThreads / 32) * 2 * kTrajMaxOps + sizeof(T) * 2 * kTrajMaxOps +
+           2 * kTrajMaxOps +
            kTrajMaxOps;
 }
 
@@ -336,7 +360,7 @@ __global__ void __launch_bounds__(kTrajThreads) traj_run_kernel(cplx<T>* __restr
     uint32_t* hoff = reinterpret_cast<uint32_t*>(bufs + (size_t(a.nbuf) << a.mmax));
     TrajSweepSmem<T> sm;
     sm.msh = reinterpret_cast<C*>(hoff + (size_t(1) << QGB_SWEEP_MAX_HIGH));
-    sm.chw_w = reinterpret_cast<double*>(sm.msh + kTrajMaxOps * 16);
+    sm.chw_w = reinterpret_cast<typename WAccOf<T>::type*>(sm.msh + kTrajMaxOps * 16);
     sm.djump = reinterpret_cast<T*>(sm.chw_w + (kTrajThreads / 32) * 2 * kTrajMaxOps);
     sm.dmode = reinterpret_cast<uint8_t*>(sm.djump + 2 * kTrajMaxOps);
     sm.dflag = sm.dmode + 2 * kTrajMaxOps;
@@ -459,7 +483,7 @@ __global__ void __launch_bounds__(kTrajThreads) traj_run_kernel(cplx<T>* __restr
                     sm.djump[c] = T(0);
                 }
                 for (int c = tid; c < nwarps * 2 * nops; c += nthr)
-                    sm.chw_w[size_t(c / (2 * nops)) * (2 * kTrajMaxOps) + (c % (2 * nops))] = 0.0;
+                    wacc_zero(sm.chw_w[size_t(c / (2 * nops)) * (2 * kTrajMaxOps) + (c % (2 * nops))]);
                 __syncthreads();
                 if (tid == 0)
                     for (int q = 0; q < s_njump; ++q) {
@@ -488,7 +512,7 @@ __global__ void __launch_bounds__(kTrajThreads) traj_run_kernel(cplx<T>* __restr
                 // the weights, summed over the warps in a fixed order
                 for (int c = tid; c < 2 * nops; c += nthr) {
                     double x = 0.0;
-                    for (int wp = 0; wp < nwarps; ++wp) x += sm.chw_w[size_t(wp) * (2 * kTrajMaxOps) + c];
+                    for (int wp = 0; wp < nwarps; ++wp) x += wacc_value(sm.chw_w[size_t(wp) * (2 * kTrajMaxOps) + c]);
                     chw[c] = x;
                 }
                 __syncthreads();

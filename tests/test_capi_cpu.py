@@ -142,6 +142,7 @@ def test_adjoint_sweep_host_validation(lib):
     assert call(sweep(pos=(5, 0))) == -1  # the tile has 5 bits
     assert call(sweep(), n=4) == -1  # tile wider than the state
     assert call(sweep(out=0, val=((0.5, 0), (1, 0)))) == -1 and b"Pauli" in lib.qgb_last_error()
+    assert call(sweep(out=0, col=(1, 1))) == -1 and b"permutation" in lib.qgb_last_error()  # rows share a column
     assert call(sweep(out=0)) == -4  # derivative wanted, no scratch
     assert call(sweep(out=0), out=None) == -1
     assert lib.qgb_adjoint_sweep_step(A, A + 64, 0, 10, C.byref(sweep()), M, 0, 1, 0, None, None, 0, None) == -1
