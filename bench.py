@@ -601,6 +601,11 @@ def section_adjoint_batch(n=20, layers=40, sets=64, single_sample=8):
             "energy_diff_vs_autograd_set0": abs(float(E[0]) - float(e_ref.item()))}
 
 
+def _is_diagonal(g):
+    m = np.asarray(g.matrix)
+    return bool(np.all(m == np.diag(np.diag(m))))
+
+
 def section_trajectories(n=20, ntraj=1024, steps=40):
     """1024 noisy TFI Trotter trajectories (depolarising 1e-3 + amplitude damping 5e-4
     after every gate): the persistent launch (default, one kernel for the whole
@@ -629,6 +634,18 @@ def section_trajectories(n=20, ntraj=1024, steps=40):
                       "hbm_algorithmic_tb": round(alg / 1e12, 3),
                       "hbm_frac": round(alg / (ms / 1e3) / 1e9 / peak, 3),
                       "shared_memory_passes_per_trajectory": ng})
+            # the FP32 pipe's share: gate products per amplitude (a dense k-site gate 2^k complex
+            # multiply-adds, a diagonal one a complex product: 8 flops each) plus the damping
+            # channel per gate site (its K0 scaling and |1> weight: 4 flops per amplitude)
+            flops_amp = sum(8 * (1 if _is_diagonal(g) else 2 ** len(g.indices)) + 4 * len(g.indices)
+                            for g in circ.gate_list)
+            fl = flops_amp * 2 ** n * ntraj
+            fp32 = fma_peaks()["fp32_tflops"]
+            r["fp32"] = {"flops_per_amplitude": flops_amp, "achieved_tflops": round(fl / (ms / 1e3) / 1e12, 2),
+                         "peak_tflops": fp32, "frac": round(fl / (ms / 1e3) / 1e12 / fp32, 3),
+                         "peak_source": "qgb_fma_probe float32 FMA rate measured in this run",
+                         "counting": "8 flops per complex multiply-add of the gate products, "
+                                     "4 per amplitude and site for the damping channel; jumps' re-runs not counted"}
         else:
             alg = ng * 2 * ntraj * 2 ** n * 8
             r.update({"hbm_algorithmic_tb": round(alg / 1e12, 2), "hbm_frac": round(alg / (ms / 1e3) / 1e9 / peak, 3)})

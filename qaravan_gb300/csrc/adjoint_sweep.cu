@@ -12,8 +12,8 @@
 // one register pass),
 //   * for a rotation exp(-i theta P) whose derivative is wanted: adds
 //     Im sum conj(lam) (P phi) over the tile's groups (float partial per
-//     thread, a fixed xor-shuffle tree per warp, a float64 accumulator per
-//     (op, warp) in shared memory);
+//     thread, a fixed xor-shuffle tree per warp, a compensated float
+//     accumulator per (op, warp) in shared memory -- float64 for complex128);
 //   * applies U^dagger to both tiles.
 // Work is split into chunks of consecutive tiles, each inside one state; a
 // chunk's accumulators are summed over the warps in order and stored as one
@@ -78,7 +78,7 @@ constexpr int kAdjMaxRun = 4;  // consecutive ops on the same sites handled in o
 template <typename T, int K, int R>
 __device__ __forceinline__ void adj_tile_run(cplx<T>* __restrict__ pt, cplx<T>* __restrict__ lt, int m,
                                              const AdjSweepArgs& a, int op0, const cplx<T>* __restrict__ ush,
-                                             double* __restrict__ red, int tid, int nthr) {
+                                             typename WAccOf<T>::type* __restrict__ red, int tid, int nthr) {
     constexpr int D = 1 << K;
     using C = cplx<T>;
     int pos[K], srt[K];
@@ -248,7 +248,7 @@ __device__ __forceinline__ void adj_tile_run(cplx<T>* __restrict__ pt, cplx<T>* 
             T v = s[q];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if ((tid & 31) == 0) red[(op0 + q) * kAdjMaxWarps + (tid >> 5)] += double(v);
+            if ((tid & 31) == 0) wacc_add(red[(op0 + q) * kAdjMaxWarps + (tid >> 5)], v);
         }
     }
 }
@@ -526,7 +526,7 @@ template <typename T, int R>
 __device__ __forceinline__ void adj_tile_runs(cplx<T>* __restrict__ pt, cplx<T>* __restrict__ lt, int m,
                                               const AdjSweepArgs& a, const cplx<T>* __restrict__ ush,
                                               const uint8_t* __restrict__ umode, const uint8_t* __restrict__ ucol,
-                                              double* __restrict__ red, int tid, int nthr) {
+                                              typename WAccOf<T>::type* __restrict__ red, int tid, int nthr) {
     using C = cplx<T>;
     constexpr int D = 1 << R;
     const int warp = tid >> 5, lane = tid & 31;
@@ -579,7 +579,7 @@ __device__ __forceinline__ void adj_tile_runs(cplx<T>* __restrict__ pt, cplx<T>*
                 if (want) {  // uniform over the CTA: every lane reaches the shuffles
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) sd += __shfl_xor_sync(0xffffffffu, sd, o);
-                    if (lane == 0) red[op * kAdjMaxWarps + warp] += double(sd);
+                    if (lane == 0) wacc_add(red[op * kAdjMaxWarps + warp], sd);
                 }
             }
             if (ok) {
@@ -606,7 +606,7 @@ __device__ __forceinline__ int adj_run_length(const AdjSweepArgs& a, int op0) {
 
 template <typename T, int K>
 __device__ __forceinline__ int adj_tile_ops(cplx<T>* pt, cplx<T>* lt, int m, const AdjSweepArgs& a, int op0,
-                                            const cplx<T>* ush, double* red, int tid, int nthr) {
+                                            const cplx<T>* ush, typename WAccOf<T>::type* red, int tid, int nthr) {
     // longest run kept in registers without spilling under the 512-thread register cap
     constexpr int kMax = sizeof(T) == 4 ? (K == 1 ? 4 : 2) : (K == 1 ? 2 : 1);
     int r = adj_run_length(a, op0);
@@ -632,11 +632,11 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 256 : kAdjMaxThreads, sizeof(
     const int L = a.L, H = a.H, m = a.m;
     const int nwarps = blockDim.x >> 5;
     // layout: nbuf x (phi tile, lam tile) | ush (n_ops x 16 complex: U^dagger of the current state) |
-    //         hoff (2^H uint64) | red (n_ops x kAdjMaxWarps double) | umode (n_ops) | ucol (n_ops x 4)
+    //         hoff (2^H uint64) | red (n_ops x kAdjMaxWarps accumulators, 8 bytes) | umode (n_ops) | ucol (n_ops x 4)
     C* bufs = reinterpret_cast<C*>(smem_raw);
     C* ush = bufs + (size_t(2 * nbuf) << m);
     uint64_t* hoff = reinterpret_cast<uint64_t*>(ush + size_t(a.n_ops) * 16);
-    double* red = reinterpret_cast<double*>(hoff + (size_t(1) << H));
+    auto* red = reinterpret_cast<typename WAccOf<T>::type*>(hoff + (size_t(1) << H));
     uint8_t* umode = reinterpret_cast<uint8_t*>(red + size_t(a.n_ops) * kAdjMaxWarps);
     uint8_t* ucol = umode + a.n_ops;
     int64_t staged = -1;  // state whose matrices sit in ush
@@ -645,7 +645,7 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 256 : kAdjMaxThreads, sizeof(
         for (int j = 0; j < H; ++j) o |= uint64_t((h >> j) & 1u) << a.high_bits[j];
         hoff[h] = o;
     }
-    for (int i = threadIdx.x; i < a.n_ops * kAdjMaxWarps; i += blockDim.x) red[i] = 0.0;
+    for (int i = threadIdx.x; i < a.n_ops * kAdjMaxWarps; i += blockDim.x) wacc_zero(red[i]);
     __syncthreads();
     const uint32_t lmask = (1u << L) - 1;
     constexpr uint32_t per16 = 16 / sizeof(C);
@@ -749,11 +749,11 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 256 : kAdjMaxThreads, sizeof(
             const uint64_t chunk = w / a.chunk_tiles;
             for (int op = threadIdx.x; op < a.n_ops; op += blockDim.x) {
                 if (a.op_out[op] < 0) continue;
-                double* row = red + op * kAdjMaxWarps;
+                auto* row = red + op * kAdjMaxWarps;
                 double t = 0.0;
                 for (int wp = 0; wp < nwarps; ++wp) {
-                    t += row[wp];
-                    row[wp] = 0.0;
+                    t += wacc_value(row[wp]);
+                    wacc_zero(row[wp]);
                 }
                 partials[chunk * a.n_ops + op] = t;
             }

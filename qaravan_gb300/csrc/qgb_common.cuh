@@ -84,6 +84,33 @@ __device__ __forceinline__ uint64_t scatter_bits(uint64_t v, const int* bits, in
 }
 
 // Offset of matrix row/column r in the state: bit (k-1-j) of r goes to bit pos[j].
+// Accumulators of many float partial sums kept on the FP32 pipe: a float sum with
+// its compensation term (Kahan summation: the error stays at a few float
+// roundings of the summed magnitudes, however many terms), and float64 for
+// double data. GB300's FP64 pipe is narrow: a float64 add per warp and op in an
+// inner loop stalls the warps that issue it.
+struct WAccF {
+    float s, c;
+};
+template <typename T> struct WAccOf { using type = double; };
+template <> struct WAccOf<float> { using type = WAccF; };
+static_assert(sizeof(WAccF) == sizeof(double), "accumulator layout");
+
+__device__ __forceinline__ void wacc_add(double& a, double v) { a += v; }
+__device__ __forceinline__ void wacc_add(WAccF& a, float v) {
+    const float y = __fsub_rn(v, a.c);
+    const float t = __fadd_rn(a.s, y);
+    a.c = __fsub_rn(__fsub_rn(t, a.s), y);
+    a.s = t;
+}
+__device__ __forceinline__ double wacc_value(const double& a) { return a; }
+__device__ __forceinline__ double wacc_value(const WAccF& a) { return double(a.s) - double(a.c); }
+__device__ __forceinline__ void wacc_zero(double& a) { a = 0.0; }
+__device__ __forceinline__ void wacc_zero(WAccF& a) {
+    a.s = 0.f;
+    a.c = 0.f;
+}
+
 __host__ __device__ __forceinline__ uint64_t matrix_offset(int r, const int* pos, int k) {
     uint64_t off = 0;
     for (int j = 0; j < k; ++j) off |= uint64_t((r >> (k - 1 - j)) & 1) << pos[j];

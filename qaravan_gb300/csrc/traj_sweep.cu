@@ -201,29 +201,9 @@ __device__ __forceinline__ void reg_damp_at(C (&v)[1 << R], int P, int mode, T s
     }
 }
 
-// Per-warp accumulators of the damping weights: for complex64 a float sum with its
-// compensation term (Kahan summation on the FP32 pipe, the weights' own float
-// precision kept over any number of tiles -- a float64 add per warp, op and tile
-// kept GB300's narrow FP64 pipe 38 % busy); for complex128 a double.
-struct WAccF {
-    float s, c;
-};
-template <typename T> struct WAccOf { using type = double; };
-template <> struct WAccOf<float> { using type = WAccF; };
-static_assert(sizeof(WAccF) == sizeof(double), "weight accumulator layout");
-
-__device__ __forceinline__ void wacc_add(double& a, double v) { a += v; }
-__device__ __forceinline__ void wacc_add(WAccF& a, float v) {
-    const float y = __fsub_rn(v, a.c);
-    const float t = __fadd_rn(a.s, y);
-    a.c = __fsub_rn(__fsub_rn(t, a.s), y);
-    a.s = t;
-}
-__device__ __forceinline__ double wacc_value(const double& a) { return a; }
-__device__ __forceinline__ double wacc_value(const WAccF& a) { return double(a.s) - double(a.c); }
-__device__ __forceinline__ void wacc_zero(double& a) { a = 0.0; }
-__device__ __forceinline__ void wacc_zero(WAccF& a) { a.s = 0.f; a.c = 0.f; }
-
+// Per-warp accumulators of the damping weights (WAccOf, qgb_common.cuh): for
+// complex64 a compensated float sum -- a float64 add per warp, op and tile kept
+// GB300's narrow FP64 pipe 38 % busy -- for complex128 a double.
 // Per-sweep, per-trajectory state in dynamic shared memory.
 template <typename T> struct TrajSweepSmem {
     cplx<T>* msh;     // [op][16]: the op's matrix with its sampled Paulis folded in (first op: times the prescale)
