@@ -8,6 +8,7 @@ reference / measured trace. These tests check which cuts the compiler marks as
 whole, which op sequences keep the trace, and the order of the executor's
 calls (the library replaced by a recorder, so no kernel runs)."""
 import numpy as np
+import pytest
 import torch
 
 from qaravan_gb300 import _lib, engine, workloads
@@ -144,3 +145,27 @@ def test_executor_trace_chain_off_on_cuda_cores_or_when_disabled(monkeypatch):
     p.trace_kept = False
     names = [n for n, _ in _run(monkeypatch, p)]
     assert "qgb_dm_trace_factor" not in names
+
+
+def test_superoperator_cache_gives_the_same_ops_read_only():
+    """Noise carriers of one op sequence share a superoperator built once per
+    (noise model, time, decoupling flag, site order): the ops equal the ones
+    built carrier by carrier, and the shared matrix cannot be written."""
+    from qaravan_gb300.gates import ID
+    from qaravan_gb300.noise import QubitNoise, depolarizing
+    n = 4
+    chans = [depolarizing(0.02), QubitNoise(80.0, 60.0, 1.0, 5.0)]
+    from qaravan_gb300.noise import PauliNoise
+    carriers = [ID(2, 1.0, [q], nm=ch) for q in range(n) for ch in chans] + \
+               [ID(2, 5.0, [q], nm=chans[1]) for q in range(n)] + \
+               [ID(2, 1.0, [3, 1], nm=PauliNoise(["ii", "xz", "yy"], [0.97, 0.02, 0.01]))]  # unsorted sites
+    cache: dict = {}
+    shared = [o for g in carriers for o in dm_ops_for_gate(g, n, cache)]
+    fresh = [o for g in carriers for o in dm_ops_for_gate(g, n)]
+    assert len(shared) == len(fresh)
+    for a, b in zip(shared, fresh):
+        assert a.bits == b.bits and a.kind == b.kind == "channel"
+        assert np.array_equal(a.matrix, b.matrix)
+    assert len(cache) == 4  # depolarising, T1/T2 at two gate times, the two-site Pauli channel
+    with pytest.raises(ValueError):
+        shared[0].matrix[0, 0] = 0.0
