@@ -131,38 +131,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
     float f_in = 0.f, f_out = 0.f;
     int n_in = 0, n_out = 0;
 
-    // B operand: W = [[Mr, Mi], [-Mi, Mr]] in (output, input) memory order, scaled by 2^sw, split hi/lo.
+    // B operand: W = [[Mr, Mi], [-Mi, Mr]] in (output, input) memory order, scaled by 2^sw, split hi/lo;
+    // a chain's correction 1 + g (|g| ~ 1e-7) goes into W (w + w g in one rounding), which the split
+    // then carries like any other matrix value
     if (tid == 0) wmax_bits = 0;
     __syncthreads();
-    {
-        float m = 0.f;
-        for (int p = tid; p < D * D; p += kTcThreads) {
-            const float2 e = op[p];
-            m = fmaxf(m, fmaxf(fabsf(e.x), fabsf(e.y)));
-        }
-        atomicMax(&wmax_bits, __float_as_uint(m));
-    }
-    __syncthreads();
-    const int sw = scale_exp(__uint_as_float(wmax_bits));
-    const float wscale = exp2i(sw), wunscale = exp2i(-sw);
-    for (int p = tid; p < D * D; p += kTcThreads) {
-        const int i = p / D, j = p - (p / D) * D;
-        const float2 m = op[a.perm_out[i] * D + a.perm_in[j]];
-        float w[4] = {m.x * wscale, -m.y * wscale, m.y * wscale, m.x * wscale};  // (2i,2j) (2i,2j+1) (2i+1,2j) (2i+1,2j+1)
-        if (MODE != 1 && gcorr != 0.f) {
-            // a chain's correction 1 + g (|g| ~ 1e-7) goes into W: w + w g in one rounding; the
-            // hi/lo split then carries it like any other matrix value
-#pragma unroll
-            for (int e = 0; e < 4; ++e) w[e] = fmaf(w[e], gcorr, w[e]);
-        }
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            const uint32_t o = b_off(2 * i + (e >> 1), 2 * j + (e & 1), R);
-            const __half hi = __float2half_rn(w[e]);
-            *reinterpret_cast<__half*>(Bhi + o) = hi;
-            *reinterpret_cast<__half*>(Blo + o) = __float2half_rn(w[e] - __half2float(hi));
-        }
-    }
+    const int sw = tc_build_w<K, kTcThreads>(Bhi, Blo, op, a.perm_out, a.perm_in, MODE != 1 ? gcorr : 0.f,
+                                             &wmax_bits, tid);
+    const float wunscale = exp2i(-sw);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem_u32(&tmem_slot)),

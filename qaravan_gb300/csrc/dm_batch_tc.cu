@@ -224,34 +224,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) dm_batch_tc_kernel(const __grid
             }
             if (tid == 0) wmax_bits = 0;
             __syncthreads();
-            {
-                float m = 0.f;
-                for (int p = tid; p < D * D; p += kTcThreads) {
-                    const float2 e = P.mat[p];
-                    m = fmaxf(m, fmaxf(fabsf(e.x), fabsf(e.y)));
-                }
-                atomicMax(&wmax_bits, __float_as_uint(m));
-            }
-            __syncthreads();
-            const int sw = scale_exp(__uint_as_float(wmax_bits));
-            const float wscale = exp2i(sw);
+            const int sw = tc_build_w<K, kTcThreads>(Bhi, Blo, P.mat, sA.perm_out, sA.perm_in, gcorr, &wmax_bits, tid);
             if (tid == 0) wunscale_s = exp2i(-sw);
-            for (int p = tid; p < D * D; p += kTcThreads) {
-                const int i = p / D, j = p - (p / D) * D;
-                const float2 mv = P.mat[sA.perm_out[i] * D + sA.perm_in[j]];
-                float w[4] = {mv.x * wscale, -mv.y * wscale, mv.y * wscale, mv.x * wscale};
-                if (gcorr != 0.f) {
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) w[e] = fmaf(w[e], gcorr, w[e]);
-                }
-#pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const uint32_t o = b_off(2 * i + (e >> 1), 2 * j + (e & 1), R);
-                    const __half hi = __float2half_rn(w[e]);
-                    *reinterpret_cast<__half*>(Bhi + o) = hi;
-                    *reinterpret_cast<__half*>(Blo + o) = __float2half_rn(w[e] - __half2float(hi));
-                }
-            }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             cur_pass = it.pass;
             __syncthreads();

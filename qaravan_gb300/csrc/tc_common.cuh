@@ -174,6 +174,69 @@ __device__ __forceinline__ void split_f16(float a, float b, uint32_t& hi, uint32
     lo = *reinterpret_cast<const uint32_t*>(&l);
 }
 
+// The B operand W = [[Mr, Mi], [-Mi, Mr]] of a 2^K x 2^K complex op (rows in
+// output memory order perm_out, columns in input order perm_in), scaled by the
+// power of two 2^sw that brings its largest entry into [2^14, 2^15), times
+// 1 + gcorr when gcorr != 0, split into fp16 hi and lo planes in the K-major
+// core-matrix layout of b_off. All nthr threads of the CTA take part (two
+// CTA barriers inside; *wmax_bits must be zero and visible to all threads on
+// entry). Each thread loads all its entries before using any -- one round of
+// L2 latency instead of one per entry -- and writes whole 16-byte core-matrix
+// rows (8 fp16 of one row); the values are those of an entry-by-entry build.
+// Returns sw.
+template <int K, int NTHR>
+__device__ __forceinline__ int tc_build_w(unsigned char* Bhi, unsigned char* Blo, const float2* __restrict__ op,
+                                          const int* perm_out, const int* perm_in, float gcorr,
+                                          uint32_t* wmax_bits, int tid) {
+    constexpr int D = 1 << K, R = 2 * D;
+    constexpr int NI = D * (D / 4);               // (complex row i, group c of 4 complex columns)
+    constexpr int IT = (NI + NTHR - 1) / NTHR;
+    float2 v[IT][4];
+    float m = 0.f;
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+        const int q = tid + it * NTHR;
+        if (q < NI) {
+            const int i = q & (D - 1), c = q >> K;
+            const float2* row = op + perm_out[i] * D;
+#pragma unroll
+            for (int t = 0; t < 4; ++t) v[it][t] = row[perm_in[4 * c + t]];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) m = fmaxf(m, fmaxf(fabsf(v[it][t].x), fabsf(v[it][t].y)));
+        }
+    }
+    atomicMax(wmax_bits, __float_as_uint(m));
+    __syncthreads();
+    const int sw = scale_exp(__uint_as_float(*wmax_bits));
+    const float wscale = exp2i(sw);
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+        const int q = tid + it * NTHR;
+        if (q < NI) {
+            const int i = q & (D - 1), c = q >> K;
+            uint32_t h0[4], l0[4], h1[4], l1[4];  // real rows 2i (Mr, -Mi) and 2i + 1 (Mi, Mr)
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                float w[4] = {v[it][t].x * wscale, -v[it][t].y * wscale, v[it][t].y * wscale, v[it][t].x * wscale};
+                if (gcorr != 0.f) {
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) w[e] = fmaf(w[e], gcorr, w[e]);
+                }
+                split_f16(w[0], w[1], h0[t], l0[t]);
+                split_f16(w[2], w[3], h1[t], l1[t]);
+            }
+            // b_off(n, 8 c, R): the core-matrix row of real row n and columns 8c .. 8c + 7
+            const uint32_t o0 = uint32_t((c >> 1) * (R * 32) + ((2 * i) >> 3) * 256 + (c & 1) * 128 + ((2 * i) & 7) * 16);
+            const uint32_t o1 = o0 + 16;  // row 2i + 1: the next row of the same core matrix
+            *reinterpret_cast<uint4*>(Bhi + o0) = make_uint4(h0[0], h0[1], h0[2], h0[3]);
+            *reinterpret_cast<uint4*>(Blo + o0) = make_uint4(l0[0], l0[1], l0[2], l0[3]);
+            *reinterpret_cast<uint4*>(Bhi + o1) = make_uint4(h1[0], h1[1], h1[2], h1[3]);
+            *reinterpret_cast<uint4*>(Blo + o1) = make_uint4(l1[0], l1[1], l1[2], l1[3]);
+        }
+    }
+    return sw;
+}
+
 __device__ __forceinline__ uint64_t b_desc(uint32_t addr) {
     return uint64_t((addr & 0x3FFFFu) >> 4) | (uint64_t(128 >> 4) << 16) | (uint64_t(256 >> 4) << 32) | (1ull << 46);
 }
