@@ -141,3 +141,20 @@ def test_fused_forward_matches_per_gate_forward(dtype, tol):
         e1, g1 = (t.cpu().numpy() for t in ba.energy_and_grad(x, terms))
         assert np.max(np.abs(e1 - e0)) < tol * np.max(np.abs(e0)) * 10
         assert np.max(np.abs(g1 - g0)) / np.max(np.abs(g0)) < tol
+
+
+def test_large_tiles_single_cta_launch():
+    """12-bit tiles of both vectors (128 KiB of shared memory: one CTA per SM,
+    256 threads for complex64) against one pass per gate."""
+    from qaravan_gb300 import workloads
+    from qaravan_gb300.adjoint import BatchedAnsatz
+    n, layers, P = 14, 2, 3
+    terms = _tfi_terms(n)
+    x = np.stack([workloads.hea_params(n, layers, 40 + s).reshape(-1) for s in range(P)])
+    base = BatchedAnsatz.hea(n, layers)
+    e0, g0 = (t.cpu().numpy() for t in BatchedAnsatz(n, base.gates, nparams=base.nparams, tile_bits=0)
+              .energy_and_grad(x, terms))
+    e1, g1 = (t.cpu().numpy() for t in BatchedAnsatz(n, base.gates, nparams=base.nparams, tile_bits=12)
+              .energy_and_grad(x, terms))
+    assert np.max(np.abs(e1 - e0)) < 1e-5
+    assert np.max(np.abs(g1 - g0)) / np.max(np.abs(g0)) < 2e-5
