@@ -107,6 +107,26 @@ __global__ void __launch_bounds__(kTcThreads, 1) dense_tc_kernel(float2* __restr
     if constexpr (MODE == 0) {
         // a factor f ~ 1 (the trace chain of density matrices): folded into W as w + w (f - 1)
         if (a.scale) gcorr = float(*a.scale - 1.0);
+        // the norm chain's later epochs open with this mode (no per-tile work): scale by
+        // sqrt(ref / out_prev) and carry the reference on; an epoch that has an output norm
+        // but no reference (the buffer was cleared mid-chain) restarts the chain from that norm
+        if (a.chain && a.c_head) {
+            double chain_ref = 0.0;
+            if (a.c_prev >= 0) {
+                const double ref = a.chain[2 * a.c_prev], out = a.chain[2 * a.c_prev + 1];
+                if (ref > 0.0 && out > 0.0) {
+                    chain_ref = ref;
+                    gcorr = float(sqrt(ref / out) - 1.0);
+                } else if (out > 0.0) {
+                    chain_ref = out;
+                }
+            }
+            if (blockIdx.x == 0 && tid == 0) {
+                a.chain[2 * a.c_next] = 0.0;
+                a.chain[2 * a.c_next + 1] = 0.0;
+                a.chain[2 * a.c_cur] = chain_ref;
+            }
+        }
     }
     if constexpr (MODE == 2) {
         if (a.c_head) {
@@ -681,13 +701,17 @@ int try_dense_tc(void* sv, const void* op, int nbits, const int* sorted, const i
         a.c_prev = e > 0 ? (e - 1) % 3 : -1;
         a.c_cur = e % 3;
         a.c_next = (e + 1) % 3;
-        if (a.c_head || a.c_tail) {
+        // the chain's first pass measures its input and every epoch's last pass its output
+        // (MODE 2, sums of squares per tile); the other epochs open in MODE 0, which folds
+        // the correction into the matrix only
+        if ((a.c_head && e == 0) || a.c_tail) {
             switch (k) {
                 case 4: return launch_tc<4, 2>(s, m, a, st);
                 case 5: return launch_tc<5, 2>(s, m, a, st);
                 default: return launch_tc<6, 2>(s, m, a, st);
             }
         }
+        if (!a.c_head) a.chain = nullptr;  // a pass inside an epoch: no chain work at all
         unitary = 0;
     }
     switch (k) {
