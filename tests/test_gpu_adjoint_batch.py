@@ -22,7 +22,6 @@ def _tfi_terms(n):
 
 
 def test_device_param_matrices_match_param_gates():
-    from qaravan_gb300 import _lib
     from qaravan_gb300.adjoint import BatchedAnsatz
     from qaravan_gb300.gates import RX, RXX, RY, RYY, RZ, RZZ
     gates = [("RX", [0], 0), ("RY", [1], 1), ("RZ", [2], 2), ("RXX", [0, 1], 3), ("RYY", [1, 2], 4), ("RZZ", [2, 0], 5)]

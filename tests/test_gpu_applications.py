@@ -41,7 +41,6 @@ def test_trotter_sv_sim_matches_oracle():
 
 def test_trotter_dm_sim_cached_and_uncached_match_oracle():
     from qaravan_gb300.applications import magnetization, trotter_dm_sim, trotter_dm_sim_uncached
-    from qaravan_gb300.circuits import Circuit
     from qaravan_gb300.hamiltonians import TFI
     from qaravan_gb300.noise import PauliNoise
     n, dt, steps = 4, 0.1, 4

@@ -5,7 +5,6 @@ left/right sweeps of environment_state_prep (cost after every update and the
 final gate matrices)."""
 import numpy as np
 import pytest
-import torch
 
 from oracle import ref
 

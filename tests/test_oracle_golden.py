@@ -1,6 +1,5 @@
 """Pin the CPU oracle (oracle/ref.py) to fixtures produced by the real reference."""
 import numpy as np
-import pytest
 
 from conftest import golden
 from gateio import unpack_gates
