@@ -547,9 +547,12 @@ class BatchedAnsatz:
     ``qgb_adjoint_step_batched`` for a fixed gate) carries all sets together;
     ``qgb_param_grads`` sums the derivatives of the gates of each parameter.
     With ``tile_bits`` > 0 (the default) both directions run as tile passes,
-    many gates per read of the states: the forward through ``qgb_apply_sweep``
-    with every set's own matrices, the reverse through
-    ``qgb_adjoint_sweep_step``; ``tile_bits=0`` runs one pass per gate.
+    many gates per read of the states: the forward as blocks of
+    ``fused_width`` qubits (default 4) composed per set on the device and
+    applied through ``qgb_apply_sweep`` with every set's own block matrices
+    (``fused_width=0``, or very many sets of small states: one op per gate),
+    the reverse through ``qgb_adjoint_sweep_step``; ``tile_bits=0`` runs one
+    pass per gate.
     Memory: three states per set."""
 
     def __init__(self, n, gates, nparams=None, dtype=torch.complex64, device="cuda", tile_bits=None,
@@ -614,14 +617,25 @@ class BatchedAnsatz:
                 self._fused["template_dev"] = torch.from_numpy(self._fused["template"]).to(self.device)
                 self._fused["sweep_structs"] = [_forward_sweep_struct_pos(lo, high, ops)
                                                 for lo, high, ops in self._fused["sweeps"]]
-            if self._fused is None:
-                fwd_tile = min(self.tile_bits + 1, self.n)  # one state only: twice the tile of the reverse pass
-                for lo, high, ops in _plan_reverse([(g, bits[g]) for g in range(len(bits))], self.n, fwd_tile):
-                    self._fwd.append(_forward_sweep_struct(lo, high, [(b, g * 16) for g, b in ops]))
+            # one tile-pass op per gate: the forward without fusion, and the fallback for very many sets
+            fwd_tile = min(self.tile_bits + 1, self.n)  # one state only: twice the tile of the reverse pass
+            for lo, high, ops in _plan_reverse([(g, bits[g]) for g in range(len(bits))], self.n, fwd_tile):
+                self._fwd.append(_forward_sweep_struct(lo, high, [(b, g * 16) for g, b in ops]))
             tile = min(self.tile_bits, self.n)
             for lo, high, ops in _plan_reverse([(g, bits[g]) for g in reversed(range(len(bits)))], self.n, tile):
                 self._rev.append(_adjoint_sweep_struct(lo, high, [(b, g * 16, g if kinds[g] else -1, kinds[g])
                                                                   for g, b in ops]))
+
+    def _use_fused(self, P):
+        """Whether ``P`` sets take the fused forward: it composes every set's blocks
+        from the sets' complex128 gate matrices (256 bytes per gate and set), a
+        buffer kept at most 2 GiB or the size of the states themselves -- for very
+        many sets of small states the per-gate forward runs instead."""
+        if self._fused is None:
+            return False
+        need = P * len(self.gates) * 256
+        states = P * (2 ** self.n) * torch.empty(0, dtype=self.dtype).element_size()
+        return need <= max(1 << 31, states)
 
     def _fused_tables(self, P):
         """Device copy of the fused forward's tables for ``P`` sets (kept for the
@@ -693,7 +707,7 @@ class BatchedAnsatz:
         _lib.check(L.qgb_init_basis(psi.data_ptr(), self.code, n, 0, P, N, st), "init")
         base = mats.data_ptr()
         set_stride = 16 * len(self.gates)
-        if self._fused is not None:
+        if self._use_fused(P):
             self._forward_fused(psi, params, P, st)
         elif self._fwd:
             for sw in self._fwd:

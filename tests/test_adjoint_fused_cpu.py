@@ -93,3 +93,18 @@ def test_fused_forward_tables_replay(n, layers, width, nsets):
         for gt in gates:
             exp = ref.op_action(_gate_matrix(gt, params[s]), gt[1], exp)
         assert np.max(np.abs(sv - exp)) < 1e-12
+
+
+def test_fused_forward_only_while_its_matrix_buffer_stays_small():
+    """The fused forward keeps every set's complex128 gate matrices (256 bytes per
+    gate and set): at most 2 GiB, or the states' own size."""
+    import torch
+    from qaravan_gb300.adjoint import BatchedAnsatz
+    ba = BatchedAnsatz.__new__(BatchedAnsatz)  # host fields only: no device needed
+    ba._fused, ba.gates, ba.dtype = {"blocks": 1}, [None] * 2360, torch.complex64
+    ba.n = 20
+    assert ba._use_fused(64) and ba._use_fused(4096)
+    ba.n = 10
+    assert ba._use_fused(1024) and not ba._use_fused(65535)
+    ba._fused = None
+    assert not ba._use_fused(1)
