@@ -485,15 +485,17 @@ def plan_fused_forward(n, gate_bits, fixed, width, itemsize):
     out [set][gate][16]. Returns the tables of one set -- ``blocks1`` (block
     matrix at element ``out`` of the set's ``total``), ``ents1`` (gate g's matrix
     at element 16 g) -- and the sweeps as (low bits, high bits, [(tile positions,
-    block offset)]), or None when the plan is not all device-fused tile sweeps."""
+    block offset)]), or None when the plan is not all device-fused tile sweeps
+    (blocks wider than the sweep kernels take: 5 qubits for complex64, 4 for
+    complex128)."""
     from .compiler import Recipe, SweepStep
     from .engine import _FUSE_BLOCK, _FUSE_ENTRY
     G = len(gate_bits)
     fixed_m = dict(fixed)
     ops = [Op(gate_bits[g], fixed_m[g] if g in fixed_m else np.eye(2 ** len(gate_bits[g]), dtype=np.complex128))
            for g in range(G)]
-    plan = compile_ops(ops, n, mode="sweep", width=width, tile_bits=13, max_sweep_k=min(width, 4),
-                       itemsize=itemsize, device_fusion=True)
+    plan = compile_ops(ops, n, mode="sweep", width=width, tile_bits=13,
+                       max_sweep_k=min(width, 5 if itemsize <= 8 else 4), itemsize=itemsize, device_fusion=True)
     if not plan.matrices or not all(isinstance(m, Recipe) for m in plan.matrices) or \
             not all(isinstance(st, SweepStep) for st in plan.steps):
         return None

@@ -49,7 +49,8 @@ def _embed(m, pos, k):
     return e
 
 
-@pytest.mark.parametrize("n,layers,width,nsets", [(9, 3, 3, 3), (14, 2, 3, 2), (15, 2, 4, 2)])
+@pytest.mark.parametrize("n,layers,width,nsets", [(9, 3, 3, 3), (14, 2, 3, 2), (15, 2, 4, 2), (10, 2, 2, 2),
+                                                  (13, 2, 5, 1)])
 def test_fused_forward_tables_replay(n, layers, width, nsets):
     from qaravan_gb300.adjoint import fused_tables, plan_fused_forward
     from qaravan_gb300.engine import _FUSE_BLOCK, _FUSE_ENTRY
@@ -59,6 +60,7 @@ def test_fused_forward_tables_replay(n, layers, width, nsets):
     fixed = [(g, gt[2]) for g, gt in enumerate(gates) if gt[0] == "fixed"]
     fplan = plan_fused_forward(n, bits, fixed, width, 8)
     assert fplan is not None and fplan["blocks"] < G
+    assert plan_fused_forward(n, bits, fixed, 6, 8) is None  # wider than the complex64 sweeps take
     host, ent_start = fused_tables(fplan, nsets, G)
     nb = nsets * len(fplan["blocks1"])
     blocks = host[:nb * _FUSE_BLOCK.itemsize].view(_FUSE_BLOCK)

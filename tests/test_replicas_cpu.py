@@ -62,3 +62,15 @@ def test_reference_arm_prints_from_rank_zero_only():
     assert len(lines[0]) == 1 and lines[1] == []
     rec = json.loads(lines[0][0])
     assert rec["impl"] == "reference" and rec["value"] > 0 and rec["cpu_baseline"]["kind"] in ("port", "reference")
+
+
+def test_cpu_baseline_is_the_reference_arm_in_a_child_process():
+    """The bench line's cpu_baseline comes from the reference arm run as a fresh
+    process (the same measurement as `bench.py --impl reference`), plus the numpy
+    complex128 and 12-qubit figures measured in place."""
+    import bench
+    gates = bench.workload_gates(14, 1)
+    out = bench.cpu_baseline(gates, 14, 1)
+    assert out["kind"] == "port" and out["unit"] == "gates/s" and out["value"] > 0 and out["cores"] >= 1
+    assert "child process" in out["sample"]
+    assert out["numpy_c128"]["gates_per_s"] > 0 and out["config1_12q_depth20_c128"]["gates"] == 460
